@@ -1,0 +1,410 @@
+#!/usr/bin/env python3
+"""Benchmark: NU points*coils/s for forward+adjoint SENSE NUFFT on one GB300.
+
+Workload (the metric's configuration): 2D SENSE, batch 4, 16 coils, image
+320x320 complex64 N(0,1), grid 640x640, numpoints 6, table_oversamp 1024,
+golden-angle radial trajectory 404 spokes x 640 samples (258,560 points),
+smooth Gaussian-bump coil maps normalised to sum_c |s_c|^2 = 1. Synthetic,
+seeded data (no dataset involved).
+
+A step is one forward NUFFT of the batch followed by one adjoint NUFFT of the
+forward's output; the work of a step is B*C*M points*coils (counted once per
+forward+adjoint pair). Every step touches > 129 MB (the L2 size), so no L2
+flush is inserted between steps.
+
+  value : device-resident inputs, timed with CUDA events around K steps.
+  e2e   : the public API (KbNufft / KbNufftAdjoint modules) with the image in
+          pinned host memory: H2D copy of the image, forward, adjoint, D2H copy
+          of the result image, every step.
+  roofline: algorithmic bytes of the dominant hand-written kernel / its
+          CUDA-event duration, against the measured HBM copy bandwidth.
+  cpu_baseline: the CPU port of the reference table path on a bounded sample.
+
+``--impl reference`` times the CPU port of the reference path (the reference
+is pure Python and cannot run here) on the host cores on the same workload
+definition and prints the same line with ``"impl": "reference"``.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+B, C, N, SPOKES, READ = 4, 16, 320, 404, 640
+METRIC = "NU points*coils/s (forward+adjoint SENSE NUFFT, 2D 320^2, 16 coils, batch 4)"
+UNIT = "points*coils/s"
+
+
+# ---------------------------------------------------------------- workload
+
+
+def golden_angle_traj(spokes: int, readout: int) -> np.ndarray:
+    """(2, spokes*readout) float32, rows (ky, kx), readout endpoint excluded."""
+    ga = np.deg2rad(180.0 / ((1 + np.sqrt(5.0)) / 2))
+    r = np.linspace(-np.pi, np.pi, readout + 1)[:-1]
+    theta = np.arange(spokes) * ga
+    ky = np.sin(theta)[:, None] * r[None, :]
+    kx = np.cos(theta)[:, None] * r[None, :]
+    return np.stack((ky.reshape(-1), kx.reshape(-1))).astype(np.float32)
+
+
+def ring_smaps(ncoil: int, n: int, batch: int, seed: int) -> np.ndarray:
+    """Complex Gaussian bumps centred on a ring (radius 0.35 n, width 0.4 n),
+    a linear phase per coil, normalised so that sum_c |s_c|^2 = 1."""
+    rng = np.random.default_rng(seed)
+    y, x = np.meshgrid(np.arange(n) - n / 2, np.arange(n) - n / 2, indexing="ij")
+    out = np.empty((batch, ncoil, n, n), dtype=np.complex64)
+    for b in range(batch):
+        rot = rng.uniform(0, 2 * np.pi)
+        maps = []
+        for c in range(ncoil):
+            ang = rot + 2 * np.pi * c / ncoil
+            cx, cy = 0.35 * n * np.cos(ang), 0.35 * n * np.sin(ang)
+            mag = np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * (0.4 * n) ** 2))
+            ph = np.exp(1j * (np.pi / n) * (np.cos(ang) * x + np.sin(ang) * y) + 1j * ang)
+            maps.append(mag * ph)
+        maps = np.stack(maps)
+        maps /= np.sqrt(np.sum(np.abs(maps) ** 2, axis=0, keepdims=True))
+        out[b] = maps
+    return out
+
+
+def make_inputs(seed: int = 1002):
+    rng = np.random.default_rng(seed)
+    image = (rng.standard_normal((B, 1, N, N)) + 1j * rng.standard_normal((B, 1, N, N))).astype(np.complex64)
+    return image, ring_smaps(C, N, B, seed + 1), golden_angle_traj(SPOKES, READ)
+
+
+def algorithmic_bytes(M: int):
+    G = 2 * N
+    cb = 8
+    gather = B * C * G * G * cb + B * C * M * cb + 2 * M * 4 + M * 4
+    scatter = B * C * M * cb + B * C * G * G * cb + 2 * M * 4 + M * 4
+    fwd = cb * (B * N * N + B * C * N * N + B * C * G * G + 2 * B * C * G * G + B * C * G * G + B * C * M) + 4 * 2 * M
+    adj = cb * (B * C * M + B * C * G * G + 2 * B * C * G * G + B * C * N * N + B * C * N * N + B * N * N) + 4 * 2 * M
+    return {"gather": gather, "scatter": scatter, "forward": fwd, "adjoint": adj}
+
+
+# ---------------------------------------------------------------- helpers
+
+
+def measured_peak_gbs():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """Per-launch DRAM bytes for `kernel` at this workload, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic_2d_sense_320.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"tkbn_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[4], parts[5:9]))
+                except ValueError:
+                    continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        smax = max(r[1] for r in rows)
+        loaded = [r for r in rows if r[2] > 200.0] or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in loaded for i, v in enumerate(r[4]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(rows), "samples_under_load": len(loaded)}
+
+
+def dist_setup():
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and not dist.is_initialized():
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int, device) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU baseline (port of the reference path)
+
+
+def cpu_sample_run(image, smaps, omega, coils: int, batch: int = 1):
+    """One forward+adjoint of the reference table path (CPU port) on a sample:
+    `batch` images, the first `coils` coils, the full trajectory."""
+    from oracle import cpu_baseline
+
+    return cpu_baseline.forward_adjoint(image[:batch], smaps[:batch, :coils], omega)
+
+
+def cpu_baseline_leg(image, smaps, omega, reps: int = 2, coils: int = 4):
+    from oracle import cpu_baseline
+
+    cpu_sample_run(image, smaps, omega, coils)  # warm-up (table build, thread pool)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        cpu_sample_run(image, smaps, omega, coils)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    M = omega.shape[1]
+    return {"value": coils * M / t, "unit": UNIT, "cores": cpu_baseline.threads(), "kind": "port",
+            "sample": f"batch 1 of {B}, {coils} of {C} coils, all {M} points; min of {reps} forward+adjoint runs "
+                      f"({t:.3f} s each); {cpu_baseline.describe()}"}
+
+
+# ---------------------------------------------------------------- arms
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    image, smaps, omega = make_inputs()
+    from oracle import cpu_baseline
+
+    coils = args.ref_coils
+    M = omega.shape[1]
+    for _ in range(args.warmup):
+        cpu_sample_run(image, smaps, omega, coils)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_sample_run(image, smaps, omega, coils)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = coils * M / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {"workload": "2D SENSE NUFFT fwd+adj, image 320x320, grid 640x640, J=6, L=1024, 16 coils, "
+                               "batch 4, golden-angle 404x640", "sample_per_step": f"batch 1, {coils} coils, {M} points"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_baseline.threads(), "kind": "port",
+                         "sample": f"batch 1 of {B}, {coils} of {C} coils, all {M} points per step; "
+                                   f"{cpu_baseline.describe()}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import torchkbnufft_gb300 as tkbn
+    from torchkbnufft_gb300 import _runtime as R
+
+    image_np, smaps_np, omega_np = make_inputs()
+    M = omega_np.shape[1]
+    image = torch.tensor(image_np, device=dev)
+    smaps = torch.tensor(smaps_np, device=dev)
+    omega = torch.tensor(omega_np, device=dev)
+    fwd = tkbn.KbNufft(im_size=(N, N), dtype=torch.complex64, device=dev)
+    adj = tkbn.KbNufftAdjoint(im_size=(N, N), dtype=torch.complex64, device=dev)
+    geom = fwd._geom(torch.complex64)
+    tables = fwd._tables()
+    scaling = fwd.scaling_coef
+    lay = R.points_layout(geom, omega)
+
+    def step_staged(ev=None):
+        if ev is not None:
+            ev[0].record()
+        grid = R.fft_and_scale(geom, image, smaps, scaling, None)
+        if ev is not None:
+            ev[1].record()
+        kdata = R.interp_fwd(geom, lay, tables, grid)
+        if ev is not None:
+            ev[2].record()
+        grid2 = R.interp_adj(geom, lay, tables, kdata)
+        if ev is not None:
+            ev[3].record()
+        out = R.ifft_and_scale(geom, grid2, smaps, scaling, None, overwrite=True)
+        if ev is not None:
+            ev[4].record()
+        return out
+
+    # correctness gate on the bench inputs: staged path == module path
+    with torch.no_grad():
+        ref_out = adj(fwd(image, omega, smaps=smaps), omega, smaps=smaps)
+        st_out = step_staged()
+        torch.cuda.synchronize()
+        gate = float((torch.linalg.vector_norm(ref_out - st_out) / torch.linalg.vector_norm(ref_out)).item())
+
+    for _ in range(args.warmup):
+        step_staged()
+    torch.cuda.synchronize()
+    barrier(world)
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(args.steps)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        start.record()
+        for k in range(args.steps):
+            step_staged(evs[k])
+        end.record()
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = start.elapsed_time(end) / args.steps
+    ms = max_over_ranks(ms, world, dev)
+    stage = {name: statistics.mean(e[i].elapsed_time(e[i + 1]) for e in evs)
+             for i, name in enumerate(["fft_and_scale", "interp_fwd", "interp_adj", "ifft_and_scale"])}
+
+    # e2e through the public modules with pinned host buffers
+    x_host = torch.tensor(image_np).pin_memory()
+    out_host = torch.empty((B, 1, N, N), dtype=torch.complex64).pin_memory()
+    x_dev = torch.empty_like(image)
+    with torch.no_grad():
+        for _ in range(args.warmup):
+            x_dev.copy_(x_host, non_blocking=True)
+            out_host.copy_(adj(fwd(x_dev, omega, smaps=smaps), omega, smaps=smaps), non_blocking=True)
+        torch.cuda.synchronize()
+        barrier(world)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            x_dev.copy_(x_host, non_blocking=True)
+            out_host.copy_(adj(fwd(x_dev, omega, smaps=smaps), omega, smaps=smaps), non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
+
+    work = B * C * M
+    value = world * work / (ms * 1e-3)
+    byts = algorithmic_bytes(M)
+    kernel = "interp_fwd" if stage["interp_fwd"] >= stage["interp_adj"] else "interp_adj"
+    kbytes = byts["gather"] if kernel == "interp_fwd" else byts["scatter"]
+    peak, peak_src = measured_peak_gbs()
+    achieved = kbytes / (stage[kernel] * 1e-3) / 1e9
+    pipeline_gbs = (byts["forward"] + byts["adjoint"]) / (ms * 1e-3) / 1e9
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_leg(image_np, smaps_np, omega_np)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {
+            "workload": "2D SENSE NUFFT fwd+adj, image 320x320, grid 640x640, J=6, L=1024, 16 coils, batch 4, "
+                        "golden-angle 404x640 (258560 points)",
+            "global_batch": B * world, "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)",
+            "work_per_step": f"{work} points*coils per GPU (B*C*M, once per fwd+adj pair)",
+            "stage_ms": {k: round(v, 4) for k, v in stage.items()},
+            "pipeline_gbs": round(pipeline_gbs, 1),
+            "pipeline_algorithmic_bytes": byts["forward"] + byts["adjoint"],
+            "parity_gate_rel_l2_staged_vs_module": gate,
+        },
+        "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": f"{peak_src} hbm_gbs",
+                     "algorithmic_bytes_per_launch": kbytes, "traffic": ncu_traffic(kernel)},
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * work / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(x_host.numel() * 8), "d2h_bytes_per_step": int(out_host.numel() * 8)},
+        "gpu_launches": 4 * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--ref-coils", type=int, default=4)
+    args = p.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,159 @@
+/*
+ * tkbn_gb300.h — C ABI of the GB300 (sm_103a) table-mode Kaiser-Bessel NUFFT.
+ *
+ * Plain C: device pointers, sizes and a CUDA stream handle (cudaStream_t passed
+ * as void*). No torch types. Every entry point returns an int status
+ * (TKBN_OK or a negative TKBN_ERR_*); tkbn_last_error() gives the message of
+ * the last failure on the calling thread.
+ *
+ * Ownership: the caller owns every buffer passed in (inputs, outputs and
+ * workspaces). The library allocates nothing except inside
+ * tkbn_fft_plan_create (the cuFFT plan and its work area), which
+ * tkbn_fft_plan_destroy releases.
+ *
+ * Streams: all work is enqueued on the given stream; no entry point
+ * synchronises the host, so sequences of calls can be captured in a CUDA
+ * graph (except plan creation/destruction).
+ *
+ * Layouts (row-major, complex = interleaved re/im of the working real type):
+ *   image   (B, Ci, N0[, N1[, N2]])   Ci = 1 when smaps are given, else C
+ *   smaps   (Bs, C, N0, ...)          Bs = 1 (shared) or B
+ *   grid    (B, C, K0[, K1[, K2]])    oversampled Fourier grid
+ *   kdata   (B, C, M)
+ *   omega   (T, d, M) real            T = 1 (shared trajectory) or B
+ *   tables  d pointers, each complex[J_d * L_d + 1]
+ *   scaling complex[N0 * N1 * ...]
+ *
+ * Reference interfaces replaced (mmuckley/torchkbnufft, paths in that project):
+ *   tkbn_points_build      sort_data / sort_one_batch   torchkbnufft/_nufft/interp.py:551-584
+ *   tkbn_interp_fwd        table_interp                 torchkbnufft/_nufft/interp.py:315-403
+ *   tkbn_interp_adj        table_interp_adjoint         torchkbnufft/_nufft/interp.py:587-726
+ *   tkbn_interp_grad_omega (none: the reference returns no omega gradient,
+ *                           torchkbnufft/_autograd/interp.py:130)
+ *   tkbn_fft_and_scale     fft_and_scale (+ SENSE multiply)
+ *                          torchkbnufft/_nufft/fft.py:35-76, modules/kbnufft.py:182-183
+ *   tkbn_ifft_and_scale    ifft_and_scale (+ coil sum)
+ *                          torchkbnufft/_nufft/fft.py:79-118, modules/kbnufft.py:404-405
+ *   tkbn_nufft_fwd         kb_table_nufft               torchkbnufft/functional/nufft.py:126-191
+ *   tkbn_nufft_adj         kb_table_nufft_adjoint       torchkbnufft/functional/nufft.py:194-260
+ *   tkbn_fft_filter        fft_filter                   torchkbnufft/_nufft/fft.py:121-173
+ *   tkbn_toep_apply        ToepNufft.forward / toep_batch_loop
+ *                          torchkbnufft/modules/kbnufft.py:441-547
+ */
+#ifndef TKBN_GB300_H
+#define TKBN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TKBN_ABI_VERSION 1
+
+/* status codes */
+#define TKBN_OK 0
+#define TKBN_ERR_INVALID (-1)     /* bad argument: shape, size, null pointer   */
+#define TKBN_ERR_UNSUPPORTED (-2) /* dtype, ndim or numpoints not supported     */
+#define TKBN_ERR_CUDA (-3)        /* CUDA runtime error                         */
+#define TKBN_ERR_CUFFT (-4)       /* cuFFT error                                */
+#define TKBN_ERR_DEVICE (-5)      /* a kernel's own check failed (status word)  */
+
+/* dtypes */
+#define TKBN_C64 0  /* complex64: float32 arithmetic  */
+#define TKBN_C128 1 /* complex128: float64 arithmetic */
+
+/* FFT normalisation */
+#define TKBN_NORM_NONE 0  /* forward unnormalised, inverse without 1/N */
+#define TKBN_NORM_ORTHO 1 /* 1/sqrt(prod K) both ways                  */
+
+/* Operator geometry (one per KbModule). Unused dims (>= ndim) are ignored. */
+typedef struct tkbn_geometry {
+  int32_t ndim;              /* 1, 2 or 3 */
+  int32_t dtype;             /* TKBN_C64 or TKBN_C128 */
+  int64_t im_size[3];        /* N_d */
+  int64_t grid_size[3];      /* K_d */
+  int32_t numpoints[3];      /* J_d, 1..8 */
+  int32_t table_oversamp[3]; /* L_d */
+  double n_shift[3];         /* fftshift distance per dim */
+} tkbn_geometry;
+
+/* Sorted-point layout of one trajectory set (built by tkbn_points_build). */
+typedef struct tkbn_points_desc {
+  int64_t npts;      /* M: points per trajectory */
+  int64_t ntraj;     /* 1 (shared by all batch items) or B */
+  int32_t tile[3];   /* tile edge per dim in grid cells; 0 = library default */
+  int32_t chunk;     /* max points per work item; 0 = library default */
+} tkbn_points_desc;
+
+typedef struct tkbn_fft_plan_s* tkbn_fft_plan;
+
+/* ---- library ---------------------------------------------------------- */
+int tkbn_abi_version(void);
+const char* tkbn_last_error(void);
+/* Reads and clears the device status word written by kernels whose internal
+ * checks failed (0 = clean). Synchronises the given stream. */
+int tkbn_device_status(void* stream, int32_t* status);
+
+/* ---- trajectory layout (K1: bin sort), once per trajectory -------------- */
+int tkbn_points_workspace_size(const tkbn_geometry* g, const tkbn_points_desc* p, size_t* bytes);
+int tkbn_points_build(const tkbn_geometry* g, const tkbn_points_desc* p, const void* omega,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- interpolation ------------------------------------------------------ */
+/* kdata = interp(grid): gather of J^d neighbours per point, times the fftshift phase. */
+int tkbn_interp_fwd(const tkbn_geometry* g, const tkbn_points_desc* p, const void* workspace,
+                    const void* const* tables, const void* grid, int64_t nbatch, int64_t ncoil,
+                    void* kdata, void* stream);
+/* grid = interp^H(kdata). grid is fully overwritten (zeroed first). */
+int tkbn_interp_adj(const tkbn_geometry* g, const tkbn_points_desc* p, const void* workspace,
+                    const void* const* tables, const void* kdata, int64_t nbatch, int64_t ncoil,
+                    void* grid, void* stream);
+/* grad_omega[t,d,m] = Re sum_{b,c} conj(v[b,c,m]) * d/d omega_d (interp(grid))[b,c,m],
+ * with the derivative of the KB kernel taken from dtables (d/du of each table
+ * entry) and linear interpolation within table bins. grad_omega is overwritten. */
+int tkbn_interp_grad_omega(const tkbn_geometry* g, const tkbn_points_desc* p, const void* workspace,
+                           const void* const* tables, const void* const* dtables, const void* grid,
+                           const void* v, int64_t nbatch, int64_t ncoil, void* grad_omega, void* stream);
+
+/* ---- FFT stages --------------------------------------------------------- */
+/* cuFFT plan for nbatch*ncoil transforms of size grid_size (in place). */
+int tkbn_fft_plan_create(const tkbn_geometry* g, int64_t nbatch, int64_t ncoil, tkbn_fft_plan* plan);
+int tkbn_fft_plan_destroy(tkbn_fft_plan plan);
+
+/* grid = FFT(zero_pad(image [* smaps] * scaling)). scaling may be NULL (ones).
+ * smaps may be NULL; then image has ncoil channels. */
+int tkbn_fft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, const void* smaps,
+                       int64_t smaps_batch, const void* scaling, int64_t nbatch, int64_t ncoil, int norm,
+                       void* grid, void* stream);
+/* image = [sum_c conj(smaps) *] conj(scaling) * crop(IFFT(grid)). grid is used as scratch. */
+int tkbn_ifft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, void* grid, const void* smaps,
+                        int64_t smaps_batch, const void* scaling, int64_t nbatch, int64_t ncoil, int norm,
+                        void* image, void* stream);
+
+/* ---- composed operators ------------------------------------------------- */
+int tkbn_nufft_fwd(const tkbn_geometry* g, const tkbn_points_desc* p, const void* workspace,
+                   tkbn_fft_plan plan, const void* const* tables, const void* scaling, const void* image,
+                   const void* smaps, int64_t smaps_batch, int64_t nbatch, int64_t ncoil, int norm,
+                   void* grid_scratch, void* kdata, void* stream);
+int tkbn_nufft_adj(const tkbn_geometry* g, const tkbn_points_desc* p, const void* workspace,
+                   tkbn_fft_plan plan, const void* const* tables, const void* scaling, const void* kdata,
+                   const void* smaps, int64_t smaps_batch, int64_t nbatch, int64_t ncoil, int norm,
+                   void* grid_scratch, void* image, void* stream);
+
+/* out = crop(IFFT(kernel * FFT(zero_pad(image)))) per channel. geometry:
+ * im_size = image spatial size, grid_size = kernel size. kernel_batch = 1 or nbatch. */
+int tkbn_fft_filter(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, const void* kernel,
+                    int64_t kernel_batch, int64_t nbatch, int64_t ncoil, int norm, void* grid_scratch,
+                    void* out, void* stream);
+/* Toeplitz normal operator with coil maps:
+ * out[b] = sum_c conj(s_c) crop(IFFT(kernel * FFT(pad(s_c * image[b])))). */
+int tkbn_toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, const void* kernel,
+                    int64_t kernel_batch, const void* smaps, int64_t smaps_batch, int64_t nbatch, int64_t ncoil,
+                    int norm, void* grid_scratch, void* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TKBN_GB300_H */

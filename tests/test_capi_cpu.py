@@ -1,0 +1,90 @@
+"""The C-ABI library loads here (no GPU) and exports every declared entry point.
+
+No compute calls: only functions that never touch the device are invoked.
+"""
+
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "tkbn_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(tkbn_\w+)\s*\(", src, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from torchkbnufft_gb300 import _lib
+
+    return _lib.load()
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert "tkbn_interp_fwd" in names and "tkbn_nufft_adj" in names and len(names) >= 16
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from torchkbnufft_gb300 import _build
+
+    out = subprocess.run(["nm", "-D", "--defined-only", _build.lib_path()], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT\s+(tkbn_\w+)", out))
+    missing = [n for n in _declared() if n not in exported]
+    assert not missing, missing
+    for n in _declared():
+        assert getattr(lib, n) is not None
+
+
+def test_python_binding_covers_header():
+    from torchkbnufft_gb300 import _lib
+
+    assert set(_declared()) == set(_lib.SIGNATURES)
+
+
+def test_abi_version(lib):
+    assert lib.tkbn_abi_version() == 1
+
+
+def test_host_side_argument_errors(lib):
+    """Argument validation happens on the host before any CUDA call."""
+    from torchkbnufft_gb300 import _lib
+
+    g = _lib.Geometry()
+    g.ndim = 4
+    g.dtype = _lib.TKBN_C64
+    n = ctypes.c_size_t(0)
+    p = _lib.PointsDesc()
+    p.npts, p.ntraj = 10, 1
+    rc = lib.tkbn_points_workspace_size(ctypes.byref(g), ctypes.byref(p), ctypes.byref(n))
+    assert rc == _lib.TKBN_ERR_UNSUPPORTED
+    assert b"ndim" in lib.tkbn_last_error()
+    g.ndim = 2
+    g.dtype = 7
+    rc = lib.tkbn_interp_fwd(ctypes.byref(g), ctypes.byref(p), None, None, None, 1, 1, None, None)
+    assert rc == _lib.TKBN_ERR_UNSUPPORTED
+    g.dtype = _lib.TKBN_C64
+    for d in range(2):
+        g.grid_size[d] = 0
+    rc = lib.tkbn_interp_fwd(ctypes.byref(g), ctypes.byref(p), None, None, None, 1, 1, None, None)
+    assert rc == _lib.TKBN_ERR_INVALID
+    with pytest.raises(ValueError):
+        _lib.check(rc)
+
+
+def test_cpu_tensors_are_rejected():
+    """No CPU fallback: the product path raises on CPU tensors."""
+    import torch
+
+    import torchkbnufft_gb300 as tkbn
+
+    ob = tkbn.KbNufft(im_size=(8, 8))
+    x = torch.randn(1, 1, 8, 8, dtype=torch.complex64)
+    om = torch.rand(2, 10) * 2 - 1
+    with pytest.raises(RuntimeError, match="CUDA"):
+        ob(x, om)

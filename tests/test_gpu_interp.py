@@ -1,0 +1,205 @@
+"""GPU parity of the interpolation kernels (K1 sort, K3 gather, K4 scatter).
+
+Checked against the reference's golden vectors, live reference fixtures and
+the CPU oracle. Tolerances: float64 paths at 1e-10 relative L2 (reference
+tests use torch.allclose), complex64 at 1e-5 relative L2 (the parity bar).
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden, rel_l2
+from oracle import kbnufft_oracle as O
+
+pytestmark = pytest.mark.gpu
+DEV = torch.device("cuda")
+TOL64 = 1e-5
+TOL128 = 1e-10
+
+
+def tkbn():
+    import torchkbnufft_gb300 as m
+
+    return m
+
+
+def _c(x):
+    return x[..., 0] + 1j * x[..., 1]
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_reference_interp_golden(case):
+    """``tests/data/interp_data.pkl`` through KbInterp in float64, real (..., 2) layout."""
+    g = load_golden("ref_interp_data")
+    image, ktraj, kdata = g[f"image_{case}"], g[f"ktraj_{case}"], g[f"kdata_{case}"]
+    im_size = image.shape[2:-1]
+    ob = tkbn().KbInterp(im_size=im_size, grid_size=im_size, dtype=torch.float64, device=DEV)
+    out = ob(torch.tensor(image, device=DEV), torch.tensor(ktraj, device=DEV))
+    assert out.shape == kdata.shape
+    assert torch.allclose(out.cpu(), torch.tensor(kdata))
+    assert rel_l2(_np(out), kdata) < TOL128
+
+
+@pytest.mark.parametrize("name", ["interp_1d", "interp_2d", "interp_2d_batched", "interp_3d", "interp_2d_c128"])
+def test_live_interp_fixtures(name):
+    g = load_golden("live_" + name)
+    cd = torch.complex64 if g["grid"].dtype == np.complex64 else torch.complex128
+    tol = TOL64 if cd == torch.complex64 else TOL128
+    im_size = g["grid"].shape[2:]
+    fwd = tkbn().KbInterp(im_size=im_size, grid_size=im_size, dtype=cd, device=DEV)
+    adj = tkbn().KbInterpAdjoint(im_size=im_size, grid_size=im_size, dtype=cd, device=DEV)
+    om = torch.tensor(g["omega"], device=DEV)
+    assert rel_l2(_np(fwd(torch.tensor(g["grid"], device=DEV), om)), g["kdata"]) < tol
+    assert rel_l2(_np(adj(torch.tensor(g["kdata_in"], device=DEV), om)), g["grid_adj"]) < tol
+
+
+def _rand(gen, shape, cd):
+    x = torch.randn(shape + (2,), generator=gen, dtype=torch.float64)
+    return torch.view_as_complex(x).to(cd)
+
+
+def _traj(gen, shape, scale=1.0):
+    return (torch.rand(shape, generator=gen, dtype=torch.float64) * 2 - 1) * np.pi * scale
+
+
+CASES = [
+    # (grid_size, B, C, M, omega batched, numpoints, table_oversamp, omega scale)
+    ((128, 128), 2, 5, 20000, False, 6, 1024, 1.0),
+    ((96, 80), 3, 16, 7000, True, 6, 1024, 1.0),
+    ((77, 93), 1, 17, 5000, False, 6, 1024, 1.0),   # odd grid, two coil chunks
+    ((64, 48), 2, 3, 3000, False, (4, 6), 512, 1.0),  # per-dim numpoints, other table
+    ((60, 64), 1, 1, 4000, False, 6, 1024, 3.0),  # omega outside [-pi, pi): periodic wrap
+    ((200,), 2, 4, 3000, False, 6, 1024, 1.0),
+    ((24, 20, 28), 1, 3, 4000, False, 6, 1024, 1.0),
+    ((16, 18, 14), 2, 2, 1500, True, (4, 5, 6), 1024, 1.0),
+]
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+@pytest.mark.parametrize("cd", [torch.complex64, torch.complex128])
+def test_interp_vs_oracle(case, cd):
+    grid_size, B, C, M, batched, J, Lo, scale = CASES[case]
+    gen = torch.Generator().manual_seed(100 + case)
+    grid = _rand(gen, (B, C) + grid_size, cd)
+    rd = torch.float32 if cd == torch.complex64 else torch.float64
+    om = _traj(gen, (B, len(grid_size), M) if batched else (len(grid_size), M), scale).to(rd)
+    kin = _rand(gen, (B, C, M), cd)
+    fwd = tkbn().KbInterp(im_size=grid_size, grid_size=grid_size, numpoints=J, table_oversamp=Lo, dtype=cd,
+                          device=DEV)
+    adj = tkbn().KbInterpAdjoint(im_size=grid_size, grid_size=grid_size, numpoints=J, table_oversamp=Lo, dtype=cd,
+                                 device=DEV)
+    op = O.Operator(grid_size, grid_size, J, None, Lo, cdtype=np.complex64 if cd == torch.complex64 else np.complex128)
+    tol = TOL64 if cd == torch.complex64 else TOL128
+    y = fwd(grid.to(DEV), om.to(DEV))
+    assert rel_l2(_np(y), op.interp(grid.numpy(), om.numpy())) < tol
+    x = adj(kin.to(DEV), om.to(DEV))
+    assert rel_l2(_np(x), op.interp_adj(kin.numpy(), om.numpy())) < tol
+
+
+@pytest.mark.parametrize("shape, kdata_shape", [
+    ([1, 1, 19], [1, 1, 25]), ([3, 1, 13], [3, 1, 18]), ([1, 1, 32, 16], [1, 1, 83]),
+    ([5, 1, 15, 12], [5, 1, 83]), ([3, 2, 13, 18, 12], [3, 2, 112]), ([1, 2, 17, 19, 12], [1, 2, 112]),
+])
+def test_interp_adjointness(shape, kdata_shape):
+    """<A x, y> == <x, A^H y> (reference tests/test_interp.py:34-70), complex128."""
+    gen = torch.Generator().manual_seed(123)
+    im_size = tuple(shape[2:])
+    x = _rand(gen, tuple(shape), torch.complex128).to(DEV)
+    y = _rand(gen, tuple(kdata_shape), torch.complex128).to(DEV)
+    om = _traj(gen, (len(im_size), kdata_shape[2])).to(DEV)
+    fwd = tkbn().KbInterp(im_size=im_size, grid_size=im_size, dtype=torch.complex128, device=DEV)
+    adj = tkbn().KbInterpAdjoint(im_size=im_size, grid_size=im_size, dtype=torch.complex128, device=DEV)
+    a = torch.vdot(y.flatten(), fwd(x, om).flatten())
+    b = torch.vdot(adj(y, om).flatten(), x.flatten())
+    assert torch.allclose(a, b)
+
+
+def test_interp_batches_match_loop():
+    """Batched omega equals a loop over batch items (reference tests/test_interp.py:283-328)."""
+    gen = torch.Generator().manual_seed(5)
+    im = (32, 16)
+    x = _rand(gen, (4, 2) + im, torch.complex64).to(DEV)
+    y = _rand(gen, (4, 2, 300), torch.complex64).to(DEV)
+    om = _traj(gen, (4, 2, 300)).float().to(DEV)
+    fwd = tkbn().KbInterp(im_size=im, grid_size=im, dtype=torch.complex64, device=DEV)
+    adj = tkbn().KbInterpAdjoint(im_size=im, grid_size=im, dtype=torch.complex64, device=DEV)
+    loop = torch.cat([fwd(x[i:i + 1], om[i]) for i in range(4)])
+    assert torch.allclose(loop, fwd(x, om), rtol=1e-6, atol=1e-5)
+    loop = torch.cat([adj(y[i:i + 1], om[i]) for i in range(4)])
+    assert torch.allclose(loop, adj(y, om), rtol=1e-6, atol=1e-4)
+
+
+def test_complex_real_layouts_match():
+    gen = torch.Generator().manual_seed(9)
+    im = (20, 22)
+    x = _rand(gen, (2, 3) + im, torch.complex64).to(DEV)
+    om = _traj(gen, (2, 200)).float().to(DEV)
+    fwd = tkbn().KbInterp(im_size=im, grid_size=im, dtype=torch.complex64, device=DEV)
+    a = fwd(x, om)
+    b = torch.view_as_complex(fwd(torch.view_as_real(x), om))
+    assert torch.equal(a, b)
+
+
+def test_edge_cases():
+    """Single point, points on the grid boundary (+-pi), one coil, empty trajectory."""
+    im = (16, 16)
+    fwd = tkbn().KbInterp(im_size=im, grid_size=im, dtype=torch.complex64, device=DEV)
+    adj = tkbn().KbInterpAdjoint(im_size=im, grid_size=im, dtype=torch.complex64, device=DEV)
+    op = O.Operator(im, im, cdtype=np.complex64)
+    gen = torch.Generator().manual_seed(3)
+    x = _rand(gen, (1, 1) + im, torch.complex64)
+    for om in (torch.tensor([[0.3], [-1.2]]), torch.tensor([[np.pi, -np.pi, 0.0], [-np.pi, np.pi, np.pi]])):
+        om = om.float()
+        y = fwd(x.to(DEV), om.to(DEV))
+        assert rel_l2(_np(y), op.interp(x.numpy(), om.numpy())) < TOL64
+        k = _rand(gen, (1, 1, om.shape[1]), torch.complex64)
+        assert rel_l2(_np(adj(k.to(DEV), om.to(DEV))), op.interp_adj(k.numpy(), om.numpy())) < TOL64
+    empty = torch.zeros((2, 0), device=DEV)
+    assert fwd(x.to(DEV), empty).shape == (1, 1, 0)
+    g = adj(torch.zeros((1, 1, 0), dtype=torch.complex64, device=DEV), empty)
+    assert g.shape == (1, 1) + im and torch.count_nonzero(g) == 0
+
+
+def test_nonfinite_omega_is_flagged():
+    """A NaN coordinate gives NaN at that point, the others stay exact, and the status word is set."""
+    from torchkbnufft_gb300 import _runtime
+
+    im = (16, 16)
+    fwd = tkbn().KbInterp(im_size=im, grid_size=im, dtype=torch.complex64, device=DEV)
+    gen = torch.Generator().manual_seed(4)
+    x = _rand(gen, (1, 1) + im, torch.complex64)
+    om = _traj(gen, (2, 50)).float()
+    om[0, 7] = float("nan")
+    _runtime.device_status(DEV)  # clear
+    y = _np(fwd(x.to(DEV), om.to(DEV)))
+    assert np.isnan(y[0, 0, 7])
+    keep = np.ones(50, bool)
+    keep[7] = False
+    op = O.Operator(im, im, cdtype=np.complex64)
+    ref = op.interp(x.numpy(), om.numpy()[:, keep])
+    assert rel_l2(y[..., keep], ref) < TOL64
+    assert _runtime.device_status(DEV) & 1
+    assert _runtime.device_status(DEV) == 0
+
+
+def test_repeated_calls_reuse_layout():
+    from torchkbnufft_gb300 import _runtime
+
+    im = (32, 32)
+    fwd = tkbn().KbInterp(im_size=im, grid_size=im, dtype=torch.complex64, device=DEV)
+    gen = torch.Generator().manual_seed(6)
+    x = _rand(gen, (1, 2) + im, torch.complex64).to(DEV)
+    om = _traj(gen, (2, 500)).float().to(DEV)
+    a = fwd(x, om)
+    n = len(_runtime._layout_cache)
+    b = fwd(x, om)
+    assert len(_runtime._layout_cache) == n and torch.equal(a, b)
+    om.mul_(0.5)  # in-place change must invalidate the cached layout
+    c = fwd(x, om)
+    op = O.Operator(im, im, cdtype=np.complex64)
+    assert rel_l2(_np(c), op.interp(_np(x), _np(om))) < TOL64

@@ -1,0 +1,476 @@
+"""Tensor-level wrappers of the C ABI: geometry, caches, launches.
+
+Everything here takes and returns CUDA tensors and enqueues work on torch's
+current stream. Inputs on the CPU raise: this package has no CPU path.
+
+Caches (per process):
+
+* geometry: parsed once per set of module buffers (reading CUDA buffers with
+  ``tolist()`` would synchronise the device on every call);
+* trajectory layouts (bin-sorted points): keyed by the omega tensor object,
+  its version counter, shape and the geometry, so a trajectory that is
+  modified in place or freed is never reused;
+* cuFFT plans: keyed by geometry, batch*coils and device.
+"""
+
+from __future__ import annotations
+
+import collections
+import ctypes
+import threading
+import weakref
+from dataclasses import dataclass
+from typing import List, Optional, Sequence, Tuple
+
+import torch
+
+from . import _lib as L
+
+_lock = threading.RLock()
+
+
+# ---------------------------------------------------------------- checks
+
+
+def require_cuda(*tensors: Optional[torch.Tensor]) -> torch.device:
+    dev = None
+    for t in tensors:
+        if t is None:
+            continue
+        if not t.is_cuda:
+            raise RuntimeError(
+                "torchkbnufft_gb300 runs on CUDA devices only; got a tensor on "
+                f"{t.device}. Move inputs and the module to a CUDA device."
+            )
+        if dev is None:
+            dev = t.device
+        elif t.device != dev:
+            raise RuntimeError(f"tensors are on different devices: {dev} and {t.device}")
+    return dev
+
+
+def stream_handle(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def dtype_code(dtype: torch.dtype) -> int:
+    if dtype == torch.complex64:
+        return L.TKBN_C64
+    if dtype == torch.complex128:
+        return L.TKBN_C128
+    raise TypeError(f"unsupported dtype {dtype}: use complex64 or complex128")
+
+
+def real_of(dtype: torch.dtype) -> torch.dtype:
+    return torch.float32 if dtype == torch.complex64 else torch.float64
+
+
+def norm_code(norm: Optional[str]) -> int:
+    if norm is None:
+        return L.TKBN_NORM_NONE
+    if norm == "ortho":
+        return L.TKBN_NORM_ORTHO
+    raise ValueError("Only option for norm is 'ortho'.")
+
+
+# ---------------------------------------------------------------- geometry
+
+
+@dataclass(frozen=True)
+class GeomKey:
+    ndim: int
+    dtype: int
+    im_size: Tuple[int, ...]
+    grid_size: Tuple[int, ...]
+    numpoints: Tuple[int, ...]
+    table_oversamp: Tuple[int, ...]
+    n_shift: Tuple[float, ...]
+
+    def struct(self) -> L.Geometry:
+        g = L.Geometry()
+        g.ndim = self.ndim
+        g.dtype = self.dtype
+        for d in range(self.ndim):
+            g.im_size[d] = self.im_size[d]
+            g.grid_size[d] = self.grid_size[d]
+            g.numpoints[d] = self.numpoints[d]
+            g.table_oversamp[d] = self.table_oversamp[d]
+            g.n_shift[d] = self.n_shift[d]
+        return g
+
+
+_geom_structs: dict = {}
+
+
+def geom_struct(key: GeomKey) -> L.Geometry:
+    s = _geom_structs.get(key)
+    if s is None:
+        s = key.struct()
+        _geom_structs[key] = s
+    return s
+
+
+def _as_tuple(x, cast) -> Tuple:
+    if isinstance(x, torch.Tensor):
+        return tuple(cast(v) for v in x.reshape(-1).tolist())
+    if isinstance(x, (list, tuple)):
+        return tuple(cast(v) for v in x)
+    return (cast(x),)
+
+
+_param_cache: "collections.OrderedDict" = collections.OrderedDict()
+
+
+def host_values(t, cast) -> Tuple:
+    """Host copy of a small parameter tensor, cached by object identity + version."""
+    if not isinstance(t, torch.Tensor):
+        return _as_tuple(t, cast)
+    key = (id(t), t._version, t.data_ptr(), tuple(t.shape), cast)
+    with _lock:
+        hit = _param_cache.get(key)
+        if hit is not None and hit[0]() is t:
+            return hit[1]
+        vals = _as_tuple(t, cast)
+        _param_cache[key] = (weakref.ref(t), vals)
+        while len(_param_cache) > 256:
+            _param_cache.popitem(last=False)
+        return vals
+
+
+def make_geom(dtype, im_size, grid_size, numpoints, table_oversamp, n_shift) -> GeomKey:
+    grid = host_values(grid_size, int)
+    ndim = len(grid)
+    im = host_values(im_size, int) if im_size is not None else grid
+    J = host_values(numpoints, int)
+    Lo = host_values(table_oversamp, int)
+    ns = host_values(n_shift, float)
+    if len(J) == 1 and ndim > 1:
+        J = J * ndim
+    if len(Lo) == 1 and ndim > 1:
+        Lo = Lo * ndim
+    if not (len(im) == len(J) == len(Lo) == len(ns) == ndim):
+        raise ValueError("im_size, grid_size, numpoints, table_oversamp and n_shift must have one entry per dim")
+    if ndim not in (1, 2, 3):
+        raise ValueError("only 1D, 2D and 3D transforms are supported")
+    return GeomKey(ndim, dtype_code(dtype), im, grid, J, Lo, ns)
+
+
+# ---------------------------------------------------------------- trajectory layout
+
+
+class PointsLayout:
+    """Bin-sorted trajectory (K1) in a torch-owned workspace."""
+
+    def __init__(self, geom: GeomKey, omega: torch.Tensor, tile=None, chunk: int = 0):
+        require_cuda(omega)
+        self.geom = geom
+        self.device = omega.device
+        self.ntraj = 1 if omega.ndim == 2 else omega.shape[0]
+        self.npts = omega.shape[-1]
+        self.desc = L.PointsDesc()
+        self.desc.npts = self.npts
+        self.desc.ntraj = self.ntraj
+        if tile is not None:
+            for d, t in enumerate(tile):
+                self.desc.tile[d] = int(t)
+        self.desc.chunk = int(chunk)
+        g = geom_struct(geom)
+        nbytes = ctypes.c_size_t(0)
+        L.check(L.lib().tkbn_points_workspace_size(ctypes.byref(g), ctypes.byref(self.desc), ctypes.byref(nbytes)))
+        self.nbytes = int(nbytes.value)
+        self.workspace = torch.empty(self.nbytes, dtype=torch.uint8, device=self.device)
+        om = omega.detach().to(real_of(torch.complex64 if geom.dtype == L.TKBN_C64 else torch.complex128)).contiguous()
+        self._omega_keepalive = om
+        L.check(
+            L.lib().tkbn_points_build(ctypes.byref(g), ctypes.byref(self.desc), om.data_ptr(),
+                                      self.workspace.data_ptr(), self.nbytes, stream_handle(self.device))
+        )
+
+
+_layout_cache: "collections.OrderedDict" = collections.OrderedDict()
+_LAYOUT_CACHE_MAX = 8
+
+
+def points_layout(geom: GeomKey, omega: torch.Tensor, tile=None, chunk: int = 0) -> PointsLayout:
+    base = omega._base if omega._base is not None else omega
+    key = (id(base), omega.data_ptr(), omega._version, tuple(omega.shape), tuple(omega.stride()), omega.dtype,
+           geom, tuple(tile) if tile else None, chunk, omega.device)
+    with _lock:
+        hit = _layout_cache.get(key)
+        if hit is not None and hit[0]() is base:
+            _layout_cache.move_to_end(key)
+            return hit[1]
+        lay = PointsLayout(geom, omega, tile, chunk)
+        _layout_cache[key] = (weakref.ref(base), lay)
+        while len(_layout_cache) > _LAYOUT_CACHE_MAX:
+            _layout_cache.popitem(last=False)
+        return lay
+
+
+def clear_caches() -> None:
+    with _lock:
+        _layout_cache.clear()
+        _param_cache.clear()
+        for p in list(_fft_cache.values()):
+            p.destroy()
+        _fft_cache.clear()
+
+
+# ---------------------------------------------------------------- FFT plans
+
+
+class FFTPlan:
+    def __init__(self, geom: GeomKey, batch: int, coils: int, device: torch.device):
+        self.handle = ctypes.c_void_p()
+        self.geom = geom
+        with torch.cuda.device(device):
+            L.check(L.lib().tkbn_fft_plan_create(ctypes.byref(geom_struct(geom)), batch, coils, ctypes.byref(self.handle)))
+
+    def destroy(self):
+        if self.handle:
+            L.lib().tkbn_fft_plan_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+
+_fft_cache: "collections.OrderedDict" = collections.OrderedDict()
+_FFT_CACHE_MAX = 16
+
+
+def fft_plan(geom: GeomKey, batch: int, coils: int, device: torch.device) -> FFTPlan:
+    # plans depend on grid size, batch and dtype only
+    key = (geom.ndim, geom.dtype, geom.grid_size, batch * coils, device)
+    with _lock:
+        p = _fft_cache.get(key)
+        if p is None:
+            g2 = GeomKey(geom.ndim, geom.dtype, geom.grid_size, geom.grid_size, geom.numpoints, geom.table_oversamp,
+                         geom.n_shift)
+            p = FFTPlan(g2, batch * coils, 1, device)
+            _fft_cache[key] = p
+            while len(_fft_cache) > _FFT_CACHE_MAX:
+                _fft_cache.popitem(last=False)[1].destroy()
+        else:
+            _fft_cache.move_to_end(key)
+        return p
+
+
+def _plan_geom(geom: GeomKey, plan: FFTPlan, B: int, C: int) -> Tuple[L.Geometry, int, int]:
+    """The C API checks the plan batch against B*C; plans are cached by B*C."""
+    return geom_struct(geom), B * C, 1
+
+
+# ---------------------------------------------------------------- tables
+
+
+def table_ptrs(tables: Sequence[torch.Tensor], dtype: torch.dtype) -> Tuple[ctypes.Array, List[torch.Tensor]]:
+    keep = []
+    for t in tables:
+        require_cuda(t)
+        if t.dtype != dtype:
+            t = t.to(dtype)
+        keep.append(t.contiguous())
+    return L.ptr_array([t.data_ptr() for t in keep]), keep
+
+
+_dtable_cache: "collections.OrderedDict" = collections.OrderedDict()
+
+
+def derivative_tables(tables: Sequence[torch.Tensor], table_oversamp: Sequence[int]) -> List[torch.Tensor]:
+    """d/du of each table by central differences on the table grid (step 1/L).
+
+    Error O(1/L^2) relative; one-sided at the ends. Cached by table identity.
+    """
+    out = []
+    for t, Lo in zip(tables, table_oversamp):
+        key = (id(t), t._version, t.data_ptr(), int(Lo))
+        with _lock:
+            hit = _dtable_cache.get(key)
+            if hit is not None and hit[0]() is t:
+                out.append(hit[1])
+                continue
+        d = torch.empty_like(t)
+        d[1:-1] = (t[2:] - t[:-2]) * (Lo / 2.0)
+        d[0] = (t[1] - t[0]) * Lo
+        d[-1] = (t[-1] - t[-2]) * Lo
+        with _lock:
+            _dtable_cache[key] = (weakref.ref(t), d)
+            while len(_dtable_cache) > 32:
+                _dtable_cache.popitem(last=False)
+        out.append(d)
+    return out
+
+
+# ---------------------------------------------------------------- launches
+
+
+def _c(t: Optional[torch.Tensor]) -> int:
+    return 0 if t is None else t.data_ptr()
+
+
+def interp_fwd(geom: GeomKey, lay: PointsLayout, tables, grid: torch.Tensor) -> torch.Tensor:
+    """kdata (B, C, M) = table interpolation of grid (B, C, *K)."""
+    dev = require_cuda(grid)
+    grid = grid.contiguous()
+    B, C = grid.shape[:2]
+    kdata = torch.empty((B, C, lay.npts), dtype=grid.dtype, device=dev)
+    tp, keep = table_ptrs(tables, grid.dtype)
+    L.check(L.lib().tkbn_interp_fwd(ctypes.byref(geom_struct(geom)), ctypes.byref(lay.desc),
+                                    lay.workspace.data_ptr(), tp, grid.data_ptr(), B, C, kdata.data_ptr(),
+                                    stream_handle(dev)))
+    return kdata
+
+
+def interp_adj(geom: GeomKey, lay: PointsLayout, tables, kdata: torch.Tensor) -> torch.Tensor:
+    """grid (B, C, *K) = adjoint table interpolation of kdata (B, C, M)."""
+    dev = require_cuda(kdata)
+    kdata = kdata.contiguous()
+    B, C = kdata.shape[:2]
+    grid = torch.empty((B, C) + geom.grid_size, dtype=kdata.dtype, device=dev)
+    tp, keep = table_ptrs(tables, kdata.dtype)
+    L.check(L.lib().tkbn_interp_adj(ctypes.byref(geom_struct(geom)), ctypes.byref(lay.desc),
+                                    lay.workspace.data_ptr(), tp, kdata.data_ptr(), B, C, grid.data_ptr(),
+                                    stream_handle(dev)))
+    return grid
+
+
+def interp_grad_omega(geom: GeomKey, lay: PointsLayout, tables, grid: torch.Tensor, v: torch.Tensor) -> torch.Tensor:
+    """(T, d, M) real: Re sum_{b,c} conj(v) * d interp(grid) / d omega."""
+    dev = require_cuda(grid, v)
+    grid = grid.contiguous()
+    v = v.contiguous()
+    B, C = grid.shape[:2]
+    rd = real_of(grid.dtype)
+    grad = torch.empty((lay.ntraj, geom.ndim, lay.npts), dtype=rd, device=dev)
+    tabs = [t.to(grid.dtype).contiguous() for t in tables]
+    dtabs = derivative_tables(tabs, geom.table_oversamp)
+    tp, keep = table_ptrs(tabs, grid.dtype)
+    dp, keep2 = table_ptrs(dtabs, grid.dtype)
+    L.check(L.lib().tkbn_interp_grad_omega(ctypes.byref(geom_struct(geom)), ctypes.byref(lay.desc),
+                                           lay.workspace.data_ptr(), tp, dp, grid.data_ptr(), v.data_ptr(), B, C,
+                                           grad.data_ptr(), stream_handle(dev)))
+    return grad
+
+
+def fft_and_scale(geom: GeomKey, image: torch.Tensor, smaps: Optional[torch.Tensor], scaling: Optional[torch.Tensor],
+                  norm: Optional[str], coils: Optional[int] = None) -> torch.Tensor:
+    """grid (B, C, *K) = FFT(pad(image [* smaps] * scaling))."""
+    dev = require_cuda(image, smaps, scaling)
+    image = image.contiguous()
+    B = image.shape[0]
+    C = smaps.shape[1] if smaps is not None else image.shape[1]
+    sb = 0
+    if smaps is not None:
+        smaps = smaps.to(image.dtype).contiguous()
+        sb = smaps.shape[0]
+    if scaling is not None:
+        scaling = scaling.to(image.dtype).contiguous()
+    plan = fft_plan(geom, B, C, dev)
+    grid = torch.empty((B, C) + geom.grid_size, dtype=image.dtype, device=dev)
+    g, pb, pc = _plan_geom(geom, plan, B, C)
+    # the plan's batch is B*C; pass the true (B, C) to the kernels
+    L.check(L.lib().tkbn_fft_and_scale(ctypes.byref(g), plan.handle, image.data_ptr(), _c(smaps), sb, _c(scaling),
+                                       B, C, norm_code(norm), grid.data_ptr(), stream_handle(dev)))
+    return grid
+
+
+def ifft_and_scale(geom: GeomKey, grid: torch.Tensor, smaps: Optional[torch.Tensor], scaling: Optional[torch.Tensor],
+                   norm: Optional[str], overwrite: bool = False) -> torch.Tensor:
+    """image = [sum_c conj(smaps) *] conj(scaling) * crop(IFFT(grid)); grid is clobbered if overwrite."""
+    dev = require_cuda(grid, smaps, scaling)
+    B, C = grid.shape[:2]
+    work = grid.contiguous() if overwrite else grid.contiguous().clone()
+    sb = 0
+    if smaps is not None:
+        smaps = smaps.to(grid.dtype).contiguous()
+        sb = smaps.shape[0]
+    if scaling is not None:
+        scaling = scaling.to(grid.dtype).contiguous()
+    plan = fft_plan(geom, B, C, dev)
+    co = 1 if smaps is not None else C
+    out = torch.empty((B, co) + geom.im_size, dtype=grid.dtype, device=dev)
+    L.check(L.lib().tkbn_ifft_and_scale(ctypes.byref(geom_struct(geom)), plan.handle, work.data_ptr(), _c(smaps), sb,
+                                        _c(scaling), B, C, norm_code(norm), out.data_ptr(), stream_handle(dev)))
+    return out
+
+
+def nufft_fwd(geom: GeomKey, lay: PointsLayout, tables, scaling, image, smaps, norm) -> torch.Tensor:
+    """Fused forward NUFFT: kdata = interp(FFT(pad(image [* smaps] * scaling)))."""
+    dev = require_cuda(image, smaps, scaling)
+    image = image.contiguous()
+    B = image.shape[0]
+    C = smaps.shape[1] if smaps is not None else image.shape[1]
+    sb = 0
+    if smaps is not None:
+        smaps = smaps.to(image.dtype).contiguous()
+        sb = smaps.shape[0]
+    if scaling is not None:
+        scaling = scaling.to(image.dtype).contiguous()
+    plan = fft_plan(geom, B, C, dev)
+    grid = torch.empty((B, C) + geom.grid_size, dtype=image.dtype, device=dev)
+    kdata = torch.empty((B, C, lay.npts), dtype=image.dtype, device=dev)
+    tp, keep = table_ptrs(tables, image.dtype)
+    L.check(L.lib().tkbn_nufft_fwd(ctypes.byref(geom_struct(geom)), ctypes.byref(lay.desc), lay.workspace.data_ptr(),
+                                   plan.handle, tp, _c(scaling), image.data_ptr(), _c(smaps), sb, B, C,
+                                   norm_code(norm), grid.data_ptr(), kdata.data_ptr(), stream_handle(dev)))
+    return kdata
+
+
+def nufft_adj(geom: GeomKey, lay: PointsLayout, tables, scaling, kdata, smaps, norm) -> torch.Tensor:
+    """Fused adjoint NUFFT: image = [sum_c conj(smaps)] conj(scaling) crop(IFFT(interp^H(kdata)))."""
+    dev = require_cuda(kdata, smaps, scaling)
+    kdata = kdata.contiguous()
+    B, C = kdata.shape[:2]
+    sb = 0
+    if smaps is not None:
+        smaps = smaps.to(kdata.dtype).contiguous()
+        sb = smaps.shape[0]
+    if scaling is not None:
+        scaling = scaling.to(kdata.dtype).contiguous()
+    plan = fft_plan(geom, B, C, dev)
+    grid = torch.empty((B, C) + geom.grid_size, dtype=kdata.dtype, device=dev)
+    co = 1 if smaps is not None else C
+    image = torch.empty((B, co) + geom.im_size, dtype=kdata.dtype, device=dev)
+    tp, keep = table_ptrs(tables, kdata.dtype)
+    L.check(L.lib().tkbn_nufft_adj(ctypes.byref(geom_struct(geom)), ctypes.byref(lay.desc), lay.workspace.data_ptr(),
+                                   plan.handle, tp, _c(scaling), kdata.data_ptr(), _c(smaps), sb, B, C,
+                                   norm_code(norm), grid.data_ptr(), image.data_ptr(), stream_handle(dev)))
+    return image
+
+
+def toep_apply(image: torch.Tensor, kernel: torch.Tensor, smaps: Optional[torch.Tensor], norm: Optional[str],
+               kernel_batched: bool) -> torch.Tensor:
+    """Toeplitz normal operator / FFT filter on the oversampled grid of ``kernel``."""
+    dev = require_cuda(image, kernel, smaps)
+    image = image.contiguous()
+    kernel = kernel.to(image.dtype).contiguous()
+    nd = image.ndim - 2
+    im_size = tuple(image.shape[2:])
+    grid_size = tuple(kernel.shape[-nd:])
+    geom = GeomKey(nd, dtype_code(image.dtype), im_size, grid_size, (1,) * nd, (1,) * nd, (0.0,) * nd)
+    B = image.shape[0]
+    kb = kernel.shape[0] if kernel_batched else 1
+    if smaps is not None:
+        smaps = smaps.to(image.dtype).contiguous()
+        C = smaps.shape[1]
+        sb = smaps.shape[0]
+    else:
+        C = image.shape[1]
+        sb = 0
+    plan = fft_plan(geom, B, C, dev)
+    grid = torch.empty((B, C) + grid_size, dtype=image.dtype, device=dev)
+    co = 1 if smaps is not None else C
+    out = torch.empty((B, co) + im_size, dtype=image.dtype, device=dev)
+    g = geom_struct(geom)
+    if smaps is not None:
+        L.check(L.lib().tkbn_toep_apply(ctypes.byref(g), plan.handle, image.data_ptr(), kernel.data_ptr(), kb,
+                                        smaps.data_ptr(), sb, B, C, norm_code(norm), grid.data_ptr(), out.data_ptr(),
+                                        stream_handle(dev)))
+    else:
+        L.check(L.lib().tkbn_fft_filter(ctypes.byref(g), plan.handle, image.data_ptr(), kernel.data_ptr(), kb, B, C,
+                                        norm_code(norm), grid.data_ptr(), out.data_ptr(), stream_handle(dev)))
+    return out
+
+
+def device_status(device: torch.device) -> int:
+    st = ctypes.c_int32(0)
+    L.check(L.lib().tkbn_device_status(stream_handle(device), ctypes.byref(st)))
+    return int(st.value)

@@ -1,0 +1,307 @@
+// K2 / K5 / K6: FFT stages of the NUFFT and the Toeplitz normal operator,
+// fused around cuFFT.
+//
+//   K2 pad_scale : grid = pad(image [* smaps] * scaling) [* 1/sqrt(prod K)]
+//                  (fft_and_scale, torchkbnufft/_nufft/fft.py:35-76, with the
+//                  SENSE multiply of modules/kbnufft.py:182-183 folded in)
+//   cuFFT        : in-place C2C/Z2Z, forward or inverse, unnormalised
+//   K5 crop_scale: image = [sum_c conj(smaps) *] conj(scaling) * crop(grid)
+//                  (ifft_and_scale, torchkbnufft/_nufft/fft.py:79-118, with the
+//                  coil sum of modules/kbnufft.py:404-405 folded in)
+//   K6 kernel_mul: grid *= kernel (fft_filter, torchkbnufft/_nufft/fft.py:121-173)
+//
+// "ortho" scales by 1/sqrt(prod K) on each transform; the scale is applied in
+// the neighbouring elementwise kernel instead of inside the FFT.
+
+#include <cufft.h>
+
+#include <cmath>
+#include <new>
+
+#include "tkbn_common.cuh"
+
+struct tkbn_fft_plan_s {
+  cufftHandle handle;
+  int ndim;
+  int dtype;
+  int64_t n[3];
+  int64_t batch;
+};
+
+namespace tkbn {
+
+struct Shape {
+  int ndim;
+  int N[3];  // image size
+  int K[3];  // grid size
+  int64_t ntot, gtot;
+};
+
+// Grid element -> image flat index, or -1 when the element is padding.
+__device__ __forceinline__ int64_t grid_to_image(const Shape& s, int64_t g) {
+  int64_t nflat = 0, nstride = 1;
+  for (int d = s.ndim - 1; d >= 0; --d) {
+    const int64_t gd = g % s.K[d];
+    g /= s.K[d];
+    if (gd >= s.N[d]) return -1;
+    nflat += gd * nstride;
+    nstride *= s.N[d];
+  }
+  return nflat;
+}
+
+// Image flat index -> grid flat index.
+__device__ __forceinline__ int64_t image_to_grid(const Shape& s, int64_t n) {
+  int64_t gflat = 0, gstride = 1;
+  for (int d = s.ndim - 1; d >= 0; --d) {
+    const int64_t nd = n % s.N[d];
+    n /= s.N[d];
+    gflat += nd * gstride;
+    gstride *= s.K[d];
+  }
+  return gflat;
+}
+
+// K2. One thread per grid element of (B, C, K...). image has `ci` channels
+// (1 with smaps, C without); smaps has `sb` batch entries (1 or B).
+template <typename R>
+__global__ void k_pad_scale(Shape s, int64_t B, int64_t C, int64_t ci, const cplx<R>* __restrict__ image,
+                            const cplx<R>* __restrict__ smaps, int64_t sb, const cplx<R>* __restrict__ scaling,
+                            R scale, cplx<R>* __restrict__ grid) {
+  const int64_t total = B * C * s.gtot;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t bc = e / s.gtot;
+    const int64_t g = e - bc * s.gtot;
+    const int64_t n = grid_to_image(s, g);
+    cplx<R> v = mk<R>(0, 0);
+    if (n >= 0) {
+      const int64_t b = bc / C, c = bc - (bc / C) * C;
+      v = image[(b * ci + (ci == 1 ? 0 : c)) * s.ntot + n];
+      if (smaps) v = cmul<R>(v, smaps[((sb == 1 ? 0 : b) * C + c) * s.ntot + n]);
+      if (scaling) v = cmul<R>(v, scaling[n]);
+      v = cscale<R>(v, scale);
+    }
+    grid[e] = v;
+  }
+}
+
+// K5. One thread per output element: (B, 1, N...) with smaps, else (B, C, N...).
+template <typename R>
+__global__ void k_crop_scale(Shape s, int64_t B, int64_t C, const cplx<R>* __restrict__ grid,
+                             const cplx<R>* __restrict__ smaps, int64_t sb, const cplx<R>* __restrict__ scaling,
+                             R scale, cplx<R>* __restrict__ out) {
+  const int64_t co = smaps ? 1 : C;
+  const int64_t total = B * co * s.ntot;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t bc = e / s.ntot;
+    const int64_t n = e - bc * s.ntot;
+    const int64_t g = image_to_grid(s, n);
+    cplx<R> sc = scaling ? cconj<R>(scaling[n]) : mk<R>(1, 0);
+    sc = cscale<R>(sc, scale);
+    if (smaps) {
+      const int64_t b = bc;
+      const cplx<R>* sm = smaps + (sb == 1 ? 0 : b) * C * s.ntot + n;
+      cplx<R> acc = mk<R>(0, 0);
+      for (int64_t c = 0; c < C; ++c) {
+        const cplx<R> v = cmul<R>(grid[(b * C + c) * s.gtot + g], sc);
+        acc = cfma<R>(v, cconj<R>(sm[c * s.ntot]), acc);
+      }
+      out[e] = acc;
+    } else {
+      out[e] = cmul<R>(grid[bc * s.gtot + g], sc);
+    }
+  }
+}
+
+// K6. grid[b, c, g] *= kernel[kb, g] * scale, kb = b when the kernel is batched.
+template <typename R>
+__global__ void k_kernel_mul(int64_t gtot, int64_t B, int64_t C, const cplx<R>* __restrict__ kernel, int64_t kbatch,
+                             R scale, cplx<R>* __restrict__ grid) {
+  const int64_t total = B * C * gtot;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t bc = e / gtot;
+    const int64_t g = e - bc * gtot;
+    const int64_t b = bc / C;
+    grid[e] = cscale<R>(cmul<R>(grid[e], kernel[(kbatch == 1 ? 0 : b) * gtot + g]), scale);
+  }
+}
+
+}  // namespace tkbn
+
+TKBN_DEFINE_STATUS_READER(status_fft)
+
+namespace tkbn_host {
+
+using namespace tkbn;
+
+static int grid_blocks(int64_t work) {
+  int64_t b = (work + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+static int check_cufft(cufftResult r, const char* what) {
+  if (r == CUFFT_SUCCESS) return TKBN_OK;
+  return set_error(TKBN_ERR_CUFFT, "%s: cuFFT error %d", what, (int)r);
+}
+
+int fft_plan_create(const tkbn_geometry* g, int64_t B, int64_t C, tkbn_fft_plan* out) {
+  if (!g || !out) return set_error(TKBN_ERR_INVALID, "null argument");
+  if (g->ndim < 1 || g->ndim > 3) return set_error(TKBN_ERR_UNSUPPORTED, "ndim must be 1, 2 or 3");
+  if (g->dtype != TKBN_C64 && g->dtype != TKBN_C128) return set_error(TKBN_ERR_UNSUPPORTED, "unsupported dtype");
+  if (B < 1 || C < 1) return set_error(TKBN_ERR_INVALID, "batch and coil counts must be >= 1");
+  tkbn_fft_plan p = new (std::nothrow) tkbn_fft_plan_s();
+  if (!p) return set_error(TKBN_ERR_INVALID, "out of host memory");
+  p->ndim = g->ndim;
+  p->dtype = g->dtype;
+  p->batch = B * C;
+  long long n[3];
+  for (int d = 0; d < g->ndim; ++d) {
+    n[d] = g->grid_size[d];
+    p->n[d] = g->grid_size[d];
+  }
+  int rc = check_cufft(cufftCreate(&p->handle), "cufftCreate");
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  size_t work = 0;
+  rc = check_cufft(cufftMakePlanMany64(p->handle, g->ndim, n, nullptr, 1, 0, nullptr, 1, 0,
+                                       g->dtype == TKBN_C64 ? CUFFT_C2C : CUFFT_Z2Z, (long long)p->batch, &work),
+                   "cufftMakePlanMany64");
+  if (rc) {
+    cufftDestroy(p->handle);
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return TKBN_OK;
+}
+
+int fft_plan_destroy(tkbn_fft_plan p) {
+  if (!p) return TKBN_OK;
+  int rc = check_cufft(cufftDestroy(p->handle), "cufftDestroy");
+  delete p;
+  return rc;
+}
+
+static int check_plan(const tkbn_geometry* g, tkbn_fft_plan p, int64_t B, int64_t C) {
+  if (!p) return set_error(TKBN_ERR_INVALID, "fft plan is null");
+  if (p->ndim != g->ndim || p->dtype != g->dtype || p->batch != B * C)
+    return set_error(TKBN_ERR_INVALID, "fft plan does not match geometry/batch");
+  for (int d = 0; d < g->ndim; ++d)
+    if (p->n[d] != g->grid_size[d]) return set_error(TKBN_ERR_INVALID, "fft plan does not match grid size");
+  return TKBN_OK;
+}
+
+int fft_exec(tkbn_fft_plan p, void* data, int direction, cudaStream_t s) {
+  int rc = check_cufft(cufftSetStream(p->handle, s), "cufftSetStream");
+  if (rc) return rc;
+  if (p->dtype == TKBN_C64)
+    return check_cufft(cufftExecC2C(p->handle, (cufftComplex*)data, (cufftComplex*)data, direction), "cufftExecC2C");
+  return check_cufft(cufftExecZ2Z(p->handle, (cufftDoubleComplex*)data, (cufftDoubleComplex*)data, direction),
+                     "cufftExecZ2Z");
+}
+
+static int make_shape(const tkbn_geometry* g, Shape* s) {
+  s->ndim = g->ndim;
+  s->ntot = 1;
+  s->gtot = 1;
+  for (int d = 0; d < 3; ++d) {
+    s->N[d] = d < g->ndim ? (int)g->im_size[d] : 1;
+    s->K[d] = d < g->ndim ? (int)g->grid_size[d] : 1;
+  }
+  for (int d = 0; d < g->ndim; ++d) {
+    if (g->im_size[d] < 1 || g->grid_size[d] < g->im_size[d])
+      return set_error(TKBN_ERR_INVALID, "grid_size must be >= im_size in every dimension");
+    s->ntot *= g->im_size[d];
+    s->gtot *= g->grid_size[d];
+  }
+  return TKBN_OK;
+}
+
+static double ortho_scale(const Shape& s, int norm) { return norm == TKBN_NORM_ORTHO ? 1.0 / std::sqrt((double)s.gtot) : 1.0; }
+
+template <typename R>
+static int pad_scale_r(const Shape& s, int64_t B, int64_t C, int64_t ci, const void* image, const void* smaps,
+                       int64_t sb, const void* scaling, double scale, void* grid, cudaStream_t st) {
+  k_pad_scale<R><<<grid_blocks(B * C * s.gtot), 256, 0, st>>>(s, B, C, ci, (const cplx<R>*)image,
+                                                                (const cplx<R>*)smaps, sb, (const cplx<R>*)scaling,
+                                                                (R)scale, (cplx<R>*)grid);
+  return check_cuda(cudaGetLastError(), "pad_scale launch");
+}
+
+template <typename R>
+static int crop_scale_r(const Shape& s, int64_t B, int64_t C, const void* grid, const void* smaps, int64_t sb,
+                        const void* scaling, double scale, void* out, cudaStream_t st) {
+  const int64_t co = smaps ? 1 : C;
+  k_crop_scale<R><<<grid_blocks(B * co * s.ntot), 256, 0, st>>>(s, B, C, (const cplx<R>*)grid,
+                                                                  (const cplx<R>*)smaps, sb, (const cplx<R>*)scaling,
+                                                                  (R)scale, (cplx<R>*)out);
+  return check_cuda(cudaGetLastError(), "crop_scale launch");
+}
+
+int fft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, const void* smaps,
+                  int64_t smaps_batch, const void* scaling, int64_t B, int64_t C, int norm, void* grid,
+                  cudaStream_t st) {
+  Shape s;
+  int rc = make_shape(g, &s);
+  if (rc || (rc = check_plan(g, plan, B, C))) return rc;
+  if (!image || !grid) return set_error(TKBN_ERR_INVALID, "null image or grid");
+  if (smaps && smaps_batch != 1 && smaps_batch != B) return set_error(TKBN_ERR_INVALID, "smaps batch must be 1 or B");
+  if (norm != TKBN_NORM_NONE && norm != TKBN_NORM_ORTHO) return set_error(TKBN_ERR_INVALID, "Only option for norm is 'ortho'.");
+  const int64_t ci = smaps ? 1 : C;
+  const double sc = ortho_scale(s, norm);
+  rc = g->dtype == TKBN_C64 ? pad_scale_r<float>(s, B, C, ci, image, smaps, smaps_batch, scaling, sc, grid, st)
+                            : pad_scale_r<double>(s, B, C, ci, image, smaps, smaps_batch, scaling, sc, grid, st);
+  if (rc) return rc;
+  return fft_exec(plan, grid, CUFFT_FORWARD, st);
+}
+
+int ifft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, void* grid, const void* smaps, int64_t smaps_batch,
+                   const void* scaling, int64_t B, int64_t C, int norm, void* image, cudaStream_t st) {
+  Shape s;
+  int rc = make_shape(g, &s);
+  if (rc || (rc = check_plan(g, plan, B, C))) return rc;
+  if (!image || !grid) return set_error(TKBN_ERR_INVALID, "null image or grid");
+  if (smaps && smaps_batch != 1 && smaps_batch != B) return set_error(TKBN_ERR_INVALID, "smaps batch must be 1 or B");
+  if (norm != TKBN_NORM_NONE && norm != TKBN_NORM_ORTHO) return set_error(TKBN_ERR_INVALID, "Only option for norm is 'ortho'.");
+  rc = fft_exec(plan, grid, CUFFT_INVERSE, st);
+  if (rc) return rc;
+  const double sc = ortho_scale(s, norm);
+  return g->dtype == TKBN_C64 ? crop_scale_r<float>(s, B, C, grid, smaps, smaps_batch, scaling, sc, image, st)
+                              : crop_scale_r<double>(s, B, C, grid, smaps, smaps_batch, scaling, sc, image, st);
+}
+
+int toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, const void* kernel, int64_t kbatch,
+               const void* smaps, int64_t smaps_batch, int64_t B, int64_t C, int norm, void* grid, void* out,
+               cudaStream_t st) {
+  Shape s;
+  int rc = make_shape(g, &s);
+  if (rc || (rc = check_plan(g, plan, B, C))) return rc;
+  if (!image || !kernel || !grid || !out) return set_error(TKBN_ERR_INVALID, "null pointer argument");
+  if (kbatch != 1 && kbatch != B) return set_error(TKBN_ERR_INVALID, "If using batch dimension, kernel must have same batch size as image");
+  if (smaps && smaps_batch != 1 && smaps_batch != B) return set_error(TKBN_ERR_INVALID, "smaps batch must be 1 or B");
+  if (norm != TKBN_NORM_NONE && norm != TKBN_NORM_ORTHO) return set_error(TKBN_ERR_INVALID, "Only option for norm is 'ortho'.");
+  const double sc = ortho_scale(s, norm);
+  const int64_t ci = smaps ? 1 : C;
+  if (g->dtype == TKBN_C64) {
+    if ((rc = pad_scale_r<float>(s, B, C, ci, image, smaps, smaps_batch, nullptr, sc, grid, st))) return rc;
+    if ((rc = fft_exec(plan, grid, CUFFT_FORWARD, st))) return rc;
+    k_kernel_mul<float><<<grid_blocks(B * C * s.gtot), 256, 0, st>>>(s.gtot, B, C, (const float2*)kernel, kbatch,
+                                                                       (float)sc, (float2*)grid);
+    if ((rc = check_cuda(cudaGetLastError(), "kernel_mul launch"))) return rc;
+    if ((rc = fft_exec(plan, grid, CUFFT_INVERSE, st))) return rc;
+    return crop_scale_r<float>(s, B, C, grid, smaps, smaps_batch, nullptr, 1.0, out, st);
+  }
+  if ((rc = pad_scale_r<double>(s, B, C, ci, image, smaps, smaps_batch, nullptr, sc, grid, st))) return rc;
+  if ((rc = fft_exec(plan, grid, CUFFT_FORWARD, st))) return rc;
+  k_kernel_mul<double><<<grid_blocks(B * C * s.gtot), 256, 0, st>>>(s.gtot, B, C, (const double2*)kernel, kbatch, sc,
+                                                                      (double2*)grid);
+  if ((rc = check_cuda(cudaGetLastError(), "kernel_mul launch"))) return rc;
+  if ((rc = fft_exec(plan, grid, CUFFT_INVERSE, st))) return rc;
+  return crop_scale_r<double>(s, B, C, grid, smaps, smaps_batch, nullptr, 1.0, out, st);
+}
+
+}  // namespace tkbn_host

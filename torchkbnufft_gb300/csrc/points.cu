@@ -1,0 +1,254 @@
+// K1: trajectory layout — bin-sort of k-space points by grid tile.
+//
+// Replaces the float-key sort of the reference adjoint (sort_one_batch,
+// torchkbnufft/_nufft/interp.py:551-584). Points are keyed by the tile that
+// holds the first cell of their J^d footprint; a stable radix sort keeps the
+// original point order inside each tile, so consecutive points of a spoke stay
+// adjacent. The sorted coordinates, original indices and a list of work items
+// (at most `chunk` points of one tile each) are written to a caller-owned
+// workspace; the interpolation kernels read only that workspace.
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <cstdarg>
+#include <cstdio>
+
+#include "tkbn_common.cuh"
+#include "geo_host.cuh"
+
+namespace tkbn {
+
+template <typename R>
+__global__ void k_point_keys(Geo<R> geo, const R* __restrict__ omega, int64_t M, int64_t ntraj,
+                             uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+  const int64_t n = M * ntraj;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = i / M;
+    const int64_t m = i - t * M;
+    int key = 0;
+    bool ok = true;
+    for (int d = 0; d < geo.ndim; ++d) {
+      R om = omega[(t * geo.ndim + d) * M + m];
+      R tm;
+      int base;
+      ok = ok && base_index<R>(om, geo.gam[d], geo.halfJ[d], &tm, &base);
+      int tile = pmod(base, geo.K[d]) / geo.T[d];
+      key = key * geo.ntile[d] + tile;
+    }
+    if (!ok) {
+      atomicOr(&g_status, kStatusNonFinite);
+      key = 0;
+    }
+    keys[i] = (uint32_t)(t * geo.ntiles + key);
+    vals[i] = (int32_t)i;
+  }
+}
+
+__global__ void k_count_keys(const uint32_t* __restrict__ keys, int64_t n, int32_t* __restrict__ counts) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&counts[keys[i]], 1);
+}
+
+__global__ void k_items_per_key(const int32_t* __restrict__ counts, int64_t nkeys, int chunk,
+                                int32_t* __restrict__ nit) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nkeys; k += (int64_t)gridDim.x * blockDim.x)
+    nit[k] = (counts[k] + chunk - 1) / chunk;
+}
+
+__global__ void k_fill_items(const int32_t* __restrict__ counts, const int32_t* __restrict__ tile_off,
+                             const int32_t* __restrict__ nit, const int32_t* __restrict__ item_off, int64_t nkeys,
+                             int chunk, Item* __restrict__ items, int64_t* __restrict__ hdr) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nkeys; k += (int64_t)gridDim.x * blockDim.x) {
+    const int c = counts[k];
+    const int o = item_off[k];
+    for (int q = 0; q < nit[k]; ++q) {
+      Item it;
+      it.key = (int)k;
+      it.start = tile_off[k] + q * chunk;
+      it.len = min(chunk, c - q * chunk);
+      it.pad = 0;
+      items[o + q] = it;
+    }
+    if (k == nkeys - 1) hdr[0] = (int64_t)o + nit[k];
+  }
+}
+
+template <typename R>
+__global__ void k_sorted_coords(const R* __restrict__ omega, const int32_t* __restrict__ vals, int64_t M,
+                                int ndim, int64_t n, R* __restrict__ coords) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t v = vals[i];
+    const int64_t t = v / M;
+    const int64_t m = v - t * M;
+    for (int d = 0; d < ndim; ++d) coords[d * n + i] = omega[(t * ndim + d) * M + m];
+  }
+}
+
+}  // namespace tkbn
+
+namespace tkbn_host {
+
+static thread_local char g_errbuf[512];
+const char* last_error() { return g_errbuf; }
+
+int set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_errbuf, sizeof(g_errbuf), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int check_cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return TKBN_OK;
+  return set_error(TKBN_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+void default_tiles(const tkbn_geometry* g, int tile[3], int* chunk) {
+  const int dflt2 = g->dtype == TKBN_C64 ? 16 : 16;
+  for (int d = 0; d < 3; ++d) tile[d] = 1;
+  if (g->ndim == 1) {
+    tile[0] = 128;
+  } else if (g->ndim == 2) {
+    tile[0] = tile[1] = dflt2;
+  } else {
+    tile[0] = tile[1] = tile[2] = 4;
+  }
+  *chunk = 256;
+}
+
+static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayout* L) {
+  if (!g || !p || !L) return set_error(TKBN_ERR_INVALID, "null argument");
+  if (g->ndim < 1 || g->ndim > 3) return set_error(TKBN_ERR_UNSUPPORTED, "ndim must be 1, 2 or 3 (got %d)", g->ndim);
+  if (p->npts < 0 || p->ntraj < 1) return set_error(TKBN_ERR_INVALID, "npts must be >= 0 and ntraj >= 1");
+  int dtile[3], dchunk;
+  default_tiles(g, dtile, &dchunk);
+  int64_t ntiles = 1;
+  for (int d = 0; d < g->ndim; ++d) {
+    if (g->grid_size[d] < 1 || g->grid_size[d] > (1 << 24))
+      return set_error(TKBN_ERR_INVALID, "grid_size[%d] out of range", d);
+    int t = p->tile[d] > 0 ? p->tile[d] : dtile[d];
+    if (t > g->grid_size[d]) t = (int)g->grid_size[d];
+    L->tile[d] = t;
+    L->ntile[d] = (int)((g->grid_size[d] + t - 1) / t);
+    ntiles *= L->ntile[d];
+  }
+  for (int d = g->ndim; d < 3; ++d) {
+    L->tile[d] = 1;
+    L->ntile[d] = 1;
+  }
+  L->chunk = p->chunk > 0 ? p->chunk : dchunk;
+  L->nkeys = ntiles * p->ntraj;
+  L->npts_total = p->npts * p->ntraj;
+  if (L->nkeys >= (int64_t)1 << 31 || L->npts_total >= (int64_t)1 << 31)
+    return set_error(TKBN_ERR_INVALID, "trajectory too large for 32-bit point indices");
+  L->max_items = L->nkeys + (L->npts_total + L->chunk - 1) / L->chunk;
+  int bits = 1;
+  while (((int64_t)1 << bits) < L->nkeys) ++bits;
+  L->key_bits = bits;
+
+  const int64_t n = L->npts_total > 0 ? L->npts_total : 1;
+  const size_t rsize = g->dtype == TKBN_C64 ? 4 : 8;
+  size_t cub_sort = 0, cub_scan = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, cub_sort, (uint32_t*)nullptr, (uint32_t*)nullptr, (int32_t*)nullptr,
+                                  (int32_t*)nullptr, (int)n, 0, bits);
+  cub::DeviceScan::ExclusiveSum(nullptr, cub_scan, (int32_t*)nullptr, (int32_t*)nullptr, (int)L->nkeys);
+  L->cub_bytes = cub_sort > cub_scan ? cub_sort : cub_scan;
+
+  size_t o = 0;
+  L->off_hdr = o;
+  o = align_up(o + 64);
+  L->off_keys_in = o;
+  o = align_up(o + 4 * n);
+  L->off_vals_in = o;
+  o = align_up(o + 4 * n);
+  L->off_keys = o;
+  o = align_up(o + 4 * n);
+  L->off_vals = o;
+  o = align_up(o + 4 * n);
+  L->off_counts = o;
+  o = align_up(o + 4 * L->nkeys);
+  L->off_tile_off = o;
+  o = align_up(o + 4 * (L->nkeys + 1));
+  L->off_nit = o;
+  o = align_up(o + 4 * L->nkeys);
+  L->off_item_off = o;
+  o = align_up(o + 4 * (L->nkeys + 1));
+  L->off_items = o;
+  o = align_up(o + sizeof(tkbn::Item) * L->max_items);
+  L->off_coords = o;
+  o = align_up(o + rsize * g->ndim * n);
+  L->off_cub = o;
+  o = align_up(o + L->cub_bytes);
+  L->total = o;
+  return TKBN_OK;
+}
+
+template <typename R>
+static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const PointsLayout& L, const void* omega,
+                      char* ws, cudaStream_t s) {
+  using namespace tkbn;
+  Geo<R> geo = make_geo<R>(g, &L, nullptr, nullptr);
+  const int64_t n = L.npts_total;
+  uint32_t* keys_in = (uint32_t*)(ws + L.off_keys_in);
+  int32_t* vals_in = (int32_t*)(ws + L.off_vals_in);
+  uint32_t* keys = (uint32_t*)(ws + L.off_keys);
+  int32_t* vals = (int32_t*)(ws + L.off_vals);
+  int32_t* counts = (int32_t*)(ws + L.off_counts);
+  int32_t* tile_off = (int32_t*)(ws + L.off_tile_off);
+  int32_t* nit = (int32_t*)(ws + L.off_nit);
+  int32_t* item_off = (int32_t*)(ws + L.off_item_off);
+  Item* items = (Item*)(ws + L.off_items);
+  R* coords = (R*)(ws + L.off_coords);
+  int64_t* hdr = (int64_t*)(ws + L.off_hdr);
+  void* cubtmp = ws + L.off_cub;
+
+  int rc;
+  if ((rc = check_cuda(cudaMemsetAsync(ws + L.off_hdr, 0, 64, s), "memset header"))) return rc;
+  if ((rc = check_cuda(cudaMemsetAsync(counts, 0, 4 * L.nkeys, s), "memset counts"))) return rc;
+  const int threads = 256;
+  auto blocks_for = [&](int64_t work) {
+    int64_t b = (work + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 152 * 32) b = 152 * 32;
+    return (int)b;
+  };
+  if (n > 0) {
+    k_point_keys<R><<<blocks_for(n), threads, 0, s>>>(geo, (const R*)omega, p->npts, p->ntraj, keys_in, vals_in);
+    size_t tb = L.cub_bytes;
+    if (cub::DeviceRadixSort::SortPairs(cubtmp, tb, keys_in, keys, vals_in, vals, (int)n, 0, L.key_bits, s) !=
+        cudaSuccess)
+      return set_error(TKBN_ERR_CUDA, "radix sort failed");
+    k_count_keys<<<blocks_for(n), threads, 0, s>>>(keys, n, counts);
+  }
+  k_items_per_key<<<blocks_for(L.nkeys), threads, 0, s>>>(counts, L.nkeys, L.chunk, nit);
+  size_t tb = L.cub_bytes;
+  if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, counts, tile_off, (int)L.nkeys, s) != cudaSuccess)
+    return set_error(TKBN_ERR_CUDA, "scan failed");
+  tb = L.cub_bytes;
+  if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, nit, item_off, (int)L.nkeys, s) != cudaSuccess)
+    return set_error(TKBN_ERR_CUDA, "scan failed");
+  k_fill_items<<<blocks_for(L.nkeys), threads, 0, s>>>(counts, tile_off, nit, item_off, L.nkeys, L.chunk, items, hdr);
+  if (n > 0) k_sorted_coords<R><<<blocks_for(n), threads, 0, s>>>((const R*)omega, vals, p->npts, g->ndim, n, coords);
+  return check_cuda(cudaGetLastError(), "points build launch");
+}
+
+int points_build(const tkbn_geometry* g, const tkbn_points_desc* p, const void* omega, void* ws, size_t bytes,
+                 cudaStream_t s) {
+  PointsLayout L;
+  int rc = points_layout(g, p, &L);
+  if (rc) return rc;
+  if (!ws) return set_error(TKBN_ERR_INVALID, "workspace is null");
+  if (bytes < L.total) return set_error(TKBN_ERR_INVALID, "workspace too small: %zu < %zu", bytes, L.total);
+  if (p->npts > 0 && !omega) return set_error(TKBN_ERR_INVALID, "omega is null");
+  if (g->dtype == TKBN_C64) return build_impl<float>(g, p, L, omega, (char*)ws, s);
+  if (g->dtype == TKBN_C128) return build_impl<double>(g, p, L, omega, (char*)ws, s);
+  return set_error(TKBN_ERR_UNSUPPORTED, "unsupported dtype %d", g->dtype);
+}
+
+}  // namespace tkbn_host
+
+TKBN_DEFINE_STATUS_READER(status_points)

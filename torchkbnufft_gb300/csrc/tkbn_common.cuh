@@ -1,0 +1,219 @@
+// Shared device helpers for the sm_103a table-mode KB NUFFT kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/tkbn_gb300.h"
+
+namespace tkbn {
+
+constexpr int kMaxDim = 3;
+constexpr int kMaxJ = 8;  // numpoints supported per dimension
+
+// Device status bits (OR-ed into g_status by kernels whose own checks fail).
+constexpr int kStatusNonFinite = 1;     // a trajectory coordinate was NaN/Inf or out of range
+constexpr int kStatusOutsidePatch = 2;  // a point's footprint left its tile patch (layout mismatch)
+constexpr int kStatusBadItem = 4;       // malformed work item
+
+// One status word per translation unit (static linkage, no relocatable device
+// code needed); each unit exposes a host reader, see TKBN_DEFINE_STATUS_READER.
+static __device__ int g_status;
+
+// ---------------------------------------------------------------- complex
+template <typename R>
+struct Cplx;
+template <>
+struct Cplx<float> {
+  using T = float2;
+};
+template <>
+struct Cplx<double> {
+  using T = double2;
+};
+template <typename R>
+using cplx = typename Cplx<R>::T;
+
+template <typename R>
+__host__ __device__ __forceinline__ cplx<R> mk(R re, R im) {
+  cplx<R> z;
+  z.x = re;
+  z.y = im;
+  return z;
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> cmul(cplx<R> a, cplx<R> b) {
+  return mk<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename R>
+__device__ __forceinline__ cplx<R> cmulc(cplx<R> a, cplx<R> b) {
+  return mk<R>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+// acc + a * b
+template <typename R>
+__device__ __forceinline__ cplx<R> cfma(cplx<R> a, cplx<R> b, cplx<R> acc) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+  return acc;
+}
+// acc + conj(a) * b
+template <typename R>
+__device__ __forceinline__ cplx<R> cfmac(cplx<R> a, cplx<R> b, cplx<R> acc) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(-a.y, b.x, acc.y);
+  return acc;
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> cscale(cplx<R> a, R s) {
+  return mk<R>(a.x * s, a.y * s);
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> cconj(cplx<R> a) {
+  return mk<R>(a.x, -a.y);
+}
+
+// Correctly rounded single operations, never contracted into FMAs. The
+// reference evaluates these steps as separate tensor ops, so each result is
+// rounded on its own; matching that keeps table-bin selection bit-identical.
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ void sincos_acc(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ void sincos_acc(double x, double* s, double* c) { sincos(x, s, c); }
+
+// ---------------------------------------------------------------- geometry
+// Per-launch constants for interpolation kernels (passed by value).
+template <typename R>
+struct Geo {
+  int ndim;
+  int K[kMaxDim];        // grid size
+  int J[kMaxDim];        // numpoints
+  int L[kMaxDim];        // table oversampling
+  int center[kMaxDim];   // floor(J*L/2)
+  int tmax[kMaxDim];     // last valid table index (J*L)
+  int T[kMaxDim];        // tile edge (cells)
+  int P[kMaxDim];        // patch extent T + J - 1
+  int ntile[kMaxDim];    // tiles per dim
+  int ntiles;            // prod ntile
+  R gam[kMaxDim];        // fl(fl(1/K) * fl(2 pi))
+  R halfJ[kMaxDim];      // J / 2
+  R Lr[kMaxDim];         // L as R
+  R nshift[kMaxDim];
+  const cplx<R>* tab[kMaxDim];
+  const cplx<R>* dtab[kMaxDim];
+};
+
+// Work item of the sorted layout: points [start, start+len) of tile `key`.
+struct Item {
+  int key;
+  int start;
+  int len;
+  int pad;
+};
+
+// Positive modulo.
+__device__ __forceinline__ int pmod(int a, int k) {
+  int r = a % k;
+  return r < 0 ? r + k : r;
+}
+
+// First neighbour index of a point along one dimension: 1 + floor(tm - J/2),
+// with tm = omega / gam (torchkbnufft/_nufft/interp.py:171, 177). Returns
+// false for coordinates that are not finite or far outside any grid.
+template <typename R>
+__device__ __forceinline__ bool base_index(R om, R gam, R halfJ, R* tm_out, int* base_out) {
+  R tm = div_rn(om, gam);
+  R f = floor(sub_rn(tm, halfJ));
+  *tm_out = tm;
+  if (!(fabs(f) < R(1 << 30))) {
+    *base_out = 0;
+    return false;
+  }
+  *base_out = 1 + (int)f;
+  return true;
+}
+
+// Table bin for the neighbour at cell g: round_half_even((tm - g) * L) + center
+// (torchkbnufft/_nufft/interp.py:129-132), clamped to the table.
+template <typename R>
+__device__ __forceinline__ int table_bin(R tm, int g, R Lr, int center, int tmax) {
+  R s = mul_rn(sub_rn(tm, (R)g), Lr);
+  int k = (int)rint(s) + center;
+  return min(max(k, 0), tmax);
+}
+
+// fftshift phase argument sum_d omega_d * n_shift_d with each product rounded
+// before the sum (torchkbnufft/_nufft/interp.py:200-203).
+template <typename R, int D>
+__device__ __forceinline__ R phase_arg(const R* om, const R* nshift) {
+  R a = mul_rn(om[0], nshift[0]);
+#pragma unroll
+  for (int d = 1; d < D; ++d) a = add_rn(a, mul_rn(om[d], nshift[d]));
+  return a;
+}
+
+}  // namespace tkbn
+
+// Host-side helpers shared by the .cu files.
+namespace tkbn_host {
+
+int set_error(int code, const char* fmt, ...);
+int check_cuda(cudaError_t e, const char* what);
+
+// Byte layout of the sorted-point workspace.
+struct PointsLayout {
+  int64_t nkeys;       // ntraj * ntiles
+  int64_t npts_total;  // ntraj * M
+  int64_t max_items;   // upper bound on work items
+  int key_bits;
+  int tile[3];
+  int ntile[3];
+  int chunk;
+  size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
+      off_items, off_coords, off_cub;
+  size_t cub_bytes;
+  size_t total;
+};
+
+int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayout* out);
+
+// Default tile edge and chunk per dimension count.
+void default_tiles(const tkbn_geometry* g, int tile[3], int* chunk);
+
+// Per-unit status readers (read and clear; synchronise the stream).
+int status_points(cudaStream_t s, int* st);
+int status_interp(cudaStream_t s, int* st);
+int status_fft(cudaStream_t s, int* st);
+
+}  // namespace tkbn_host
+
+#define TKBN_DEFINE_STATUS_READER(NAME)                                                   \
+  namespace tkbn_host {                                                                    \
+  int NAME(cudaStream_t s, int* st) {                                                      \
+    int v = 0;                                                                             \
+    int rc = check_cuda(cudaMemcpyFromSymbolAsync(&v, tkbn::g_status, sizeof(int), 0,     \
+                                                  cudaMemcpyDeviceToHost, s),              \
+                        "read status");                                                    \
+    if (rc) return rc;                                                                     \
+    rc = check_cuda(cudaStreamSynchronize(s), "sync for status");                         \
+    if (rc) return rc;                                                                     \
+    const int zero = 0;                                                                    \
+    rc = check_cuda(cudaMemcpyToSymbolAsync(tkbn::g_status, &zero, sizeof(int), 0,         \
+                                            cudaMemcpyHostToDevice, s),                    \
+                    "clear status");                                                       \
+    if (rc) return rc;                                                                     \
+    rc = check_cuda(cudaStreamSynchronize(s), "sync for status");                         \
+    *st |= v;                                                                              \
+    return rc;                                                                             \
+  }                                                                                        \
+  }
