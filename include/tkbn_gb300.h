@@ -143,7 +143,9 @@ int tkbn_nufft_adj(const tkbn_geometry* g, const tkbn_points_desc* p, const void
                    void* grid_scratch, void* image, void* stream);
 
 /* out = crop(IFFT(kernel * FFT(zero_pad(image)))) per channel. geometry:
- * im_size = image spatial size, grid_size = kernel size. kernel_batch = 1 or nbatch. */
+ * im_size = image spatial size, grid_size = kernel size. kernel_batch = 1
+ * (shared) or ncoil: kernel k filters channel k of every batch item, which is
+ * how torch broadcasts a (K, *grid) kernel against a (B, C, *grid) spectrum. */
 int tkbn_fft_filter(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, const void* kernel,
                     int64_t kernel_batch, int64_t nbatch, int64_t ncoil, int norm, void* grid_scratch,
                     void* out, void* stream);

@@ -161,20 +161,20 @@ class ToepApply(Function):
     """Toeplitz normal operator; backward applies the conjugate kernel."""
 
     @staticmethod
-    def forward(ctx, image, kernel, smaps, norm, kernel_batched):
+    def forward(ctx, image, kernel, smaps, norm, kernel_mode):
         if kernel.requires_grad:
             raise NotImplementedError("gradients with respect to the Toeplitz kernel are not supported")
         R.require_cuda(image, kernel, smaps)
-        ctx.norm, ctx.kernel_batched = norm, kernel_batched
+        ctx.norm, ctx.kernel_mode = norm, kernel_mode
         ctx.save_for_backward(kernel, smaps)
-        return R.toep_apply(image, kernel, smaps, norm, kernel_batched)
+        return R.toep_apply(image, kernel, smaps, norm, kernel_mode)
 
     @staticmethod
     def backward(ctx, grad):
         kernel, smaps = ctx.saved_tensors
         gi = None
         if ctx.needs_input_grad[0]:
-            gi = R.toep_apply(grad, kernel.conj(), smaps, ctx.norm, ctx.kernel_batched)
+            gi = R.toep_apply(grad, kernel.conj(), smaps, ctx.norm, ctx.kernel_mode)
         if smaps is not None and ctx.needs_input_grad[2]:
             raise NotImplementedError("gradients with respect to smaps in ToepNufft are not supported")
         return gi, None, None, None, None

@@ -277,7 +277,7 @@ _dtable_cache: "collections.OrderedDict" = collections.OrderedDict()
 def derivative_tables(tables: Sequence[torch.Tensor], table_oversamp: Sequence[int]) -> List[torch.Tensor]:
     """d/du of each table by central differences on the table grid (step 1/L).
 
-    Error O(1/L^2) relative; one-sided at the ends. Cached by table identity.
+    Error O(1/L^2) relative inside the support. Cached by table identity.
     """
     out = []
     for t, Lo in zip(tables, table_oversamp):
@@ -287,10 +287,12 @@ def derivative_tables(tables: Sequence[torch.Tensor], table_oversamp: Sequence[i
             if hit is not None and hit[0]() is t:
                 out.append(hit[1])
                 continue
+        # entries 0 and J*L sit at u = -+J/2 where the truncated kernel is set to
+        # zero; the two end bins use one-sided differences of interior entries.
         d = torch.empty_like(t)
         d[1:-1] = (t[2:] - t[:-2]) * (Lo / 2.0)
-        d[0] = (t[1] - t[0]) * Lo
-        d[-1] = (t[-1] - t[-2]) * Lo
+        d[0] = d[1] = (t[2] - t[1]) * Lo
+        d[-1] = d[-2] = (t[-2] - t[-3]) * Lo
         with _lock:
             _dtable_cache[key] = (weakref.ref(t), d)
             while len(_dtable_cache) > 32:
@@ -437,8 +439,12 @@ def nufft_adj(geom: GeomKey, lay: PointsLayout, tables, scaling, kdata, smaps, n
 
 
 def toep_apply(image: torch.Tensor, kernel: torch.Tensor, smaps: Optional[torch.Tensor], norm: Optional[str],
-               kernel_batched: bool) -> torch.Tensor:
-    """Toeplitz normal operator / FFT filter on the oversampled grid of ``kernel``."""
+               kernel_mode: str) -> torch.Tensor:
+    """Toeplitz normal operator / FFT filter on the oversampled grid of ``kernel``.
+
+    kernel_mode: "shared" (kernel is ``*grid``), "batch" (``(B, *grid)``, one
+    per batch item; with smaps) or "channel" (``(C, *grid)``, one per channel).
+    """
     dev = require_cuda(image, kernel, smaps)
     image = image.contiguous()
     kernel = kernel.to(image.dtype).contiguous()
@@ -447,7 +453,7 @@ def toep_apply(image: torch.Tensor, kernel: torch.Tensor, smaps: Optional[torch.
     grid_size = tuple(kernel.shape[-nd:])
     geom = GeomKey(nd, dtype_code(image.dtype), im_size, grid_size, (1,) * nd, (1,) * nd, (0.0,) * nd)
     B = image.shape[0]
-    kb = kernel.shape[0] if kernel_batched else 1
+    kb = 1 if kernel_mode == "shared" else kernel.shape[0]
     if smaps is not None:
         smaps = smaps.to(image.dtype).contiguous()
         C = smaps.shape[1]

@@ -24,8 +24,8 @@ int fft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image,
 int ifft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, void* grid, const void* smaps, int64_t smaps_batch,
                    const void* scaling, int64_t B, int64_t C, int norm, void* image, cudaStream_t st);
 int toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, const void* kernel, int64_t kbatch,
-               const void* smaps, int64_t smaps_batch, int64_t B, int64_t C, int norm, void* grid, void* out,
-               cudaStream_t st);
+               int by_channel, const void* smaps, int64_t smaps_batch, int64_t B, int64_t C, int norm, void* grid,
+               void* out, cudaStream_t st);
 }  // namespace tkbn_host
 
 using namespace tkbn_host;
@@ -165,7 +165,7 @@ int tkbn_fft_filter(const tkbn_geometry* g, tkbn_fft_plan plan, const void* imag
                     void* stream) {
   int rc = check_geometry(g);
   if (rc) return rc;
-  TKBN_GUARD(toep_apply(g, plan, image, kernel, kernel_batch, nullptr, 1, nbatch, ncoil, norm, grid_scratch, out,
+  TKBN_GUARD(toep_apply(g, plan, image, kernel, kernel_batch, 1, nullptr, 1, nbatch, ncoil, norm, grid_scratch, out,
                         (cudaStream_t)stream));
 }
 
@@ -175,8 +175,8 @@ int tkbn_toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* imag
   int rc = check_geometry(g);
   if (rc) return rc;
   if (!smaps) return set_error(TKBN_ERR_INVALID, "smaps is null (use tkbn_fft_filter without maps)");
-  TKBN_GUARD(toep_apply(g, plan, image, kernel, kernel_batch, smaps, smaps_batch, nbatch, ncoil, norm, grid_scratch,
-                        out, (cudaStream_t)stream));
+  TKBN_GUARD(toep_apply(g, plan, image, kernel, kernel_batch, 0, smaps, smaps_batch, nbatch, ncoil, norm,
+                        grid_scratch, out, (cudaStream_t)stream));
 }
 
 }  // extern "C"

@@ -113,16 +113,18 @@ __global__ void k_crop_scale(Shape s, int64_t B, int64_t C, const cplx<R>* __res
   }
 }
 
-// K6. grid[b, c, g] *= kernel[kb, g] * scale, kb = b when the kernel is batched.
+// K6. grid[b, c, g] *= kernel[k, g] * scale with k = 0 (shared kernel), b
+// (one kernel per batch item) or c (one kernel per channel: torch
+// broadcasting of a (K, *grid) kernel against (B, C, *grid)).
 template <typename R>
 __global__ void k_kernel_mul(int64_t gtot, int64_t B, int64_t C, const cplx<R>* __restrict__ kernel, int64_t kbatch,
-                             R scale, cplx<R>* __restrict__ grid) {
+                             int by_channel, R scale, cplx<R>* __restrict__ grid) {
   const int64_t total = B * C * gtot;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t bc = e / gtot;
     const int64_t g = e - bc * gtot;
-    const int64_t b = bc / C;
-    grid[e] = cscale<R>(cmul<R>(grid[e], kernel[(kbatch == 1 ? 0 : b) * gtot + g]), scale);
+    const int64_t k = kbatch == 1 ? 0 : (by_channel ? bc % C : bc / C);
+    grid[e] = cscale<R>(cmul<R>(grid[e], kernel[k * gtot + g]), scale);
   }
 }
 
@@ -275,13 +277,16 @@ int ifft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, void* grid, const
 }
 
 int toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, const void* kernel, int64_t kbatch,
-               const void* smaps, int64_t smaps_batch, int64_t B, int64_t C, int norm, void* grid, void* out,
-               cudaStream_t st) {
+               int by_channel, const void* smaps, int64_t smaps_batch, int64_t B, int64_t C, int norm, void* grid,
+               void* out, cudaStream_t st) {
   Shape s;
   int rc = make_shape(g, &s);
   if (rc || (rc = check_plan(g, plan, B, C))) return rc;
   if (!image || !kernel || !grid || !out) return set_error(TKBN_ERR_INVALID, "null pointer argument");
-  if (kbatch != 1 && kbatch != B) return set_error(TKBN_ERR_INVALID, "If using batch dimension, kernel must have same batch size as image");
+  if (!by_channel && kbatch != 1 && kbatch != B)
+    return set_error(TKBN_ERR_INVALID, "If using batch dimension, kernel must have same batch size as image");
+  if (by_channel && kbatch != 1 && kbatch != C)
+    return set_error(TKBN_ERR_INVALID, "kernel batch must be 1 or the channel count");
   if (smaps && smaps_batch != 1 && smaps_batch != B) return set_error(TKBN_ERR_INVALID, "smaps batch must be 1 or B");
   if (norm != TKBN_NORM_NONE && norm != TKBN_NORM_ORTHO) return set_error(TKBN_ERR_INVALID, "Only option for norm is 'ortho'.");
   const double sc = ortho_scale(s, norm);
@@ -290,15 +295,15 @@ int toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, co
     if ((rc = pad_scale_r<float>(s, B, C, ci, image, smaps, smaps_batch, nullptr, sc, grid, st))) return rc;
     if ((rc = fft_exec(plan, grid, CUFFT_FORWARD, st))) return rc;
     k_kernel_mul<float><<<grid_blocks(B * C * s.gtot), 256, 0, st>>>(s.gtot, B, C, (const float2*)kernel, kbatch,
-                                                                       (float)sc, (float2*)grid);
+                                                                       by_channel, (float)sc, (float2*)grid);
     if ((rc = check_cuda(cudaGetLastError(), "kernel_mul launch"))) return rc;
     if ((rc = fft_exec(plan, grid, CUFFT_INVERSE, st))) return rc;
     return crop_scale_r<float>(s, B, C, grid, smaps, smaps_batch, nullptr, 1.0, out, st);
   }
   if ((rc = pad_scale_r<double>(s, B, C, ci, image, smaps, smaps_batch, nullptr, sc, grid, st))) return rc;
   if ((rc = fft_exec(plan, grid, CUFFT_FORWARD, st))) return rc;
-  k_kernel_mul<double><<<grid_blocks(B * C * s.gtot), 256, 0, st>>>(s.gtot, B, C, (const double2*)kernel, kbatch, sc,
-                                                                      (double2*)grid);
+  k_kernel_mul<double><<<grid_blocks(B * C * s.gtot), 256, 0, st>>>(s.gtot, B, C, (const double2*)kernel, kbatch,
+                                                                      by_channel, sc, (double2*)grid);
   if ((rc = check_cuda(cudaGetLastError(), "kernel_mul launch"))) return rc;
   if ((rc = fft_exec(plan, grid, CUFFT_INVERSE, st))) return rc;
   return crop_scale_r<double>(s, B, C, grid, smaps, smaps_batch, nullptr, 1.0, out, st);

@@ -80,27 +80,53 @@ __device__ __forceinline__ void job_decode(const Geo<R>& geo, const Item& it, in
   *b_out = ntraj == 1 ? bb : t;
 }
 
-// Stage Cc coil planes of the periodic patch [origin, origin + P) into smem.
+// Row decomposition of a patch: a row is P[D-1] cells contiguous in smem and
+// (up to the periodic wrap) contiguous in the global grid.
+template <typename R, int D>
+__device__ __forceinline__ int64_t patch_row_base(const Geo<R>& geo, int row, const int* origin, int64_t* gstride_x) {
+  // row -> (c is handled by the caller), outer coordinates
+  int64_t flat = 0, stride = geo.K[D - 1];
+#pragma unroll
+  for (int d = D - 2; d >= 0; --d) {
+    const int p = row % geo.P[d];
+    row /= geo.P[d];
+    flat += (int64_t)pmod(origin[d] + p, geo.K[d]) * stride;
+    stride *= geo.K[d];
+  }
+  *gstride_x = 1;
+  return flat;
+}
+
+// Stage Cc coil planes of the periodic patch [origin, origin + P) into smem:
+// one warp per patch row, lanes along the innermost dimension.
 template <typename R, int D>
 __device__ __forceinline__ void load_patch(const Geo<R>& geo, const cplx<R>* __restrict__ grid, int64_t plane0,
                                            int64_t gtot, int ncl, int cells, int ps, const int* origin,
                                            cplx<R>* patch) {
-  for (int idx = threadIdx.x; idx < ncl * cells; idx += blockDim.x) {
-    const int c = idx / cells;
-    int cell = idx - c * cells;
-    int64_t flat = 0;
-    int64_t stride = 1;
-#pragma unroll
-    for (int d = D - 1; d >= 0; --d) {
-      const int p = cell % geo.P[d];
-      cell /= geo.P[d];
-      const int gidx = pmod(origin[d] + p, geo.K[d]);
-      flat += gidx * stride;
-      stride *= geo.K[d];
+  const int PX = geo.P[D - 1];
+  const int KX = geo.K[D - 1];
+  const int rows_per_plane = cells / PX;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int r = warp; r < ncl * rows_per_plane; r += nwarps) {
+    const int c = r / rows_per_plane;
+    const int rr = r - c * rows_per_plane;
+    int64_t sx;
+    const cplx<R>* src = grid + (plane0 + c) * gtot + patch_row_base<R, D>(geo, rr, origin, &sx);
+    cplx<R>* dst = patch + c * ps + rr * PX;
+    for (int px = lane; px < PX; px += 32) {
+      int gx = origin[D - 1] + px;
+      gx = gx >= KX ? gx - KX * (gx / KX) : gx;
+      dst[px] = src[gx];
     }
-    patch[c * ps + (idx - c * cells)] = grid[(plane0 + c) * gtot + flat];
   }
 }
+
+// Add the staged patch into the global grid with vector atomics (cells that
+// stayed zero are skipped).
+template <typename R, int D>
+__device__ __forceinline__ void flush_patch(const Geo<R>& geo, cplx<R>* __restrict__ grid, int64_t plane0,
+                                            int64_t gtot, int ncl, int cells, int ps, const int* origin,
+                                            const cplx<R>* patch);
 
 template <typename R, int D, int JC>
 __device__ __forceinline__ cplx<R> gather_point(const Geo<R>& geo, const PointSetup<R, D, JC>& ps,
@@ -161,6 +187,30 @@ __device__ __forceinline__ void atomic_add_global(float2* p, float2 v) { atomicA
 __device__ __forceinline__ void atomic_add_global(double2* p, double2 v) {
   atomicAdd(&p->x, v.x);
   atomicAdd(&p->y, v.y);
+}
+
+template <typename R, int D>
+__device__ __forceinline__ void flush_patch(const Geo<R>& geo, cplx<R>* __restrict__ grid, int64_t plane0,
+                                            int64_t gtot, int ncl, int cells, int ps, const int* origin,
+                                            const cplx<R>* patch) {
+  const int PX = geo.P[D - 1];
+  const int KX = geo.K[D - 1];
+  const int rows_per_plane = cells / PX;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int r = warp; r < ncl * rows_per_plane; r += nwarps) {
+    const int c = r / rows_per_plane;
+    const int rr = r - c * rows_per_plane;
+    int64_t sx;
+    cplx<R>* dst = grid + (plane0 + c) * gtot + patch_row_base<R, D>(geo, rr, origin, &sx);
+    const cplx<R>* src = patch + c * ps + rr * PX;
+    for (int px = lane; px < PX; px += 32) {
+      const cplx<R> v = src[px];
+      if (v.x == R(0) && v.y == R(0)) continue;
+      int gx = origin[D - 1] + px;
+      gx = gx >= KX ? gx - KX * (gx / KX) : gx;
+      atomic_add_global(&dst[gx], v);
+    }
+  }
 }
 
 template <typename R, int D, int JC>
@@ -306,23 +356,7 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj(Geo<R> geo, Launch a, c
       if (!ps.ok && c == 0) atomicOr(&g_status, kStatusNonFinite | kStatusOutsidePatch);
     }
     __syncthreads();
-    // flush the patch: wrapped cells, skipped when untouched
-    for (int idx = threadIdx.x; idx < ncl * a.cells; idx += blockDim.x) {
-      const int cl = idx / a.cells;
-      const int cell0 = idx - cl * a.cells;
-      const cplx<R> v = patch[cl * a.ps + cell0];
-      if (v.x == R(0) && v.y == R(0)) continue;
-      int cell = cell0;
-      int64_t flat = 0, stride = 1;
-#pragma unroll
-      for (int d = D - 1; d >= 0; --d) {
-        const int p = cell % geo.P[d];
-        cell /= geo.P[d];
-        flat += pmod(origin[d] + p, geo.K[d]) * stride;
-        stride *= geo.K[d];
-      }
-      atomic_add_global(&grid[(b * a.C + c0 + cl) * a.gtot + flat], v);
-    }
+    flush_patch<R, D>(geo, grid, b * a.C + c0, a.gtot, ncl, a.cells, a.ps, origin, patch);
   }
 }
 
@@ -505,7 +539,7 @@ struct InterpPlan {
   PointsLayout L;
   Launch a;
   size_t smem;
-  int blocks;
+  int64_t max_jobs;
 };
 
 template <typename R>
@@ -548,11 +582,26 @@ static int prepare(const tkbn_geometry* g, const tkbn_points_desc* p, const void
   ip->smem = (size_t)a.Cc * a.ps * sizeof(cplx<R>);
   if (ip->smem > 220 * 1024)
     return set_error(TKBN_ERR_UNSUPPORTED, "tile patch needs %zu bytes of shared memory", ip->smem);
-  int64_t max_jobs = ip->L.max_items * a.nbpt * a.ncc;
-  int64_t blocks = 152 * 4;
-  if (max_jobs < blocks) blocks = max_jobs;
-  if (blocks < 1) blocks = 1;
-  ip->blocks = (int)blocks;
+  ip->max_jobs = ip->L.max_items * a.nbpt * a.ncc;
+  return TKBN_OK;
+}
+
+// Persistent grid: as many CTAs as are resident at once (no second wave), at
+// most one per job.
+template <typename K>
+static int resident_blocks(K kernel, size_t smem, int64_t max_jobs, int* blocks) {
+  int rc = check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                      "smem attribute");
+  if (rc) return rc;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice"))) return rc;
+  if ((rc = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"))) return rc;
+  if ((rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem), "occupancy")))
+    return rc;
+  if (per_sm < 1) return set_error(TKBN_ERR_UNSUPPORTED, "interpolation kernel cannot be resident with %zu B smem", smem);
+  int64_t b = (int64_t)per_sm * sms;
+  if (max_jobs < b) b = max_jobs;
+  *blocks = (int)(b < 1 ? 1 : b);
   return TKBN_OK;
 }
 
@@ -560,10 +609,10 @@ template <typename R, int D, int JC>
 static int launch_fwd_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* grid, void* kdata,
                         cudaStream_t s) {
   auto k = k_interp_fwd<R, D, JC>;
-  int rc = check_cuda(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ip.smem),
-                      "smem attribute");
+  int blocks;
+  int rc = resident_blocks(k, ip.smem, ip.max_jobs, &blocks);
   if (rc) return rc;
-  k<<<ip.blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords), (const cplx<R>*)grid,
+  k<<<blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords), (const cplx<R>*)grid,
                                          (cplx<R>*)kdata);
   return check_cuda(cudaGetLastError(), "interp_fwd launch");
 }
@@ -572,10 +621,10 @@ template <typename R, int D, int JC>
 static int launch_adj_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* kdata, void* grid,
                         cudaStream_t s) {
   auto k = k_interp_adj<R, D, JC>;
-  int rc = check_cuda(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ip.smem),
-                      "smem attribute");
+  int blocks;
+  int rc = resident_blocks(k, ip.smem, ip.max_jobs, &blocks);
   if (rc) return rc;
-  k<<<ip.blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords), (const cplx<R>*)kdata,
+  k<<<blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords), (const cplx<R>*)kdata,
                                          (cplx<R>*)grid);
   return check_cuda(cudaGetLastError(), "interp_adj launch");
 }
@@ -631,10 +680,10 @@ template <typename R, int D>
 static int launch_grad_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* grid, const void* v,
                          void* grad, cudaStream_t s) {
   auto k = k_interp_grad<R, D>;
-  int rc = check_cuda(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ip.smem),
-                      "smem attribute");
+  int blocks;
+  int rc = resident_blocks(k, ip.smem, ip.max_jobs, &blocks);
   if (rc) return rc;
-  k<<<ip.blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords), (const cplx<R>*)grid,
+  k<<<blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords), (const cplx<R>*)grid,
                                          (const cplx<R>*)v, (R*)grad);
   return check_cuda(cudaGetLastError(), "interp_grad launch");
 }

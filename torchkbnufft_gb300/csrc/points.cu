@@ -74,6 +74,24 @@ __global__ void k_fill_items(const int32_t* __restrict__ counts, const int32_t* 
   }
 }
 
+// Work items are ordered longest first, so that a grid-stride walk over them
+// (CTA k takes items k, k + grid, ...) schedules the heavy k-space-centre tiles
+// in the first wave (longest-processing-time-first).
+__global__ void k_item_keys(const Item* __restrict__ items, const int64_t* __restrict__ hdr, int64_t max_items,
+                            int chunk, uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+  const int64_t nitems = hdr[0];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < max_items; i += (int64_t)gridDim.x * blockDim.x) {
+    keys[i] = i < nitems ? (uint32_t)(chunk - items[i].len) : (uint32_t)(chunk + 1);
+    vals[i] = (int32_t)i;
+  }
+}
+
+__global__ void k_gather_items(const Item* __restrict__ items, const int32_t* __restrict__ order, int64_t max_items,
+                               Item* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < max_items; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = items[order[i]];
+}
+
 template <typename R>
 __global__ void k_sorted_coords(const R* __restrict__ omega, const int32_t* __restrict__ vals, int64_t M,
                                 int ndim, int64_t n, R* __restrict__ coords) {
@@ -115,7 +133,7 @@ void default_tiles(const tkbn_geometry* g, int tile[3], int* chunk) {
   } else {
     tile[0] = tile[1] = tile[2] = 4;
   }
-  *chunk = 256;
+  *chunk = 1024;
 }
 
 static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -152,11 +170,17 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
 
   const int64_t n = L->npts_total > 0 ? L->npts_total : 1;
   const size_t rsize = g->dtype == TKBN_C64 ? 4 : 8;
-  size_t cub_sort = 0, cub_scan = 0;
+  int ibits = 1;
+  while (((int64_t)1 << ibits) <= L->chunk + 1) ++ibits;
+  L->item_key_bits = ibits;
+  size_t cub_sort = 0, cub_scan = 0, cub_isort = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, cub_sort, (uint32_t*)nullptr, (uint32_t*)nullptr, (int32_t*)nullptr,
                                   (int32_t*)nullptr, (int)n, 0, bits);
   cub::DeviceScan::ExclusiveSum(nullptr, cub_scan, (int32_t*)nullptr, (int32_t*)nullptr, (int)L->nkeys);
+  cub::DeviceRadixSort::SortPairs(nullptr, cub_isort, (uint32_t*)nullptr, (uint32_t*)nullptr, (int32_t*)nullptr,
+                                  (int32_t*)nullptr, (int)L->max_items, 0, ibits);
   L->cub_bytes = cub_sort > cub_scan ? cub_sort : cub_scan;
+  if (cub_isort > L->cub_bytes) L->cub_bytes = cub_isort;
 
   size_t o = 0;
   L->off_hdr = o;
@@ -179,6 +203,16 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   o = align_up(o + 4 * (L->nkeys + 1));
   L->off_items = o;
   o = align_up(o + sizeof(tkbn::Item) * L->max_items);
+  L->off_items_raw = o;
+  o = align_up(o + sizeof(tkbn::Item) * L->max_items);
+  L->off_ikeys_in = o;
+  o = align_up(o + 4 * L->max_items);
+  L->off_ikeys = o;
+  o = align_up(o + 4 * L->max_items);
+  L->off_ivals_in = o;
+  o = align_up(o + 4 * L->max_items);
+  L->off_ivals = o;
+  o = align_up(o + 4 * L->max_items);
   L->off_coords = o;
   o = align_up(o + rsize * g->ndim * n);
   L->off_cub = o;
@@ -202,6 +236,11 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
   int32_t* nit = (int32_t*)(ws + L.off_nit);
   int32_t* item_off = (int32_t*)(ws + L.off_item_off);
   Item* items = (Item*)(ws + L.off_items);
+  Item* items_raw = (Item*)(ws + L.off_items_raw);
+  uint32_t* ikeys_in = (uint32_t*)(ws + L.off_ikeys_in);
+  uint32_t* ikeys = (uint32_t*)(ws + L.off_ikeys);
+  int32_t* ivals_in = (int32_t*)(ws + L.off_ivals_in);
+  int32_t* ivals = (int32_t*)(ws + L.off_ivals);
   R* coords = (R*)(ws + L.off_coords);
   int64_t* hdr = (int64_t*)(ws + L.off_hdr);
   void* cubtmp = ws + L.off_cub;
@@ -231,7 +270,14 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
   tb = L.cub_bytes;
   if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, nit, item_off, (int)L.nkeys, s) != cudaSuccess)
     return set_error(TKBN_ERR_CUDA, "scan failed");
-  k_fill_items<<<blocks_for(L.nkeys), threads, 0, s>>>(counts, tile_off, nit, item_off, L.nkeys, L.chunk, items, hdr);
+  k_fill_items<<<blocks_for(L.nkeys), threads, 0, s>>>(counts, tile_off, nit, item_off, L.nkeys, L.chunk, items_raw,
+                                                       hdr);
+  k_item_keys<<<blocks_for(L.max_items), threads, 0, s>>>(items_raw, hdr, L.max_items, L.chunk, ikeys_in, ivals_in);
+  tb = L.cub_bytes;
+  if (cub::DeviceRadixSort::SortPairs(cubtmp, tb, ikeys_in, ikeys, ivals_in, ivals, (int)L.max_items, 0,
+                                      L.item_key_bits, s) != cudaSuccess)
+    return set_error(TKBN_ERR_CUDA, "item sort failed");
+  k_gather_items<<<blocks_for(L.max_items), threads, 0, s>>>(items_raw, ivals, L.max_items, items);
   if (n > 0) k_sorted_coords<R><<<blocks_for(n), threads, 0, s>>>((const R*)omega, vals, p->npts, g->ndim, n, coords);
   return check_cuda(cudaGetLastError(), "points build launch");
 }

@@ -176,11 +176,12 @@ struct PointsLayout {
   int64_t npts_total;  // ntraj * M
   int64_t max_items;   // upper bound on work items
   int key_bits;
+  int item_key_bits;
   int tile[3];
   int ntile[3];
   int chunk;
   size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
-      off_items, off_coords, off_cub;
+      off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_cub;
   size_t cub_bytes;
   size_t total;
 };

@@ -84,11 +84,28 @@ def kb_table_nufft_adjoint(data: Tensor, scaling_coef: Tensor, im_size: Tensor, 
 
 
 def fft_filter(image: Tensor, kernel: Tensor, norm: Optional[str] = "ortho") -> Tensor:
-    """pad -> FFT -> multiply by kernel -> IFFT -> crop (``_nufft/fft.py:121-173``)."""
+    """pad -> FFT -> multiply by kernel -> IFFT -> crop (``_nufft/fft.py:121-173``).
+
+    The kernel multiplies the ``(B, C, *grid)`` spectrum with torch broadcasting,
+    as in the reference: a ``(*grid)`` kernel is shared; a ``(K, *grid)`` kernel
+    needs ``K == C`` (kernel k filters channel k) or ``C == 1`` (the output then
+    has ``K`` channels, one per kernel).
+    """
     R.norm_code(norm)
     nd = image.ndim - 2
-    batched = kernel.ndim > nd
-    return ToepApply.apply(image, kernel, None, norm, batched)
+    if kernel.ndim == nd:
+        return ToepApply.apply(image, kernel, None, norm, "shared")
+    if kernel.ndim != nd + 1:
+        raise NotImplementedError("fft_filter supports kernels of shape (*grid) or (K, *grid)")
+    K, C = kernel.shape[0], image.shape[1]
+    if K == 1:
+        return ToepApply.apply(image, kernel[0], None, norm, "shared")
+    if C == 1:
+        image = image.expand((image.shape[0], K) + tuple(image.shape[2:]))
+    elif C != K:
+        raise RuntimeError(
+            f"The size of tensor a ({C}) must match the size of tensor b ({K}) at non-singleton dimension 1")
+    return ToepApply.apply(image, kernel, None, norm, "channel")
 
 
 def _check_omega(omega: Tensor, batch: int, what: str = "image") -> None:

@@ -221,13 +221,15 @@ class ToepNufft(nn.Module):
             kernel = torch.view_as_complex(kernel.contiguous())
         R.norm_code(norm)
         nd = image.ndim - 2
-        batched = False
         if kernel.ndim > nd:
             if kernel.shape[0] == 1:
                 kernel = kernel[0]
             elif kernel.shape[0] != image.shape[0]:
                 raise ValueError("If using batch dimension, kernel must have same batch size as image")
-            else:
-                batched = True
-        out = ToepApply.apply(image, kernel, smaps, norm, batched)
+        if smaps is None:
+            # the reference applies fft_filter to the whole batch (modules/kbnufft.py:537-538)
+            out = F.fft_filter(image, kernel, norm)
+        else:
+            # one kernel per batch item (toep_batch_loop, modules/kbnufft.py:441-484)
+            out = ToepApply.apply(image, kernel, smaps, norm, "batch" if kernel.ndim > nd else "shared")
         return out if is_complex else torch.view_as_real(out)
