@@ -4,17 +4,19 @@
 // One work item = up to `chunk` points whose footprints start inside one grid
 // tile. A CTA takes a job (item, batch, coil chunk), stages the tile's patch
 // (tile + J-1 halo, wrapped periodically) of Cc coil planes in shared memory,
-// and processes the item's points with Cc lanes per point (lane = coil), so the
-// J^d table coefficients of a point are shared by its coils and the patch
-// reads of one point are spread over distinct banks.
+// and processes the item's points with Cc lanes per point (lane = coil).
+// The J^d table coefficients of a point are computed once per point: its Cc
+// lanes each evaluate some of the D*J per-dimension table factors and share
+// them through a per-warp shared-memory scratch. The normalised frequency tm
+// and the fftshift phase of every point come precomputed from the layout.
 //
 // Reference semantics (mmuckley/torchkbnufft):
 //   forward  y[b,c,m] = phase_m * sum_j coef_j(m) * X[b,c,idx_j(m)]
 //            (table_interp_one_batch, torchkbnufft/_nufft/interp.py:153-203)
 //   adjoint  X[b,c,idx_j(m)] += conj(coef_j(m)) * conj(phase_m) * y[b,c,m]
 //            (table_interp_adjoint, torchkbnufft/_nufft/interp.py:587-726)
-// The separable sums below group the products per dimension; the table bins,
-// cell indices and phase argument are computed exactly as the reference does.
+// The separable sums group the products per dimension; the table bins, cell
+// indices and phase argument are computed exactly as the reference does.
 
 #include "geo_host.cuh"
 #include "tkbn_common.cuh"
@@ -22,69 +24,117 @@
 namespace tkbn {
 
 constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
 
-template <int D, int JC>
-struct JDims {
+template <int JC>
+struct NJOf {
   static constexpr int N = JC > 0 ? JC : kMaxJ;
 };
 
-// Per-point setup shared by all kernels: table factors per dim and the
-// point's local footprint origin inside the tile patch.
-template <typename R, int D, int JC>
-struct PointSetup {
-  cplx<R> h[D][JDims<D, JC>::N];
-  int local[D];
-  R om[D];
-  bool ok;
+struct Launch {
+  const Item* items;
+  const int64_t* hdr;   // hdr[0] = number of items
+  const int32_t* vals;  // sorted -> original flat index t*M + m
+  int64_t n;            // ntraj * M
+  int64_t M;
+  int64_t ntraj;
+  int64_t B, C;
+  int Cc;               // coils per job (power of two <= 32)
+  int ncc;              // coil chunks
+  int64_t nbpt;         // batch items per trajectory job (B if shared trajectory else 1)
+  int cells;            // prod P
+  int ps;               // smem plane stride (elements)
+  int64_t gtot;         // prod K
+  int scratch;          // per-warp factor scratch (complex elements)
 };
-
-template <typename R, int D, int JC>
-__device__ __forceinline__ void setup_point(const Geo<R>& geo, const R* __restrict__ coords, int64_t n, int64_t i,
-                                            const int* origin, PointSetup<R, D, JC>& ps) {
-  ps.ok = true;
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const R om = coords[d * n + i];
-    ps.om[d] = om;
-    R tm;
-    int base;
-    ps.ok &= base_index<R>(om, geo.gam[d], geo.halfJ[d], &tm, &base);
-    const int w = pmod(base, geo.K[d]);
-    const int l = w - origin[d];
-    ps.ok &= (l >= 0) & (l < geo.T[d]);
-    ps.local[d] = l;
-    const int J = JC > 0 ? JC : geo.J[d];
-#pragma unroll
-    for (int j = 0; j < JDims<D, JC>::N; ++j) {
-      if (j < J) {
-        const int k = table_bin<R>(tm, base + j, geo.Lr[d], geo.center[d], geo.tmax[d]);
-        ps.h[d][j] = __ldg(&geo.tab[d][k]);
-      } else {
-        ps.h[d][j] = mk<R>(0, 0);
-      }
-    }
-  }
-}
 
 template <typename R>
 __device__ __forceinline__ void job_decode(const Geo<R>& geo, const Item& it, int64_t ntraj, int64_t bb, int* origin,
                                            int64_t* t_out, int64_t* b_out) {
   const int64_t t = it.key / geo.ntiles;
   int rem = (int)(it.key - t * geo.ntiles);
-  for (int d = geo.ndim - 1; d >= 0; --d) {
-    const int td = rem % geo.ntile[d];
-    rem /= geo.ntile[d];
-    origin[d] = td * geo.T[d];
+#pragma unroll
+  for (int d = kMaxDim - 1; d >= 0; --d) {
+    if (d < geo.ndim) {
+      const int td = rem % geo.ntile[d];
+      rem /= geo.ntile[d];
+      origin[d] = td * geo.T[d];
+    } else {
+      origin[d] = 0;
+    }
   }
   *t_out = t;
   *b_out = ntraj == 1 ? bb : t;
 }
 
+// Per-point data every lane needs: tm, the first footprint cell and its
+// offset inside the tile patch. False for a non-finite point or a point whose
+// footprint does not start inside this tile.
+template <typename R, int D>
+__device__ __forceinline__ bool point_base(const Geo<R>& geo, const R* __restrict__ tm, int64_t n, int64_t i,
+                                           const int* origin, R* tmv, int* base, int* local) {
+  bool ok = true;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const R t = tm[d * n + i];
+    tmv[d] = t;
+    const R f = floor(sub_rn(t, geo.halfJ[d]));
+    const bool fin = fabs(f) < R(1 << 30);
+    base[d] = fin ? 1 + (int)f : 0;
+    const int l = pmod(base[d], geo.K[d]) - origin[d];
+    local[d] = l;
+    ok = ok && fin && (l >= 0) && (l < geo.T[d]);
+  }
+  return ok;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ T sel(const T* v, int d) {
+  return (D > 2 && d == 2) ? v[2 % D] : ((D > 1 && d == 1) ? v[1 % D] : v[0]);
+}
+
+// Table factors h[d][j] = table_d[bin(tm_d, base_d + j)]. With coop, the
+// `lanes` lanes of a point split the D*NJ evaluations and exchange them via
+// `scr` (per-point scratch); every lane of the warp must call this.
+template <typename R, int D, int JC>
+__device__ __forceinline__ void table_factors(const Geo<R>& geo, const R* tmv, const int* base, int lane_in_pt,
+                                              int lanes, bool coop, cplx<R>* scr, cplx<R> (&h)[D][NJOf<JC>::N]) {
+  constexpr int NJ = NJOf<JC>::N;
+  if (coop) {
+    for (int f = lane_in_pt; f < D * NJ; f += lanes) {
+      const int d = f / NJ, j = f - (f / NJ) * NJ;
+      const int J = JC > 0 ? JC : sel<int, 3>(geo.J, d);
+      cplx<R> v = mk<R>(0, 0);
+      if (j < J) {
+        const int k = table_bin<R>(sel<R, D>(tmv, d), sel<int, D>(base, d) + j, sel<R, 3>(geo.Lr, d),
+                                   sel<int, 3>(geo.center, d), sel<int, 3>(geo.tmax, d));
+        v = __ldg(&sel<const cplx<R>*, 3>(geo.tab, d)[k]);
+      }
+      scr[f] = v;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) h[d][j] = scr[d * NJ + j];
+    __syncwarp();
+  } else {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const int J = JC > 0 ? JC : geo.J[d];
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        h[d][j] = mk<R>(0, 0);
+        if (j < J) h[d][j] = __ldg(&geo.tab[d][table_bin<R>(tmv[d], base[d] + j, geo.Lr[d], geo.center[d], geo.tmax[d])]);
+      }
+    }
+  }
+}
+
 // Row decomposition of a patch: a row is P[D-1] cells contiguous in smem and
 // (up to the periodic wrap) contiguous in the global grid.
 template <typename R, int D>
-__device__ __forceinline__ int64_t patch_row_base(const Geo<R>& geo, int row, const int* origin, int64_t* gstride_x) {
-  // row -> (c is handled by the caller), outer coordinates
+__device__ __forceinline__ int64_t patch_row_base(const Geo<R>& geo, int row, const int* origin) {
   int64_t flat = 0, stride = geo.K[D - 1];
 #pragma unroll
   for (int d = D - 2; d >= 0; --d) {
@@ -93,7 +143,6 @@ __device__ __forceinline__ int64_t patch_row_base(const Geo<R>& geo, int row, co
     flat += (int64_t)pmod(origin[d] + p, geo.K[d]) * stride;
     stride *= geo.K[d];
   }
-  *gstride_x = 1;
   return flat;
 }
 
@@ -106,12 +155,11 @@ __device__ __forceinline__ void load_patch(const Geo<R>& geo, const cplx<R>* __r
   const int PX = geo.P[D - 1];
   const int KX = geo.K[D - 1];
   const int rows_per_plane = cells / PX;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (int r = warp; r < ncl * rows_per_plane; r += nwarps) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = warp; r < ncl * rows_per_plane; r += kWarps) {
     const int c = r / rows_per_plane;
     const int rr = r - c * rows_per_plane;
-    int64_t sx;
-    const cplx<R>* src = grid + (plane0 + c) * gtot + patch_row_base<R, D>(geo, rr, origin, &sx);
+    const cplx<R>* src = grid + (plane0 + c) * gtot + patch_row_base<R, D>(geo, rr, origin);
     cplx<R>* dst = patch + c * ps + rr * PX;
     for (int px = lane; px < PX; px += 32) {
       int gx = origin[D - 1] + px;
@@ -121,33 +169,26 @@ __device__ __forceinline__ void load_patch(const Geo<R>& geo, const cplx<R>* __r
   }
 }
 
-// Add the staged patch into the global grid with vector atomics (cells that
-// stayed zero are skipped).
-template <typename R, int D>
-__device__ __forceinline__ void flush_patch(const Geo<R>& geo, cplx<R>* __restrict__ grid, int64_t plane0,
-                                            int64_t gtot, int ncl, int cells, int ps, const int* origin,
-                                            const cplx<R>* patch);
-
 template <typename R, int D, int JC>
-__device__ __forceinline__ cplx<R> gather_point(const Geo<R>& geo, const PointSetup<R, D, JC>& ps,
-                                                const cplx<R>* __restrict__ plane) {
-  constexpr int NJ = JDims<D, JC>::N;
+__device__ __forceinline__ cplx<R> gather_point(const Geo<R>& geo, const cplx<R> (&h)[D][NJOf<JC>::N],
+                                                const int* local, const cplx<R>* __restrict__ plane) {
+  constexpr int NJ = NJOf<JC>::N;
   cplx<R> acc = mk<R>(0, 0);
   if (D == 1) {
 #pragma unroll
     for (int j = 0; j < NJ; ++j)
-      if (JC > 0 || j < geo.J[0]) acc = cfma<R>(ps.h[0][j], plane[ps.local[0] + j], acc);
+      if (JC > 0 || j < geo.J[0]) acc = cfma<R>(h[0][j], plane[local[0] + j], acc);
   } else if (D == 2) {
     const int P1 = geo.P[1];
 #pragma unroll
     for (int jy = 0; jy < NJ; ++jy) {
       if (JC > 0 || jy < geo.J[0]) {
-        const cplx<R>* row = plane + (ps.local[0] + jy) * P1 + ps.local[1 % D];
+        const cplx<R>* row = plane + (local[0] + jy) * P1 + local[1 % D];
         cplx<R> r = mk<R>(0, 0);
 #pragma unroll
         for (int jx = 0; jx < NJ; ++jx)
-          if (JC > 0 || jx < geo.J[1 % D]) r = cfma<R>(ps.h[1 % D][jx], row[jx], r);
-        acc = cfma<R>(ps.h[0][jy], r, acc);
+          if (JC > 0 || jx < geo.J[1 % D]) r = cfma<R>(h[1 % D][jx], row[jx], r);
+        acc = cfma<R>(h[0][jy], r, acc);
       }
     }
   } else {
@@ -159,29 +200,21 @@ __device__ __forceinline__ cplx<R> gather_point(const Geo<R>& geo, const PointSe
 #pragma unroll
         for (int jy = 0; jy < NJ; ++jy) {
           if (JC > 0 || jy < geo.J[1 % D]) {
-            const cplx<R>* row = plane + ((ps.local[0] + jz) * P1 + ps.local[1 % D] + jy) * P2 + ps.local[2 % D];
+            const cplx<R>* row = plane + ((local[0] + jz) * P1 + local[1 % D] + jy) * P2 + local[2 % D];
             cplx<R> r = mk<R>(0, 0);
 #pragma unroll
             for (int jx = 0; jx < NJ; ++jx)
-              if (JC > 0 || jx < geo.J[2 % D]) r = cfma<R>(ps.h[2 % D][jx], row[jx], r);
-            sz = cfma<R>(ps.h[1 % D][jy], r, sz);
+              if (JC > 0 || jx < geo.J[2 % D]) r = cfma<R>(h[2 % D][jx], row[jx], r);
+            sz = cfma<R>(h[1 % D][jy], r, sz);
           }
         }
-        acc = cfma<R>(ps.h[0][jz], sz, acc);
+        acc = cfma<R>(h[0][jz], sz, acc);
       }
     }
   }
   return acc;
 }
 
-__device__ __forceinline__ void atomic_add_c(float2* p, float2 v) {
-  atomicAdd(&p->x, v.x);
-  atomicAdd(&p->y, v.y);
-}
-__device__ __forceinline__ void atomic_add_c(double2* p, double2 v) {
-  atomicAdd(&p->x, v.x);
-  atomicAdd(&p->y, v.y);
-}
 // Global-memory flush: one vector atomic for float2 (sm_90+), two for double.
 __device__ __forceinline__ void atomic_add_global(float2* p, float2 v) { atomicAdd(p, v); }
 __device__ __forceinline__ void atomic_add_global(double2* p, double2 v) {
@@ -189,22 +222,81 @@ __device__ __forceinline__ void atomic_add_global(double2* p, double2 v) {
   atomicAdd(&p->y, v.y);
 }
 
+// Adjoint accumulation planes: real and imaginary parts in separate planes
+// (re plane c at c*ps, im plane c at (Cc + c)*ps), so that the Cc lanes of a
+// point hit Cc distinct banks with an odd plane stride.
+template <typename R, int D, int JC>
+__device__ __forceinline__ void scatter_point(const Geo<R>& geo, const cplx<R> (&h)[D][NJOf<JC>::N],
+                                              const int* local, cplx<R> v, R* pre, R* pim) {
+  constexpr int NJ = NJOf<JC>::N;
+  if (D == 1) {
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      if (JC > 0 || j < geo.J[0]) {
+        const cplx<R> w = cmulc<R>(v, h[0][j]);
+        atomicAdd(&pre[local[0] + j], w.x);
+        atomicAdd(&pim[local[0] + j], w.y);
+      }
+    }
+  } else if (D == 2) {
+    const int P1 = geo.P[1];
+#pragma unroll
+    for (int jy = 0; jy < NJ; ++jy) {
+      if (JC > 0 || jy < geo.J[0]) {
+        const cplx<R> vy = cmulc<R>(v, h[0][jy]);
+        const int row = (local[0] + jy) * P1 + local[1 % D];
+#pragma unroll
+        for (int jx = 0; jx < NJ; ++jx) {
+          if (JC > 0 || jx < geo.J[1 % D]) {
+            const cplx<R> w = cmulc<R>(vy, h[1 % D][jx]);
+            atomicAdd(&pre[row + jx], w.x);
+            atomicAdd(&pim[row + jx], w.y);
+          }
+        }
+      }
+    }
+  } else {
+    const int P1 = geo.P[1 % D], P2 = geo.P[2 % D];
+#pragma unroll 1
+    for (int jz = 0; jz < NJ; ++jz) {
+      if (JC > 0 || jz < geo.J[0]) {
+        const cplx<R> vz = cmulc<R>(v, h[0][jz]);
+#pragma unroll
+        for (int jy = 0; jy < NJ; ++jy) {
+          if (JC > 0 || jy < geo.J[1 % D]) {
+            const cplx<R> vy = cmulc<R>(vz, h[1 % D][jy]);
+            const int row = ((local[0] + jz) * P1 + local[1 % D] + jy) * P2 + local[2 % D];
+#pragma unroll
+            for (int jx = 0; jx < NJ; ++jx) {
+              if (JC > 0 || jx < geo.J[2 % D]) {
+                const cplx<R> w = cmulc<R>(vy, h[2 % D][jx]);
+                atomicAdd(&pre[row + jx], w.x);
+                atomicAdd(&pim[row + jx], w.y);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
 template <typename R, int D>
 __device__ __forceinline__ void flush_patch(const Geo<R>& geo, cplx<R>* __restrict__ grid, int64_t plane0,
-                                            int64_t gtot, int ncl, int cells, int ps, const int* origin,
-                                            const cplx<R>* patch) {
+                                            int64_t gtot, int ncl, int cells, int ps, int Cc, const int* origin,
+                                            const R* pre, const R* pim) {
   const int PX = geo.P[D - 1];
   const int KX = geo.K[D - 1];
   const int rows_per_plane = cells / PX;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (int r = warp; r < ncl * rows_per_plane; r += nwarps) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = warp; r < ncl * rows_per_plane; r += kWarps) {
     const int c = r / rows_per_plane;
     const int rr = r - c * rows_per_plane;
-    int64_t sx;
-    cplx<R>* dst = grid + (plane0 + c) * gtot + patch_row_base<R, D>(geo, rr, origin, &sx);
-    const cplx<R>* src = patch + c * ps + rr * PX;
+    cplx<R>* dst = grid + (plane0 + c) * gtot + patch_row_base<R, D>(geo, rr, origin);
+    const int o = c * ps + rr * PX;
+    const int oi = (Cc + c) * ps + rr * PX;
     for (int px = lane; px < PX; px += 32) {
-      const cplx<R> v = src[px];
+      const cplx<R> v = mk<R>(pre[o + px], pim[oi + px]);
       if (v.x == R(0) && v.y == R(0)) continue;
       int gx = origin[D - 1] + px;
       gx = gx >= KX ? gx - KX * (gx / KX) : gx;
@@ -213,150 +305,121 @@ __device__ __forceinline__ void flush_patch(const Geo<R>& geo, cplx<R>* __restri
   }
 }
 
-template <typename R, int D, int JC>
-__device__ __forceinline__ void scatter_point(const Geo<R>& geo, const PointSetup<R, D, JC>& ps, cplx<R> v,
-                                              cplx<R>* plane) {
-  constexpr int NJ = JDims<D, JC>::N;
-  if (D == 1) {
-#pragma unroll
-    for (int j = 0; j < NJ; ++j)
-      if (JC > 0 || j < geo.J[0]) atomic_add_c(&plane[ps.local[0] + j], cmulc<R>(v, ps.h[0][j]));
-  } else if (D == 2) {
-    const int P1 = geo.P[1];
-#pragma unroll
-    for (int jy = 0; jy < NJ; ++jy) {
-      if (JC > 0 || jy < geo.J[0]) {
-        const cplx<R> vy = cmulc<R>(v, ps.h[0][jy]);
-        cplx<R>* row = plane + (ps.local[0] + jy) * P1 + ps.local[1 % D];
-#pragma unroll
-        for (int jx = 0; jx < NJ; ++jx)
-          if (JC > 0 || jx < geo.J[1 % D]) atomic_add_c(&row[jx], cmulc<R>(vy, ps.h[1 % D][jx]));
-      }
-    }
-  } else {
-    const int P1 = geo.P[1 % D], P2 = geo.P[2 % D];
-#pragma unroll 1
-    for (int jz = 0; jz < NJ; ++jz) {
-      if (JC > 0 || jz < geo.J[0]) {
-        const cplx<R> vz = cmulc<R>(v, ps.h[0][jz]);
-#pragma unroll
-        for (int jy = 0; jy < NJ; ++jy) {
-          if (JC > 0 || jy < geo.J[1 % D]) {
-            const cplx<R> vy = cmulc<R>(vz, ps.h[1 % D][jy]);
-            cplx<R>* row = plane + ((ps.local[0] + jz) * P1 + ps.local[1 % D] + jy) * P2 + ps.local[2 % D];
-#pragma unroll
-            for (int jx = 0; jx < NJ; ++jx)
-              if (JC > 0 || jx < geo.J[2 % D]) atomic_add_c(&row[jx], cmulc<R>(vy, ps.h[2 % D][jx]));
-          }
-        }
-      }
-    }
-  }
-}
+// Common job loop skeleton pieces ------------------------------------------
 
-struct Launch {
-  const Item* items;
-  const int64_t* hdr;  // hdr[0] = number of items
-  const int32_t* vals; // sorted -> original flat index t*M + m
-  int64_t n;           // ntraj * M
-  int64_t M;
-  int64_t ntraj;
-  int64_t B, C;
-  int Cc;              // coils per job (power of two <= 32)
-  int ncc;             // coil chunks
-  int64_t nbpt;        // batch items per trajectory job (B if shared trajectory else 1)
-  int cells;           // prod P
-  int ps;              // smem plane stride (elements)
-  int64_t gtot;        // prod K
+struct JobCtx {
+  int64_t t, b;
+  int c0, ncl;
+  int origin[kMaxDim];
 };
 
+template <typename R>
+__device__ __forceinline__ bool next_job(const Geo<R>& geo, const Launch& a, int64_t job, int64_t nitems, Item* it,
+                                         JobCtx* j) {
+  const int64_t item_idx = job % nitems;
+  const int64_t rest = job / nitems;
+  const int cc = (int)(rest % a.ncc);
+  const int64_t bb = rest / a.ncc;
+  *it = a.items[item_idx];
+  job_decode<R>(geo, *it, a.ntraj, bb, j->origin, &j->t, &j->b);
+  j->c0 = cc * a.Cc;
+  j->ncl = (int)min((int64_t)a.Cc, a.C - j->c0);
+  return true;
+}
+
 template <typename R, int D, int JC>
-__global__ void __launch_bounds__(kThreads) k_interp_fwd(Geo<R> geo, Launch a, const R* __restrict__ coords,
+__global__ void __launch_bounds__(kThreads) k_interp_fwd(Geo<R> geo, Launch a, const R* __restrict__ tm,
+                                                         const cplx<R>* __restrict__ ph,
                                                          const cplx<R>* __restrict__ grid, cplx<R>* __restrict__ kdata) {
+  constexpr int NJ = NJOf<JC>::N;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* patch = reinterpret_cast<cplx<R>*>(smem_raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  cplx<R>* scr_warp = patch + a.Cc * a.ps + warp * a.scratch;
   const int64_t nitems = a.hdr[0];
   const int64_t njobs = nitems * a.nbpt * a.ncc;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int ppw = 32 / a.Cc;
-  const int ppb = ppw * (blockDim.x >> 5);
+  const int ppb = ppw * kWarps;
   const int c = lane % a.Cc;
+  const int pslot = lane / a.Cc;
+  const bool coop = a.Cc >= 4;
+  cplx<R>* scr = scr_warp + pslot * (D * NJ);
   for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x) {
-    const int64_t item_idx = job % nitems;
-    const int64_t rest = job / nitems;
-    const int cc = (int)(rest % a.ncc);
-    const int64_t bb = rest / a.ncc;
-    const Item it = a.items[item_idx];
-    int origin[kMaxDim];
-    int64_t t, b;
-    job_decode<R>(geo, it, a.ntraj, bb, origin, &t, &b);
-    const int c0 = cc * a.Cc;
-    const int ncl = (int)min((int64_t)a.Cc, a.C - c0);
+    Item it;
+    JobCtx jc;
+    next_job<R>(geo, a, job, nitems, &it, &jc);
     __syncthreads();
-    load_patch<R, D>(geo, grid, b * a.C + c0, a.gtot, ncl, a.cells, a.ps, origin, patch);
+    load_patch<R, D>(geo, grid, jc.b * a.C + jc.c0, a.gtot, jc.ncl, a.cells, a.ps, jc.origin, patch);
     __syncthreads();
-    for (int s = warp * ppw + lane / a.Cc; s < it.len; s += ppb) {
-      const int64_t i = it.start + s;
-      PointSetup<R, D, JC> ps;
-      setup_point<R, D, JC>(geo, coords, a.n, i, origin, ps);
-      const int64_t m = a.vals[i] - t * a.M;
-      if (c < ncl) {
+    const int nrounds = (it.len + ppb - 1) / ppb;
+    for (int r = 0; r < nrounds; ++r) {
+      const int s = r * ppb + warp * ppw + pslot;
+      const bool active = s < it.len;
+      const int64_t i = it.start + (active ? s : 0);
+      R tmv[D];
+      int base[D], local[D];
+      const bool ok = point_base<R, D>(geo, tm, a.n, i, jc.origin, tmv, base, local);
+      cplx<R> h[D][NJ];
+      table_factors<R, D, JC>(geo, tmv, base, c, a.Cc, coop, scr, h);
+      if (active && c < jc.ncl) {
+        const int64_t m = a.vals[i] - jc.t * a.M;
         cplx<R> y;
-        if (ps.ok) {
-          const cplx<R> acc = gather_point<R, D, JC>(geo, ps, patch + c * a.ps);
-          R sn, cs;
-          sincos_acc(phase_arg<R, D>(ps.om, geo.nshift), &sn, &cs);
-          y = cmul<R>(acc, mk<R>(cs, sn));
+        if (ok) {
+          y = cmul<R>(gather_point<R, D, JC>(geo, h, local, patch + c * a.ps), ph[i]);
         } else {
           y = mk<R>(R(NAN), R(NAN));
         }
-        kdata[(b * a.C + c0 + c) * a.M + m] = y;
+        kdata[(jc.b * a.C + jc.c0 + c) * a.M + m] = y;
       }
-      if (!ps.ok && c == 0) atomicOr(&g_status, kStatusNonFinite | kStatusOutsidePatch);
+      if (active && !ok && c == 0) atomicOr(&g_status, kStatusNonFinite | kStatusOutsidePatch);
     }
   }
 }
 
 template <typename R, int D, int JC>
-__global__ void __launch_bounds__(kThreads) k_interp_adj(Geo<R> geo, Launch a, const R* __restrict__ coords,
+__global__ void __launch_bounds__(kThreads) k_interp_adj(Geo<R> geo, Launch a, const R* __restrict__ tm,
+                                                         const cplx<R>* __restrict__ ph,
                                                          const cplx<R>* __restrict__ kdata, cplx<R>* __restrict__ grid) {
+  constexpr int NJ = NJOf<JC>::N;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cplx<R>* patch = reinterpret_cast<cplx<R>*>(smem_raw);
+  R* pre = reinterpret_cast<R*>(smem_raw);
+  R* pim = pre + a.Cc * a.ps;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  cplx<R>* scr_warp = reinterpret_cast<cplx<R>*>(pre + 2 * a.Cc * a.ps) + warp * a.scratch;
   const int64_t nitems = a.hdr[0];
   const int64_t njobs = nitems * a.nbpt * a.ncc;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int ppw = 32 / a.Cc;
-  const int ppb = ppw * (blockDim.x >> 5);
+  const int ppb = ppw * kWarps;
   const int c = lane % a.Cc;
+  const int pslot = lane / a.Cc;
+  const bool coop = a.Cc >= 4;
+  cplx<R>* scr = scr_warp + pslot * (D * NJ);
   for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x) {
-    const int64_t item_idx = job % nitems;
-    const int64_t rest = job / nitems;
-    const int cc = (int)(rest % a.ncc);
-    const int64_t bb = rest / a.ncc;
-    const Item it = a.items[item_idx];
-    int origin[kMaxDim];
-    int64_t t, b;
-    job_decode<R>(geo, it, a.ntraj, bb, origin, &t, &b);
-    const int c0 = cc * a.Cc;
-    const int ncl = (int)min((int64_t)a.Cc, a.C - c0);
+    Item it;
+    JobCtx jc;
+    next_job<R>(geo, a, job, nitems, &it, &jc);
     __syncthreads();
-    for (int idx = threadIdx.x; idx < ncl * a.ps; idx += blockDim.x) patch[idx] = mk<R>(0, 0);
+    for (int idx = threadIdx.x; idx < 2 * a.Cc * a.ps; idx += kThreads) pre[idx] = R(0);
     __syncthreads();
-    for (int s = warp * ppw + lane / a.Cc; s < it.len; s += ppb) {
-      const int64_t i = it.start + s;
-      PointSetup<R, D, JC> ps;
-      setup_point<R, D, JC>(geo, coords, a.n, i, origin, ps);
-      const int64_t m = a.vals[i] - t * a.M;
-      if (ps.ok && c < ncl) {
-        R sn, cs;
-        sincos_acc(phase_arg<R, D>(ps.om, geo.nshift), &sn, &cs);
-        const cplx<R> v = cmulc<R>(kdata[(b * a.C + c0 + c) * a.M + m], mk<R>(cs, sn));
-        scatter_point<R, D, JC>(geo, ps, v, patch + c * a.ps);
+    const int nrounds = (it.len + ppb - 1) / ppb;
+    for (int r = 0; r < nrounds; ++r) {
+      const int s = r * ppb + warp * ppw + pslot;
+      const bool active = s < it.len;
+      const int64_t i = it.start + (active ? s : 0);
+      R tmv[D];
+      int base[D], local[D];
+      const bool ok = point_base<R, D>(geo, tm, a.n, i, jc.origin, tmv, base, local);
+      cplx<R> h[D][NJ];
+      table_factors<R, D, JC>(geo, tmv, base, c, a.Cc, coop, scr, h);
+      if (active && ok && c < jc.ncl) {
+        const int64_t m = a.vals[i] - jc.t * a.M;
+        const cplx<R> v = cmulc<R>(kdata[(jc.b * a.C + jc.c0 + c) * a.M + m], ph[i]);
+        scatter_point<R, D, JC>(geo, h, local, v, pre + c * a.ps, pim + c * a.ps);
       }
-      if (!ps.ok && c == 0) atomicOr(&g_status, kStatusNonFinite | kStatusOutsidePatch);
+      if (active && !ok && c == 0) atomicOr(&g_status, kStatusNonFinite | kStatusOutsidePatch);
     }
     __syncthreads();
-    flush_patch<R, D>(geo, grid, b * a.C + c0, a.gtot, ncl, a.cells, a.ps, origin, patch);
+    flush_patch<R, D>(geo, grid, jc.b * a.C + jc.c0, a.gtot, jc.ncl, a.cells, a.ps, a.Cc, jc.origin, pre, pim);
   }
 }
 
@@ -383,11 +446,13 @@ __device__ __forceinline__ void lerp_tables(const Geo<R>& geo, int d, R tm, int 
 }
 
 // K7: grad_omega[t,d,m] += Re sum_{b,c} conj(v[b,c,m]) * dy/d omega_d, with
-// y = phase * sum_j prod_d h_d(u_d) X[idx_j], u_d = tm_d - g_d, tm = omega/gam.
+// y = phase * sum_j prod_d h_d(u_d) X[idx_j], u_d = tm_d - g_d, tm = omega/gam,
+// d tm_d / d omega_d = 1 / gam_d and d phase / d omega_d = i n_shift_d phase.
 // Uses the patch staging of the forward; one lane per (point, coil), coils
 // reduced with warp shuffles, batches with atomics.
 template <typename R, int D>
-__global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, const R* __restrict__ coords,
+__global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, const R* __restrict__ tm,
+                                                          const cplx<R>* __restrict__ ph,
                                                           const cplx<R>* __restrict__ grid,
                                                           const cplx<R>* __restrict__ v, R* __restrict__ grad) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -396,41 +461,30 @@ __global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, 
   const int64_t njobs = nitems * a.nbpt * a.ncc;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int ppw = 32 / a.Cc;
-  const int ppb = ppw * (blockDim.x >> 5);
+  const int ppb = ppw * kWarps;
   const int c = lane % a.Cc;
   for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x) {
-    const int64_t item_idx = job % nitems;
-    const int64_t rest = job / nitems;
-    const int cc = (int)(rest % a.ncc);
-    const int64_t bb = rest / a.ncc;
-    const Item it = a.items[item_idx];
-    int origin[kMaxDim];
-    int64_t t, b;
-    job_decode<R>(geo, it, a.ntraj, bb, origin, &t, &b);
-    const int c0 = cc * a.Cc;
-    const int ncl = (int)min((int64_t)a.Cc, a.C - c0);
+    Item it;
+    JobCtx jc;
+    next_job<R>(geo, a, job, nitems, &it, &jc);
     __syncthreads();
-    load_patch<R, D>(geo, grid, b * a.C + c0, a.gtot, ncl, a.cells, a.ps, origin, patch);
+    load_patch<R, D>(geo, grid, jc.b * a.C + jc.c0, a.gtot, jc.ncl, a.cells, a.ps, jc.origin, patch);
     __syncthreads();
     const int nrounds = (it.len + ppb - 1) / ppb;
     for (int r = 0; r < nrounds; ++r) {
       const int s = r * ppb + warp * ppw + lane / a.Cc;
       const bool active = s < it.len;
       const int64_t i = it.start + (active ? s : 0);
-      R om[D], tm[D];
+      R tmv[D];
       int base[D], local[D];
-      bool ok = active;
+      const bool ok = point_base<R, D>(geo, tm, a.n, i, jc.origin, tmv, base, local) && active;
       cplx<R> hv[D][kMaxJ], hd[D][kMaxJ];
 #pragma unroll
       for (int d = 0; d < D; ++d) {
-        om[d] = coords[d * a.n + i];
-        ok &= base_index<R>(om[d], geo.gam[d], geo.halfJ[d], &tm[d], &base[d]);
-        local[d] = pmod(base[d], geo.K[d]) - origin[d];
-        ok &= (local[d] >= 0) & (local[d] < geo.T[d]);
 #pragma unroll
         for (int j = 0; j < kMaxJ; ++j) {
           if (j < geo.J[d]) {
-            lerp_tables<R>(geo, d, tm[d], base[d] + j, &hv[d][j], &hd[d][j]);
+            lerp_tables<R>(geo, d, tmv[d], base[d] + j, &hv[d][j], &hd[d][j]);
           } else {
             hv[d][j] = mk<R>(0, 0);
             hd[d][j] = mk<R>(0, 0);
@@ -441,71 +495,88 @@ __global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, 
 #pragma unroll
       for (int d = 0; d < D; ++d) gsum[d] = R(0);
       int64_t m = 0;
-      if (ok) m = a.vals[i] - t * a.M;
-      if (ok && c < ncl) {
+      if (ok) m = a.vals[i] - jc.t * a.M;
+      if (ok && c < jc.ncl) {
         const cplx<R>* plane = patch + c * a.ps;
-        // value and per-dim derivative sums
         cplx<R> val = mk<R>(0, 0);
         cplx<R> der[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) der[d] = mk<R>(0, 0);
         if (D == 1) {
-          for (int j = 0; j < geo.J[0]; ++j) {
-            const cplx<R> x = plane[local[0] + j];
-            val = cfma<R>(hv[0][j], x, val);
-            der[0] = cfma<R>(hd[0][j], x, der[0]);
+#pragma unroll
+          for (int j = 0; j < kMaxJ; ++j) {
+            if (j < geo.J[0]) {
+              const cplx<R> x = plane[local[0] + j];
+              val = cfma<R>(hv[0][j], x, val);
+              der[0] = cfma<R>(hd[0][j], x, der[0]);
+            }
           }
         } else if (D == 2) {
-          for (int jy = 0; jy < geo.J[0]; ++jy) {
-            cplx<R> rv = mk<R>(0, 0), rd = mk<R>(0, 0);
-            const cplx<R>* row = plane + (local[0] + jy) * geo.P[1 % D] + local[1 % D];
 #pragma unroll
-            for (int jx = 0; jx < kMaxJ; ++jx) {
-              if (jx < geo.J[1 % D]) {
-                const cplx<R> x = row[jx];
-                rv = cfma<R>(hv[1 % D][jx], x, rv);
-                rd = cfma<R>(hd[1 % D][jx], x, rd);
-              }
-            }
-            val = cfma<R>(hv[0][jy], rv, val);
-            der[0] = cfma<R>(hd[0][jy], rv, der[0]);
-            der[1 % D] = cfma<R>(hv[0][jy], rd, der[1 % D]);
-          }
-        } else {
-          for (int jz = 0; jz < geo.J[0]; ++jz) {
-            cplx<R> zv = mk<R>(0, 0), zdy = mk<R>(0, 0), zdx = mk<R>(0, 0);
-            for (int jy = 0; jy < geo.J[1 % D]; ++jy) {
+          for (int jy = 0; jy < kMaxJ; ++jy) {
+            if (jy < geo.J[0]) {
               cplx<R> rv = mk<R>(0, 0), rd = mk<R>(0, 0);
-              const cplx<R>* row =
-                  plane + ((local[0] + jz) * geo.P[1 % D] + local[1 % D] + jy) * geo.P[2 % D] + local[2 % D];
+              const cplx<R>* row = plane + (local[0] + jy) * geo.P[1 % D] + local[1 % D];
 #pragma unroll
               for (int jx = 0; jx < kMaxJ; ++jx) {
-                if (jx < geo.J[2 % D]) {
+                if (jx < geo.J[1 % D]) {
                   const cplx<R> x = row[jx];
-                  rv = cfma<R>(hv[2 % D][jx], x, rv);
-                  rd = cfma<R>(hd[2 % D][jx], x, rd);
+                  rv = cfma<R>(hv[1 % D][jx], x, rv);
+                  rd = cfma<R>(hd[1 % D][jx], x, rd);
                 }
               }
-              zv = cfma<R>(hv[1 % D][jy], rv, zv);
-              zdy = cfma<R>(hd[1 % D][jy], rv, zdy);
-              zdx = cfma<R>(hv[1 % D][jy], rd, zdx);
+              val = cfma<R>(hv[0][jy], rv, val);
+              der[0] = cfma<R>(hd[0][jy], rv, der[0]);
+              der[1 % D] = cfma<R>(hv[0][jy], rd, der[1 % D]);
             }
-            val = cfma<R>(hv[0][jz], zv, val);
-            der[0] = cfma<R>(hd[0][jz], zv, der[0]);
-            der[1 % D] = cfma<R>(hv[0][jz], zdy, der[1 % D]);
-            der[2 % D] = cfma<R>(hv[0][jz], zdx, der[2 % D]);
+          }
+        } else {
+#pragma unroll 1
+          for (int jz = 0; jz < kMaxJ; ++jz) {
+            if (jz < geo.J[0]) {
+              cplx<R> zv = mk<R>(0, 0), zdy = mk<R>(0, 0), zdx = mk<R>(0, 0);
+#pragma unroll
+              for (int jy = 0; jy < kMaxJ; ++jy) {
+                if (jy < geo.J[1 % D]) {
+                  cplx<R> rv = mk<R>(0, 0), rd = mk<R>(0, 0);
+                  const cplx<R>* row =
+                      plane + ((local[0] + jz) * geo.P[1 % D] + local[1 % D] + jy) * geo.P[2 % D] + local[2 % D];
+#pragma unroll
+                  for (int jx = 0; jx < kMaxJ; ++jx) {
+                    if (jx < geo.J[2 % D]) {
+                      const cplx<R> x = row[jx];
+                      rv = cfma<R>(hv[2 % D][jx], x, rv);
+                      rd = cfma<R>(hd[2 % D][jx], x, rd);
+                    }
+                  }
+                  zv = cfma<R>(hv[1 % D][jy], rv, zv);
+                  zdy = cfma<R>(hd[1 % D][jy], rv, zdy);
+                  zdx = cfma<R>(hv[1 % D][jy], rd, zdx);
+                }
+              }
+              // jz is a runtime index, so hv[0][jz] is read through a select chain
+              cplx<R> hz = hv[0][0], dz = hd[0][0];
+#pragma unroll
+              for (int q = 1; q < kMaxJ; ++q)
+                if (q == jz) {
+                  hz = hv[0][q];
+                  dz = hd[0][q];
+                }
+              val = cfma<R>(hz, zv, val);
+              der[0] = cfma<R>(dz, zv, der[0]);
+              der[1 % D] = cfma<R>(hz, zdy, der[1 % D]);
+              der[2 % D] = cfma<R>(hz, zdx, der[2 % D]);
+            }
           }
         }
-        R sn, cs;
-        sincos_acc(phase_arg<R, D>(om, geo.nshift), &sn, &cs);
-        const cplx<R> ph = mk<R>(cs, sn);
-        const cplx<R> vv = v[(b * a.C + c0 + c) * a.M + m];
+        const cplx<R> p = ph[i];
+        const cplx<R> vv = v[(jc.b * a.C + jc.c0 + c) * a.M + m];
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           // dy/d omega_d = phase * (der_d / gam_d + i * nshift_d * val)
           const cplx<R> inner = mk<R>(der[d].x / geo.gam[d] - geo.nshift[d] * val.y,
                                       der[d].y / geo.gam[d] + geo.nshift[d] * val.x);
-          const cplx<R> dy = cmul<R>(ph, inner);
+          const cplx<R> dy = cmul<R>(p, inner);
           gsum[d] = vv.x * dy.x + vv.y * dy.y;  // Re(conj(v) * dy)
         }
       }
@@ -516,7 +587,7 @@ __global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, 
       }
       if (ok && c == 0) {
 #pragma unroll
-        for (int d = 0; d < D; ++d) atomicAdd(&grad[(t * D + d) * a.M + m], gsum[d]);
+        for (int d = 0; d < D; ++d) atomicAdd(&grad[(jc.t * D + d) * a.M + m], gsum[d]);
       }
       if (active && !ok && c == 0) atomicOr(&g_status, kStatusNonFinite | kStatusOutsidePatch);
     }
@@ -542,8 +613,10 @@ struct InterpPlan {
   int64_t max_jobs;
 };
 
+enum class Op { kFwd, kAdj, kGrad };
+
 template <typename R>
-static int prepare(const tkbn_geometry* g, const tkbn_points_desc* p, const void* ws, int64_t B, int64_t C,
+static int prepare(const tkbn_geometry* g, const tkbn_points_desc* p, const void* ws, int64_t B, int64_t C, Op op,
                    InterpPlan* ip) {
   int rc = points_layout(g, p, &ip->L);
   if (rc) return rc;
@@ -573,13 +646,18 @@ static int prepare(const tkbn_geometry* g, const tkbn_points_desc* p, const void
   a.nbpt = p->ntraj == 1 ? B : 1;
   int cells = 1;
   a.gtot = 1;
+  bool j6 = true;
   for (int d = 0; d < g->ndim; ++d) {
     cells *= ip->L.tile[d] + g->numpoints[d] - 1;
     a.gtot *= g->grid_size[d];
+    j6 = j6 && g->numpoints[d] == 6;
   }
   a.cells = cells;
   a.ps = cells | 1;  // odd plane stride spreads coil planes over banks
-  ip->smem = (size_t)a.Cc * a.ps * sizeof(cplx<R>);
+  const int nj = j6 ? 6 : kMaxJ;
+  a.scratch = (32 / a.Cc) * g->ndim * nj;
+  const size_t patch = op == Op::kAdj ? (size_t)2 * a.Cc * a.ps * sizeof(R) : (size_t)a.Cc * a.ps * sizeof(cplx<R>);
+  ip->smem = patch + (op == Op::kGrad ? 0 : (size_t)kWarps * a.scratch * sizeof(cplx<R>));
   if (ip->smem > 220 * 1024)
     return set_error(TKBN_ERR_UNSUPPORTED, "tile patch needs %zu bytes of shared memory", ip->smem);
   ip->max_jobs = ip->L.max_items * a.nbpt * a.ncc;
@@ -612,8 +690,8 @@ static int launch_fwd_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws,
   int blocks;
   int rc = resident_blocks(k, ip.smem, ip.max_jobs, &blocks);
   if (rc) return rc;
-  k<<<blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords), (const cplx<R>*)grid,
-                                         (cplx<R>*)kdata);
+  k<<<blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords),
+                                      (const cplx<R>*)(ws + ip.L.off_phase), (const cplx<R>*)grid, (cplx<R>*)kdata);
   return check_cuda(cudaGetLastError(), "interp_fwd launch");
 }
 
@@ -624,9 +702,22 @@ static int launch_adj_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws,
   int blocks;
   int rc = resident_blocks(k, ip.smem, ip.max_jobs, &blocks);
   if (rc) return rc;
-  k<<<blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords), (const cplx<R>*)kdata,
-                                         (cplx<R>*)grid);
+  k<<<blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords),
+                                      (const cplx<R>*)(ws + ip.L.off_phase), (const cplx<R>*)kdata, (cplx<R>*)grid);
   return check_cuda(cudaGetLastError(), "interp_adj launch");
+}
+
+template <typename R, int D>
+static int launch_grad_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* grid, const void* v,
+                         void* grad, cudaStream_t s) {
+  auto k = k_interp_grad<R, D>;
+  int blocks;
+  int rc = resident_blocks(k, ip.smem, ip.max_jobs, &blocks);
+  if (rc) return rc;
+  k<<<blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords),
+                                      (const cplx<R>*)(ws + ip.L.off_phase), (const cplx<R>*)grid,
+                                      (const cplx<R>*)v, (R*)grad);
+  return check_cuda(cudaGetLastError(), "interp_grad launch");
 }
 
 static bool all_j(const tkbn_geometry* g, int j) {
@@ -639,7 +730,7 @@ template <typename R>
 static int interp_fwd_r(const tkbn_geometry* g, const tkbn_points_desc* p, const void* ws, const void* const* tables,
                         const void* grid, int64_t B, int64_t C, void* kdata, cudaStream_t s) {
   InterpPlan ip;
-  int rc = prepare<R>(g, p, ws, B, C, &ip);
+  int rc = prepare<R>(g, p, ws, B, C, Op::kFwd, &ip);
   if (rc) return rc;
   if (p->npts == 0) return TKBN_OK;
   Geo<R> geo = make_geo<R>(g, &ip.L, tables, nullptr);
@@ -659,7 +750,7 @@ template <typename R>
 static int interp_adj_r(const tkbn_geometry* g, const tkbn_points_desc* p, const void* ws, const void* const* tables,
                         const void* kdata, int64_t B, int64_t C, void* grid, cudaStream_t s) {
   InterpPlan ip;
-  int rc = prepare<R>(g, p, ws, B, C, &ip);
+  int rc = prepare<R>(g, p, ws, B, C, Op::kAdj, &ip);
   if (rc) return rc;
   rc = check_cuda(cudaMemsetAsync(grid, 0, (size_t)(B * C * ip.a.gtot) * sizeof(cplx<R>), s), "zero grid");
   if (rc || p->npts == 0) return rc;
@@ -676,24 +767,12 @@ static int interp_adj_r(const tkbn_geometry* g, const tkbn_points_desc* p, const
   }
 }
 
-template <typename R, int D>
-static int launch_grad_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* grid, const void* v,
-                         void* grad, cudaStream_t s) {
-  auto k = k_interp_grad<R, D>;
-  int blocks;
-  int rc = resident_blocks(k, ip.smem, ip.max_jobs, &blocks);
-  if (rc) return rc;
-  k<<<blocks, kThreads, ip.smem, s>>>(geo, ip.a, (const R*)(ws + ip.L.off_coords), (const cplx<R>*)grid,
-                                         (const cplx<R>*)v, (R*)grad);
-  return check_cuda(cudaGetLastError(), "interp_grad launch");
-}
-
 template <typename R>
 static int interp_grad_r(const tkbn_geometry* g, const tkbn_points_desc* p, const void* ws, const void* const* tables,
                          const void* const* dtables, const void* grid, const void* v, int64_t B, int64_t C,
                          void* grad, cudaStream_t s) {
   InterpPlan ip;
-  int rc = prepare<R>(g, p, ws, B, C, &ip);
+  int rc = prepare<R>(g, p, ws, B, C, Op::kGrad, &ip);
   if (rc) return rc;
   if (!dtables) return set_error(TKBN_ERR_INVALID, "derivative tables are required");
   rc = check_cuda(cudaMemsetAsync(grad, 0, (size_t)(p->ntraj * g->ndim * p->npts) * sizeof(R), s), "zero grad");

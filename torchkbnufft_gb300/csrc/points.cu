@@ -92,14 +92,27 @@ __global__ void k_gather_items(const Item* __restrict__ items, const int32_t* __
     out[i] = items[order[i]];
 }
 
+// Per sorted point: normalised frequency tm_d = omega_d / gam_d and the
+// fftshift phase exp(i sum_d omega_d n_shift_d), both with the reference's
+// rounding (see base_index / phase_arg). The interpolation kernels read only
+// these, never omega.
 template <typename R>
-__global__ void k_sorted_coords(const R* __restrict__ omega, const int32_t* __restrict__ vals, int64_t M,
-                                int ndim, int64_t n, R* __restrict__ coords) {
+__global__ void k_sorted_points(Geo<R> geo, const R* __restrict__ omega, const int32_t* __restrict__ vals, int64_t M,
+                                int64_t n, R* __restrict__ tm, cplx<R>* __restrict__ ph) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t v = vals[i];
     const int64_t t = v / M;
     const int64_t m = v - t * M;
-    for (int d = 0; d < ndim; ++d) coords[d * n + i] = omega[(t * ndim + d) * M + m];
+    R om[kMaxDim];
+    for (int d = 0; d < geo.ndim; ++d) {
+      om[d] = omega[(t * geo.ndim + d) * M + m];
+      tm[d * n + i] = div_rn(om[d], geo.gam[d]);
+    }
+    R a = mul_rn(om[0], geo.nshift[0]);
+    for (int d = 1; d < geo.ndim; ++d) a = add_rn(a, mul_rn(om[d], geo.nshift[d]));
+    R sn, cs;
+    sincos_acc(a, &sn, &cs);
+    ph[i] = mk<R>(cs, sn);
   }
 }
 
@@ -215,6 +228,8 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   o = align_up(o + 4 * L->max_items);
   L->off_coords = o;
   o = align_up(o + rsize * g->ndim * n);
+  L->off_phase = o;
+  o = align_up(o + 2 * rsize * n);
   L->off_cub = o;
   o = align_up(o + L->cub_bytes);
   L->total = o;
@@ -278,7 +293,9 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
                                       L.item_key_bits, s) != cudaSuccess)
     return set_error(TKBN_ERR_CUDA, "item sort failed");
   k_gather_items<<<blocks_for(L.max_items), threads, 0, s>>>(items_raw, ivals, L.max_items, items);
-  if (n > 0) k_sorted_coords<R><<<blocks_for(n), threads, 0, s>>>((const R*)omega, vals, p->npts, g->ndim, n, coords);
+  if (n > 0)
+    k_sorted_points<R><<<blocks_for(n), threads, 0, s>>>(geo, (const R*)omega, vals, p->npts, n, coords,
+                                                         (cplx<R>*)(ws + L.off_phase));
   return check_cuda(cudaGetLastError(), "points build launch");
 }
 

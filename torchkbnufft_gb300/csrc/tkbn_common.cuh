@@ -181,7 +181,7 @@ struct PointsLayout {
   int ntile[3];
   int chunk;
   size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
-      off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_cub;
+      off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_phase, off_cub;
   size_t cub_bytes;
   size_t total;
 };
