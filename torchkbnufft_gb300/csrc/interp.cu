@@ -293,10 +293,10 @@ __device__ __forceinline__ void flush_patch(const Geo<R>& geo, cplx<R>* __restri
     const int c = r / rows_per_plane;
     const int rr = r - c * rows_per_plane;
     cplx<R>* dst = grid + (plane0 + c) * gtot + patch_row_base<R, D>(geo, rr, origin);
+    // pre and pim are the bases of the real and imaginary plane sets
     const int o = c * ps + rr * PX;
-    const int oi = (Cc + c) * ps + rr * PX;
     for (int px = lane; px < PX; px += 32) {
-      const cplx<R> v = mk<R>(pre[o + px], pim[oi + px]);
+      const cplx<R> v = mk<R>(pre[o + px], pim[o + px]);
       if (v.x == R(0) && v.y == R(0)) continue;
       int gx = origin[D - 1] + px;
       gx = gx >= KX ? gx - KX * (gx / KX) : gx;
