@@ -81,7 +81,7 @@ __device__ __forceinline__ bool point_base(const Geo<R>& geo, const R* __restric
     const R f = floor(sub_rn(t, geo.halfJ[d]));
     const bool fin = fabs(f) < R(1 << 30);
     base[d] = fin ? 1 + (int)f : 0;
-    const int l = pmod(base[d], geo.K[d]) - origin[d];
+    const int l = wrap_cell(base[d], geo.K[d]) - origin[d];
     local[d] = l;
     ok = ok && fin && (l >= 0) && (l < geo.T[d]);
   }
@@ -131,40 +131,47 @@ __device__ __forceinline__ void table_factors(const Geo<R>& geo, const R* tmv, c
   }
 }
 
-// Row decomposition of a patch: a row is P[D-1] cells contiguous in smem and
-// (up to the periodic wrap) contiguous in the global grid.
+// Non-negative x reduced into [0, k) by repeated subtraction (patch offsets
+// exceed k by less than one tile, so this is one compare in practice).
+__device__ __forceinline__ int wrap_up(int x, int k) {
+  while (x >= k) x -= k;
+  return x;
+}
+
+// Global offset of patch row rr (the outer coordinates of a row of P[D-1]
+// cells), wrapped periodically.
 template <typename R, int D>
-__device__ __forceinline__ int64_t patch_row_base(const Geo<R>& geo, int row, const int* origin) {
-  int64_t flat = 0, stride = geo.K[D - 1];
-#pragma unroll
-  for (int d = D - 2; d >= 0; --d) {
-    const int p = row % geo.P[d];
-    row /= geo.P[d];
-    flat += (int64_t)pmod(origin[d] + p, geo.K[d]) * stride;
-    stride *= geo.K[d];
-  }
-  return flat;
+__device__ __forceinline__ int64_t patch_row_base(const Geo<R>& geo, int rr, const int* origin) {
+  if (D == 1) return 0;
+  if (D == 2) return (int64_t)wrap_up(origin[0] + rr, geo.K[0]) * geo.K[1];
+  const int pz = rr / geo.P[1 % D];
+  const int py = rr - pz * geo.P[1 % D];
+  return ((int64_t)wrap_up(origin[0] + pz, geo.K[0]) * geo.K[1 % D] + wrap_up(origin[1 % D] + py, geo.K[1 % D])) *
+         geo.K[2 % D];
 }
 
 // Stage Cc coil planes of the periodic patch [origin, origin + P) into smem:
-// one warp per patch row, lanes along the innermost dimension.
+// one warp per patch row, lanes along the innermost dimension; each lane
+// wraps its column offsets once per job.
 template <typename R, int D>
 __device__ __forceinline__ void load_patch(const Geo<R>& geo, const cplx<R>* __restrict__ grid, int64_t plane0,
                                            int64_t gtot, int ncl, int cells, int ps, const int* origin,
                                            cplx<R>* patch) {
   const int PX = geo.P[D - 1];
   const int KX = geo.K[D - 1];
-  const int rows_per_plane = cells / PX;
+  const int rows = cells / PX;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int r = warp; r < ncl * rows_per_plane; r += kWarps) {
-    const int c = r / rows_per_plane;
-    const int rr = r - c * rows_per_plane;
-    const cplx<R>* src = grid + (plane0 + c) * gtot + patch_row_base<R, D>(geo, rr, origin);
-    cplx<R>* dst = patch + c * ps + rr * PX;
-    for (int px = lane; px < PX; px += 32) {
-      int gx = origin[D - 1] + px;
-      gx = gx >= KX ? gx - KX * (gx / KX) : gx;
-      dst[px] = src[gx];
+  const int gx0 = wrap_up(origin[D - 1] + lane, KX);
+  for (int rr = warp; rr < rows; rr += kWarps) {
+    const int64_t rbase = patch_row_base<R, D>(geo, rr, origin);
+    for (int c = 0; c < ncl; ++c) {
+      const cplx<R>* src = grid + (plane0 + c) * gtot + rbase;
+      cplx<R>* dst = patch + c * ps + rr * PX;
+      int gx = gx0;
+      for (int px = lane; px < PX; px += 32) {
+        dst[px] = src[gx];
+        gx = wrap_up(gx + 32, KX);
+      }
     }
   }
 }
@@ -420,6 +427,245 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj(Geo<R> geo, Launch a, c
     }
     __syncthreads();
     flush_patch<R, D>(geo, grid, jc.b * a.C + jc.c0, a.gtot, jc.ncl, a.cells, a.ps, a.Cc, jc.origin, pre, pim);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K4 (owned tiles): atomic-free, deterministic adjoint.
+//
+// A CTA owns one output tile (T cells per dim, no halo) of Cc coil planes and
+// accumulates, in shared memory, every point whose footprint reaches the tile:
+// the points of the tile itself and of the nsrc-1 tiles before it in each
+// dim. Points are taken in batches of kNB: the CTA first compacts the batch to
+// the points that reach the tile and stages their conjugated table factors
+// and phase-corrected k-space values; then each warp applies the batch to the
+// rows of the tile it owns (disjoint rows: plain read-modify-write, no
+// atomics; each cell sees its points in a fixed order). The tile is written
+// once with coalesced stores, so the grid needs no zeroing.
+// Requires K_d >= T_d + J_d - 1 (a footprint meets a tile in one run).
+
+constexpr int kNB = 64;
+
+struct OwnLaunch {
+  const int32_t* order;     // output tile keys, heaviest first
+  const int32_t* counts;    // points per key
+  const int32_t* tile_off;  // first sorted point of each key
+  const int32_t* vals;
+  int64_t n, M, ntraj, B, C;
+  int Cc, ncc;
+  int64_t nbpt;
+  int64_t nkeys;  // ntraj * ntiles
+  int tcells;     // prod T
+  int aps;        // accumulator plane stride (complex elements)
+  int64_t gtot;
+  SrcSpan span;
+};
+
+template <typename R, int D, int JC>
+__global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaunch a, const R* __restrict__ tm,
+                                                             const cplx<R>* __restrict__ ph,
+                                                             const cplx<R>* __restrict__ kdata,
+                                                             cplx<R>* __restrict__ grid) {
+  constexpr int NJ = NJOf<JC>::N;
+  constexpr int MAXCOMBO = D == 1 ? 8 : (D == 2 ? 16 : 27);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* acc = reinterpret_cast<cplx<R>*>(smem_raw);  // [Cc][aps]
+  cplx<R>* sfac = acc + a.Cc * a.aps;                    // [kNB][D*NJ], conjugated
+  cplx<R>* sv = sfac + kNB * D * NJ;                     // [kNB][Cc]
+  int* sloc = reinterpret_cast<int*>(sv + kNB * a.Cc);   // [kNB][D] footprint start relative to the tile
+  int* spt = sloc + kNB * D;                             // [kNB] sorted point index
+  int* slist = spt + kNB;                                // [MAXCOMBO] list starts
+  int* spre = slist + MAXCOMBO;                          // [MAXCOMBO + 1] candidate prefix
+  int* snv = spre + MAXCOMBO + 1;                        // [2] valid count per staging warp
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t njobs = a.nkeys * a.nbpt * a.ncc;
+  const int G = 32 / a.Cc;                       // lane groups per coil
+  const int c = lane % a.Cc, grp = lane / a.Cc;  // this lane's coil and x-group
+  const int JX = JC > 0 ? JC : geo.J[D - 1];
+  const int cpg = (JX + G - 1) / G;              // footprint columns per group
+  // rows of the tile (outer coordinates) owned by this warp: [r_lo, r_hi)
+  int trows = 1;
+#pragma unroll
+  for (int d = 0; d < D - 1; ++d) trows *= geo.T[d];
+  const int r_lo = (warp * trows) / kWarps, r_hi = ((warp + 1) * trows) / kWarps;
+  const int TX = geo.T[D - 1];
+
+  for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x) {
+    const int64_t kidx = job % a.nkeys;
+    const int64_t rest = job / a.nkeys;
+    const int cc = (int)(rest % a.ncc);
+    const int64_t bb = rest / a.ncc;
+    const int key = a.order[kidx];
+    const int64_t t = key / geo.ntiles;
+    const int64_t b = a.ntraj == 1 ? bb : t;
+    const int c0 = cc * a.Cc;
+    const int ncl = (int)min((int64_t)a.Cc, a.C - c0);
+    int td[kMaxDim] = {0, 0, 0}, origin[kMaxDim] = {0, 0, 0}, ext[kMaxDim] = {1, 1, 1};
+    {
+      int rem = (int)(key - t * geo.ntiles);
+#pragma unroll
+      for (int d = D - 1; d >= 0; --d) {
+        td[d] = rem % geo.ntile[d];
+        rem /= geo.ntile[d];
+        origin[d] = td[d] * geo.T[d];
+        ext[d] = min(geo.T[d], geo.K[d] - origin[d]);
+      }
+    }
+    __syncthreads();  // previous job's write-out done with acc / lists
+    if (threadIdx.x < a.span.ncombo) {
+      const int skey = (int)(t * geo.ntiles) + source_tile(geo, a.span, td, threadIdx.x);
+      slist[threadIdx.x] = a.tile_off[skey];
+      spre[threadIdx.x + 1] = a.counts[skey];
+    }
+    if (threadIdx.x == 0) spre[0] = 0;
+    for (int idx = threadIdx.x; idx < a.Cc * a.aps; idx += kThreads) acc[idx] = mk<R>(0, 0);
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int l = 0; l < a.span.ncombo; ++l) spre[l + 1] += spre[l];
+    __syncthreads();
+    const int total = spre[a.span.ncombo];
+
+    for (int q0 = 0; q0 < total; q0 += kNB) {
+      // A1: which candidates reach the tile; compact them (two staging warps)
+      if (warp < kNB / 32) {
+        const int q = q0 + threadIdx.x;
+        bool valid = false;
+        int i = 0, rel[kMaxDim] = {0, 0, 0};
+        if (q < total) {
+          int l = 0;
+          while (spre[l + 1] <= q) ++l;
+          i = slist[l] + (q - spre[l]);
+          valid = true;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            const R tv = tm[d * a.n + i];
+            const R f = floor(sub_rn(tv, geo.halfJ[d]));
+            const bool fin = fabs(f) < R(1 << 30);
+            const int w = fin ? wrap_cell(1 + (int)f, geo.K[d]) : 0;
+            int r = w - origin[d];
+            if (r >= geo.T[d]) r -= geo.K[d];
+            const int J = JC > 0 ? JC : geo.J[d];
+            valid = valid && fin && (r > -J) && (r < ext[d]);
+            rel[d] = r;
+          }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, valid);
+        if (lane == 0) snv[warp] = __popc(bal);
+        __syncwarp();
+        // positions: warp 0 first, then warp 1 (written after both counts are known)
+        asm volatile("bar.sync 1, 64;");
+        const int pos = (warp == 0 ? 0 : snv[0]) + __popc(bal & ((1u << lane) - 1));
+        if (valid) {
+          spt[pos] = i;
+#pragma unroll
+          for (int d = 0; d < D; ++d) sloc[pos * D + d] = rel[d];
+        }
+      }
+      __syncthreads();
+      const int nv = snv[0] + snv[1];
+      // A2: conjugated table factors and conj(phase) * kdata of the staged points
+      for (int e = threadIdx.x; e < nv * D * NJ; e += kThreads) {
+        const int p = e / (D * NJ);
+        const int f = e - p * (D * NJ);
+        const int d = f / NJ, j = f - d * NJ;
+        const int J = JC > 0 ? JC : sel<int, 3>(geo.J, d);
+        cplx<R> v = mk<R>(0, 0);
+        if (j < J) {
+          const int i = spt[p];
+          const R tv = tm[d * a.n + i];
+          const int base = 1 + (int)floor(sub_rn(tv, sel<R, 3>(geo.halfJ, d)));
+          const int k = table_bin<R>(tv, base + j, sel<R, 3>(geo.Lr, d), sel<int, 3>(geo.center, d),
+                                     sel<int, 3>(geo.tmax, d));
+          v = cconj<R>(__ldg(&sel<const cplx<R>*, 3>(geo.tab, d)[k]));
+        }
+        sfac[e] = v;
+      }
+      for (int e = threadIdx.x; e < nv * a.Cc; e += kThreads) {
+        const int p = e / a.Cc;
+        const int cl = e - p * a.Cc;
+        cplx<R> v = mk<R>(0, 0);
+        if (cl < ncl) {
+          const int i = spt[p];
+          const int64_t m = a.vals[i] - t * a.M;
+          v = cmulc<R>(kdata[(b * a.C + c0 + cl) * a.M + m], ph[i]);
+        }
+        sv[e] = v;
+      }
+      __syncthreads();
+      // B: each warp applies the staged points to its rows
+      for (int p = 0; p < nv; ++p) {
+        const int* loc = sloc + p * D;
+        const cplx<R>* fp = sfac + p * D * NJ;
+        const cplx<R> v = sv[p * a.Cc + c];
+        if (D == 1) {
+          if (warp == 0) {
+            for (int k = 0; k < cpg; ++k) {
+              const int jx = grp * cpg + k;
+              const int x = loc[0] + jx;
+              if (jx < JX && x >= 0 && x < ext[0]) {
+                cplx<R>* cell = acc + c * a.aps + x;
+                *cell = cfma<R>(v, fp[jx], *cell);
+              }
+            }
+          }
+        } else if (D == 2) {
+          const int JY = JC > 0 ? JC : geo.J[0];
+          const int jlo = max(0, r_lo - loc[0]);
+          const int jhi = min(JY, min(r_hi, ext[0]) - loc[0]);
+          for (int jy = jlo; jy < jhi; ++jy) {
+            const cplx<R> vy = cmul<R>(v, fp[jy]);
+            cplx<R>* row = acc + c * a.aps + (loc[0] + jy) * TX;
+            for (int k = 0; k < cpg; ++k) {
+              const int jx = grp * cpg + k;
+              const int x = loc[1] + jx;
+              if (jx < JX && x >= 0 && x < ext[1]) row[x] = cfma<R>(vy, fp[NJ + jx], row[x]);
+            }
+          }
+        } else {
+          const int JZ = JC > 0 ? JC : geo.J[0];
+          const int JY = JC > 0 ? JC : geo.J[1 % D];
+          const int T1 = geo.T[1 % D];
+          for (int jz = 0; jz < JZ; ++jz) {
+            const int z = loc[0] + jz;
+            if (z < 0 || z >= ext[0]) continue;
+            const cplx<R> vz = cmul<R>(v, fp[jz]);
+            for (int jy = 0; jy < JY; ++jy) {
+              const int y = loc[1 % D] + jy;
+              const int rr = z * T1 + y;
+              if (y < 0 || y >= ext[1 % D] || rr < r_lo || rr >= r_hi) continue;
+              const cplx<R> vy = cmul<R>(vz, fp[NJ + jy]);
+              cplx<R>* row = acc + c * a.aps + rr * TX;
+              for (int k = 0; k < cpg; ++k) {
+                const int jx = grp * cpg + k;
+                const int x = loc[2 % D] + jx;
+                if (jx < JX && x >= 0 && x < ext[2 % D]) row[x] = cfma<R>(vy, fp[2 * NJ + jx], row[x]);
+              }
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // C: write the tile (rows of TX cells, coalesced)
+    for (int r = warp; r < ncl * trows; r += kWarps) {
+      const int cl = r / trows;
+      const int rr = r - cl * trows;
+      int64_t off = 0;
+      bool inside = true;
+      if (D == 2) {
+        inside = rr < ext[0];
+        off = (int64_t)(origin[0] + rr) * geo.K[1];
+      } else if (D == 3) {
+        const int z = rr / geo.T[1 % D], y = rr - (rr / geo.T[1 % D]) * geo.T[1 % D];
+        inside = z < ext[0] && y < ext[1 % D];
+        off = ((int64_t)(origin[0] + z) * geo.K[1 % D] + origin[1 % D] + y) * geo.K[2 % D];
+      }
+      if (!inside) continue;
+      cplx<R>* dst = grid + (b * a.C + c0 + cl) * a.gtot + off + origin[D - 1];
+      const cplx<R>* src = acc + cl * a.aps + rr * TX;
+      for (int x = lane; x < ext[D - 1]; x += 32) dst[x] = src[x];
+    }
   }
 }
 
@@ -746,9 +992,83 @@ static int interp_fwd_r(const tkbn_geometry* g, const tkbn_points_desc* p, const
   }
 }
 
+template <int D>
+constexpr int max_combo() {
+  return D == 1 ? 8 : (D == 2 ? 16 : 27);
+}
+
+template <typename R, int D, int JC>
+static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* kdata, void* grid,
+                            cudaStream_t s) {
+  constexpr int NJ = NJOf<JC>::N;
+  OwnLaunch o;
+  o.order = (const int32_t*)(ws + ip.L.off_tile_order);
+  o.counts = (const int32_t*)(ws + ip.L.off_counts);
+  o.tile_off = (const int32_t*)(ws + ip.L.off_tile_off);
+  o.vals = ip.a.vals;
+  o.n = ip.a.n;
+  o.M = ip.a.M;
+  o.ntraj = ip.a.ntraj;
+  o.B = ip.a.B;
+  o.C = ip.a.C;
+  o.Cc = ip.a.Cc;
+  o.ncc = ip.a.ncc;
+  o.nbpt = ip.a.nbpt;
+  o.nkeys = ip.L.nkeys;
+  o.tcells = 1;
+  for (int d = 0; d < D; ++d) o.tcells *= ip.L.tile[d];
+  o.aps = o.tcells | 1;
+  o.gtot = ip.a.gtot;
+  o.span = ip.L.span;
+  const size_t smem = (size_t)o.Cc * o.aps * sizeof(cplx<R>) + (size_t)kNB * D * NJ * sizeof(cplx<R>) +
+                      (size_t)kNB * o.Cc * sizeof(cplx<R>) + sizeof(int) * ((size_t)kNB * D + kNB + 2 * max_combo<D>() + 3);
+  if (smem > 220 * 1024) return set_error(TKBN_ERR_UNSUPPORTED, "adjoint tile needs %zu bytes of shared memory", smem);
+  auto k = k_interp_adj_own<R, D, JC>;
+  int blocks;
+  int rc = resident_blocks(k, smem, o.nkeys * o.nbpt * o.ncc, &blocks);
+  if (rc) return rc;
+  k<<<blocks, kThreads, smem, s>>>(geo, o, (const R*)(ws + ip.L.off_coords), (const cplx<R>*)(ws + ip.L.off_phase),
+                                   (const cplx<R>*)kdata, (cplx<R>*)grid);
+  return check_cuda(cudaGetLastError(), "interp_adj launch");
+}
+
+template <typename R, int D, int JC>
+static int adj_dispatch(const Geo<R>& geo, const InterpPlan& ip, const char* w, const void* kdata, void* grid,
+                        int64_t B, int64_t C, cudaStream_t s) {
+  if (ip.L.owned_ok && ip.L.span.ncombo <= max_combo<D>()) return launch_adj_own_t<R, D, JC>(geo, ip, w, kdata, grid, s);
+  int rc = check_cuda(cudaMemsetAsync(grid, 0, (size_t)(B * C * ip.a.gtot) * sizeof(cplx<R>), s), "zero grid");
+  if (rc) return rc;
+  return launch_adj_t<R, D, JC>(geo, ip, w, kdata, grid, s);
+}
+
 template <typename R>
 static int interp_adj_r(const tkbn_geometry* g, const tkbn_points_desc* p, const void* ws, const void* const* tables,
                         const void* kdata, int64_t B, int64_t C, void* grid, cudaStream_t s) {
+  InterpPlan ip;
+  int rc = prepare<R>(g, p, ws, B, C, Op::kAdj, &ip);
+  if (rc) return rc;
+  if (p->npts == 0)
+    return check_cuda(cudaMemsetAsync(grid, 0, (size_t)(B * C * ip.a.gtot) * sizeof(cplx<R>), s), "zero grid");
+  Geo<R> geo = make_geo<R>(g, &ip.L, tables, nullptr);
+  const char* w = (const char*)ws;
+  const bool j6 = all_j(g, 6);
+  switch (g->ndim) {
+    case 1:
+      return j6 ? adj_dispatch<R, 1, 6>(geo, ip, w, kdata, grid, B, C, s)
+                : adj_dispatch<R, 1, 0>(geo, ip, w, kdata, grid, B, C, s);
+    case 2:
+      return j6 ? adj_dispatch<R, 2, 6>(geo, ip, w, kdata, grid, B, C, s)
+                : adj_dispatch<R, 2, 0>(geo, ip, w, kdata, grid, B, C, s);
+    default:
+      return j6 ? adj_dispatch<R, 3, 6>(geo, ip, w, kdata, grid, B, C, s)
+                : adj_dispatch<R, 3, 0>(geo, ip, w, kdata, grid, B, C, s);
+  }
+}
+
+template <typename R>
+static int interp_adj_atomic_r(const tkbn_geometry* g, const tkbn_points_desc* p, const void* ws,
+                               const void* const* tables, const void* kdata, int64_t B, int64_t C, void* grid,
+                               cudaStream_t s) {
   InterpPlan ip;
   int rc = prepare<R>(g, p, ws, B, C, Op::kAdj, &ip);
   if (rc) return rc;

@@ -92,6 +92,30 @@ __global__ void k_gather_items(const Item* __restrict__ items, const int32_t* __
     out[i] = items[order[i]];
 }
 
+// Adjoint work of an output tile: the points of every tile whose footprints
+// can reach it (itself and up to nsrc-1 tiles before it in each dim). The
+// sort key is the bitwise complement, so an ascending sort puts the heaviest
+// tile first.
+template <typename R>
+__global__ void k_tile_work(Geo<R> geo, const int32_t* __restrict__ counts, int64_t nkeys, SrcSpan span,
+                            uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nkeys; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = k / geo.ntiles;
+    int rem = (int)(k - t * geo.ntiles);
+    int td[kMaxDim] = {0, 0, 0};
+    for (int d = geo.ndim - 1; d >= 0; --d) {
+      td[d] = rem % geo.ntile[d];
+      rem /= geo.ntile[d];
+    }
+    int64_t work = 0;
+    for (int combo = 0; combo < span.ncombo; ++combo) {
+      work += counts[t * geo.ntiles + source_tile(geo, span, td, combo)];
+    }
+    keys[k] = ~(uint32_t)(work > 0x7fffffff ? 0x7fffffff : work);
+    vals[k] = (int32_t)k;
+  }
+}
+
 // Per sorted point: normalised frequency tm_d = omega_d / gam_d and the
 // fftshift phase exp(i sum_d omega_d n_shift_d), both with the reference's
 // rounding (see base_index / phase_arg). The interpolation kernels read only
@@ -137,12 +161,15 @@ int check_cuda(cudaError_t e, const char* what) {
 }
 
 void default_tiles(const tkbn_geometry* g, int tile[3], int* chunk) {
-  const int dflt2 = g->dtype == TKBN_C64 ? 16 : 16;
   for (int d = 0; d < 3; ++d) tile[d] = 1;
   if (g->ndim == 1) {
     tile[0] = 128;
   } else if (g->ndim == 2) {
-    tile[0] = tile[1] = dflt2;
+    // 14 x 16 cells: a 19 x 21 forward patch of 16 complex64 coil planes is
+    // 51 KB, so four 256-thread CTAs fit an SM; 14 rows split evenly enough
+    // over the 8 warps of the adjoint's row ownership.
+    tile[0] = 14;
+    tile[1] = 16;
   } else {
     tile[0] = tile[1] = tile[2] = 4;
   }
@@ -194,6 +221,27 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
                                   (int32_t*)nullptr, (int)L->max_items, 0, ibits);
   L->cub_bytes = cub_sort > cub_scan ? cub_sort : cub_scan;
   if (cub_isort > L->cub_bytes) L->cub_bytes = cub_isort;
+  size_t cub_tsort = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, cub_tsort, (uint32_t*)nullptr, (uint32_t*)nullptr, (int32_t*)nullptr,
+                                  (int32_t*)nullptr, (int)L->nkeys, 0, 32);
+  if (cub_tsort > L->cub_bytes) L->cub_bytes = cub_tsort;
+  // output-tile sources for the adjoint
+  L->span.ncombo = 1;
+  L->owned_ok = true;
+  for (int d = 0; d < 3; ++d) {
+    if (d >= g->ndim) {
+      L->span.nsrc[d] = 1;
+      continue;
+    }
+    const int T = L->tile[d];
+    const int lastw = (int)(g->grid_size[d] - (int64_t)(L->ntile[d] - 1) * T);
+    const int minw = lastw < T ? lastw : T;
+    int ns = 1 + (g->numpoints[d] - 1 + minw - 1) / minw;
+    if (ns > L->ntile[d]) ns = L->ntile[d];
+    L->span.nsrc[d] = ns;
+    L->span.ncombo *= ns;
+    if (g->grid_size[d] < (int64_t)T + g->numpoints[d] - 1) L->owned_ok = false;
+  }
 
   size_t o = 0;
   L->off_hdr = o;
@@ -226,6 +274,8 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   o = align_up(o + 4 * L->max_items);
   L->off_ivals = o;
   o = align_up(o + 4 * L->max_items);
+  L->off_tile_order = o;
+  o = align_up(o + 4 * L->nkeys);
   L->off_coords = o;
   o = align_up(o + rsize * g->ndim * n);
   L->off_phase = o;
@@ -293,6 +343,12 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
                                       L.item_key_bits, s) != cudaSuccess)
     return set_error(TKBN_ERR_CUDA, "item sort failed");
   k_gather_items<<<blocks_for(L.max_items), threads, 0, s>>>(items_raw, ivals, L.max_items, items);
+  // adjoint tile order, heaviest first (reuses the item sort buffers; nkeys <= max_items)
+  k_tile_work<R><<<blocks_for(L.nkeys), threads, 0, s>>>(geo, counts, L.nkeys, L.span, ikeys_in, ivals_in);
+  tb = L.cub_bytes;
+  if (cub::DeviceRadixSort::SortPairs(cubtmp, tb, ikeys_in, ikeys, ivals_in, (int32_t*)(ws + L.off_tile_order),
+                                      (int)L.nkeys, 0, 32, s) != cudaSuccess)
+    return set_error(TKBN_ERR_CUDA, "tile sort failed");
   if (n > 0)
     k_sorted_points<R><<<blocks_for(n), threads, 0, s>>>(geo, (const R*)omega, vals, p->npts, n, coords,
                                                          (cplx<R>*)(ws + L.off_phase));

@@ -127,6 +127,44 @@ __device__ __forceinline__ int pmod(int a, int k) {
   return r < 0 ? r + k : r;
 }
 
+// a mod k for a within one period of [0, k) (the usual case: one compare and
+// add), falling back to the general modulo otherwise.
+__device__ __forceinline__ int wrap_cell(int a, int k) {
+  int w = a < 0 ? a + k : (a >= k ? a - k : a);
+  if ((unsigned)w >= (unsigned)k) w = pmod(a, k);
+  return w;
+}
+
+// Tiles whose points can reach an output tile: per dim, the tile itself and
+// up to nsrc-1 tiles before it (periodic). ncombo = prod nsrc.
+struct SrcSpan {
+  int nsrc[kMaxDim];
+  int ncombo;
+};
+
+// Linear tile index (within one trajectory) of source combination `combo`
+// for the output tile with per-dim tile coordinates td.
+template <typename R>
+__device__ __forceinline__ int source_tile(const Geo<R>& geo, const SrcSpan& span, const int* td, int combo) {
+  int rest = combo;
+  int sd[kMaxDim] = {0, 0, 0};
+#pragma unroll
+  for (int d = kMaxDim - 1; d >= 0; --d) {
+    if (d < geo.ndim) {
+      const int delta = rest % span.nsrc[d];
+      rest /= span.nsrc[d];
+      int s = td[d] - delta;
+      if (s < 0) s += geo.ntile[d];
+      sd[d] = s;
+    }
+  }
+  int key = 0;
+#pragma unroll
+  for (int d = 0; d < kMaxDim; ++d)
+    if (d < geo.ndim) key = key * geo.ntile[d] + sd[d];
+  return key;
+}
+
 // First neighbour index of a point along one dimension: 1 + floor(tm - J/2),
 // with tm = omega / gam (torchkbnufft/_nufft/interp.py:171, 177). Returns
 // false for coordinates that are not finite or far outside any grid.
@@ -180,8 +218,11 @@ struct PointsLayout {
   int tile[3];
   int ntile[3];
   int chunk;
+  tkbn::SrcSpan span;  // source tiles of an output tile (adjoint)
+  bool owned_ok;       // every K_d >= T_d + J_d - 1: a footprint meets a tile in one contiguous run
   size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
-      off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_phase, off_cub;
+      off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_phase, off_tile_order,
+      off_cub;
   size_t cub_bytes;
   size_t total;
 };
