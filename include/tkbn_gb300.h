@@ -68,6 +68,11 @@ extern "C" {
 #define TKBN_NORM_NONE 0  /* forward unnormalised, inverse without 1/N */
 #define TKBN_NORM_ORTHO 1 /* 1/sqrt(prod K) both ways                  */
 
+/* geometry flags */
+#define TKBN_TABLES_CONJ_SYMMETRIC 1 /* table[J*L/2 + k] == conj(table[J*L/2 - k]) exactly, for
+                                        every dim with J*L even (true for KB tables); the
+                                        kernels then read only the first half of each table */
+
 /* Operator geometry (one per KbModule). Unused dims (>= ndim) are ignored. */
 typedef struct tkbn_geometry {
   int32_t ndim;              /* 1, 2 or 3 */
@@ -77,6 +82,7 @@ typedef struct tkbn_geometry {
   int32_t numpoints[3];      /* J_d, 1..8 */
   int32_t table_oversamp[3]; /* L_d */
   double n_shift[3];         /* fftshift distance per dim */
+  int32_t flags;             /* TKBN_TABLES_* bits */
 } tkbn_geometry;
 
 /* Sorted-point layout of one trajectory set (built by tkbn_points_build). */

@@ -35,7 +35,11 @@ class Geometry(ctypes.Structure):
         ("numpoints", ctypes.c_int32 * 3),
         ("table_oversamp", ctypes.c_int32 * 3),
         ("n_shift", ctypes.c_double * 3),
+        ("flags", ctypes.c_int32),
     ]
+
+
+TKBN_TABLES_CONJ_SYMMETRIC = 1
 
 
 class PointsDesc(ctypes.Structure):

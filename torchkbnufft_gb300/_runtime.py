@@ -102,11 +102,12 @@ class GeomKey:
 _geom_structs: dict = {}
 
 
-def geom_struct(key: GeomKey) -> L.Geometry:
-    s = _geom_structs.get(key)
+def geom_struct(key: GeomKey, flags: int = 0) -> L.Geometry:
+    s = _geom_structs.get((key, flags))
     if s is None:
         s = key.struct()
-        _geom_structs[key] = s
+        s.flags = flags
+        _geom_structs[(key, flags)] = s
     return s
 
 
@@ -261,14 +262,54 @@ def _plan_geom(geom: GeomKey, plan: FFTPlan, B: int, C: int) -> Tuple[L.Geometry
 # ---------------------------------------------------------------- tables
 
 
-def table_ptrs(tables: Sequence[torch.Tensor], dtype: torch.dtype) -> Tuple[ctypes.Array, List[torch.Tensor]]:
+_table_props: "collections.OrderedDict" = collections.OrderedDict()
+
+
+def _cached_prop(key, t, fn):
+    with _lock:
+        hit = _table_props.get(key)
+        if hit is not None and hit[0]() is t:
+            return hit[1]
+    v = fn()
+    with _lock:
+        _table_props[key] = (weakref.ref(t), v)
+        while len(_table_props) > 64:
+            _table_props.popitem(last=False)
+    return v
+
+
+def _conj_symmetric(t: torch.Tensor) -> bool:
+    """table[c + k] == conj(table[c - k]) bitwise (c = (len - 1) / 2)."""
+    n = t.numel()
+    if n % 2 == 0:
+        return False
+    c = (n - 1) // 2
+    return _cached_prop(("sym", id(t), t._version, t.data_ptr()), t,
+                        lambda: bool(torch.equal(t[c + 1:], t[:c].flip(0).conj())))
+
+
+def table_ptrs(tables: Sequence[torch.Tensor], dtype: torch.dtype):
+    """Device pointers of the per-dim tables, the tensors kept alive, and geometry flags.
+
+    Tables with identical contents share one pointer (one cache footprint);
+    when every table is exactly conjugate-symmetric the kernels read half of it.
+    """
     keep = []
     for t in tables:
         require_cuda(t)
         if t.dtype != dtype:
             t = t.to(dtype)
         keep.append(t.contiguous())
-    return L.ptr_array([t.data_ptr() for t in keep]), keep
+    ptrs = [t.data_ptr() for t in keep]
+    for d in range(1, len(keep)):
+        a, b = keep[0], keep[d]
+        if a.shape == b.shape and ptrs[d] != ptrs[0]:
+            same = _cached_prop(("eq", id(b), b._version, b.data_ptr(), a.data_ptr(), a._version), b,
+                                lambda: bool(torch.equal(a, b)))
+            if same:
+                ptrs[d] = ptrs[0]
+    flags = L.TKBN_TABLES_CONJ_SYMMETRIC if all(_conj_symmetric(t) for t in keep) else 0
+    return L.ptr_array(ptrs), keep, flags
 
 
 _dtable_cache: "collections.OrderedDict" = collections.OrderedDict()
@@ -314,8 +355,8 @@ def interp_fwd(geom: GeomKey, lay: PointsLayout, tables, grid: torch.Tensor) -> 
     grid = grid.contiguous()
     B, C = grid.shape[:2]
     kdata = torch.empty((B, C, lay.npts), dtype=grid.dtype, device=dev)
-    tp, keep = table_ptrs(tables, grid.dtype)
-    L.check(L.lib().tkbn_interp_fwd(ctypes.byref(geom_struct(geom)), ctypes.byref(lay.desc),
+    tp, keep, fl = table_ptrs(tables, grid.dtype)
+    L.check(L.lib().tkbn_interp_fwd(ctypes.byref(geom_struct(geom, fl)), ctypes.byref(lay.desc),
                                     lay.workspace.data_ptr(), tp, grid.data_ptr(), B, C, kdata.data_ptr(),
                                     stream_handle(dev)))
     return kdata
@@ -327,8 +368,8 @@ def interp_adj(geom: GeomKey, lay: PointsLayout, tables, kdata: torch.Tensor) ->
     kdata = kdata.contiguous()
     B, C = kdata.shape[:2]
     grid = torch.empty((B, C) + geom.grid_size, dtype=kdata.dtype, device=dev)
-    tp, keep = table_ptrs(tables, kdata.dtype)
-    L.check(L.lib().tkbn_interp_adj(ctypes.byref(geom_struct(geom)), ctypes.byref(lay.desc),
+    tp, keep, fl = table_ptrs(tables, kdata.dtype)
+    L.check(L.lib().tkbn_interp_adj(ctypes.byref(geom_struct(geom, fl)), ctypes.byref(lay.desc),
                                     lay.workspace.data_ptr(), tp, kdata.data_ptr(), B, C, grid.data_ptr(),
                                     stream_handle(dev)))
     return grid
@@ -344,8 +385,8 @@ def interp_grad_omega(geom: GeomKey, lay: PointsLayout, tables, grid: torch.Tens
     grad = torch.empty((lay.ntraj, geom.ndim, lay.npts), dtype=rd, device=dev)
     tabs = [t.to(grid.dtype).contiguous() for t in tables]
     dtabs = derivative_tables(tabs, geom.table_oversamp)
-    tp, keep = table_ptrs(tabs, grid.dtype)
-    dp, keep2 = table_ptrs(dtabs, grid.dtype)
+    tp, keep, fl = table_ptrs(tabs, grid.dtype)
+    dp, keep2, _ = table_ptrs(dtabs, grid.dtype)
     L.check(L.lib().tkbn_interp_grad_omega(ctypes.byref(geom_struct(geom)), ctypes.byref(lay.desc),
                                            lay.workspace.data_ptr(), tp, dp, grid.data_ptr(), v.data_ptr(), B, C,
                                            grad.data_ptr(), stream_handle(dev)))
@@ -409,8 +450,8 @@ def nufft_fwd(geom: GeomKey, lay: PointsLayout, tables, scaling, image, smaps, n
     plan = fft_plan(geom, B, C, dev)
     grid = torch.empty((B, C) + geom.grid_size, dtype=image.dtype, device=dev)
     kdata = torch.empty((B, C, lay.npts), dtype=image.dtype, device=dev)
-    tp, keep = table_ptrs(tables, image.dtype)
-    L.check(L.lib().tkbn_nufft_fwd(ctypes.byref(geom_struct(geom)), ctypes.byref(lay.desc), lay.workspace.data_ptr(),
+    tp, keep, fl = table_ptrs(tables, image.dtype)
+    L.check(L.lib().tkbn_nufft_fwd(ctypes.byref(geom_struct(geom, fl)), ctypes.byref(lay.desc), lay.workspace.data_ptr(),
                                    plan.handle, tp, _c(scaling), image.data_ptr(), _c(smaps), sb, B, C,
                                    norm_code(norm), grid.data_ptr(), kdata.data_ptr(), stream_handle(dev)))
     return kdata
@@ -431,8 +472,8 @@ def nufft_adj(geom: GeomKey, lay: PointsLayout, tables, scaling, kdata, smaps, n
     grid = torch.empty((B, C) + geom.grid_size, dtype=kdata.dtype, device=dev)
     co = 1 if smaps is not None else C
     image = torch.empty((B, co) + geom.im_size, dtype=kdata.dtype, device=dev)
-    tp, keep = table_ptrs(tables, kdata.dtype)
-    L.check(L.lib().tkbn_nufft_adj(ctypes.byref(geom_struct(geom)), ctypes.byref(lay.desc), lay.workspace.data_ptr(),
+    tp, keep, fl = table_ptrs(tables, kdata.dtype)
+    L.check(L.lib().tkbn_nufft_adj(ctypes.byref(geom_struct(geom, fl)), ctypes.byref(lay.desc), lay.workspace.data_ptr(),
                                    plan.handle, tp, _c(scaling), kdata.data_ptr(), _c(smaps), sb, B, C,
                                    norm_code(norm), grid.data_ptr(), image.data_ptr(), stream_handle(dev)))
     return image

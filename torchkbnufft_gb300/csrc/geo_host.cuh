@@ -39,6 +39,7 @@ inline tkbn::Geo<R> make_geo(const tkbn_geometry* g, const PointsLayout* L, cons
     geo.Lr[d] = (R)geo.L[d];
     geo.nshift[d] = on ? (R)g->n_shift[d] : R(0);
     geo.tab[d] = (on && tables) ? (const tkbn::cplx<R>*)tables[d] : nullptr;
+    geo.half[d] = on && (g->flags & TKBN_TABLES_CONJ_SYMMETRIC) && (((int64_t)geo.J[d] * geo.L[d]) % 2 == 0);
     geo.dtab[d] = (on && dtables) ? (const tkbn::cplx<R>*)dtables[d] : nullptr;
   }
   return geo;

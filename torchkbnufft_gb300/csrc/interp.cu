@@ -88,6 +88,23 @@ __device__ __forceinline__ bool point_base(const Geo<R>& geo, const R* __restric
   return ok;
 }
 
+// point_base with tm already in registers.
+template <typename R, int D>
+__device__ __forceinline__ bool point_base_at(const Geo<R>& geo, const R* tmv, const int* origin, int* base,
+                                              int* local) {
+  bool ok = true;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const R f = floor(sub_rn(tmv[d], geo.halfJ[d]));
+    const bool fin = fabs(f) < R(1 << 30);
+    base[d] = fin ? 1 + (int)f : 0;
+    const int l = wrap_cell(base[d], geo.K[d]) - origin[d];
+    local[d] = l;
+    ok = ok && fin && (l >= 0) && (l < geo.T[d]);
+  }
+  return ok;
+}
+
 template <typename T, int D>
 __device__ __forceinline__ T sel(const T* v, int d) {
   return (D > 2 && d == 2) ? v[2 % D] : ((D > 1 && d == 1) ? v[1 % D] : v[0]);
@@ -108,7 +125,7 @@ __device__ __forceinline__ void table_factors(const Geo<R>& geo, const R* tmv, c
       if (j < J) {
         const int k = table_bin<R>(sel<R, D>(tmv, d), sel<int, D>(base, d) + j, sel<R, 3>(geo.Lr, d),
                                    sel<int, 3>(geo.center, d), sel<int, 3>(geo.tmax, d));
-        v = __ldg(&sel<const cplx<R>*, 3>(geo.tab, d)[k]);
+        v = table_entry<R>(sel<const cplx<R>*, 3>(geo.tab, d), k, sel<int, 3>(geo.center, d), sel<bool, 3>(geo.half, d));
       }
       scr[f] = v;
     }
@@ -125,7 +142,9 @@ __device__ __forceinline__ void table_factors(const Geo<R>& geo, const R* tmv, c
 #pragma unroll
       for (int j = 0; j < NJ; ++j) {
         h[d][j] = mk<R>(0, 0);
-        if (j < J) h[d][j] = __ldg(&geo.tab[d][table_bin<R>(tmv[d], base[d] + j, geo.Lr[d], geo.center[d], geo.tmax[d])]);
+        if (j < J)
+          h[d][j] = table_entry<R>(geo.tab[d], table_bin<R>(tmv[d], base[d] + j, geo.Lr[d], geo.center[d], geo.tmax[d]),
+                                   geo.center[d], geo.half[d]);
       }
     }
   }
@@ -359,20 +378,37 @@ __global__ void __launch_bounds__(kThreads) k_interp_fwd(Geo<R> geo, Launch a, c
     load_patch<R, D>(geo, grid, jc.b * a.C + jc.c0, a.gtot, jc.ncl, a.cells, a.ps, jc.origin, patch);
     __syncthreads();
     const int nrounds = (it.len + ppb - 1) / ppb;
+    // the next round's point data is loaded one round ahead (hides its latency)
+    int64_t i_next = it.start + min(warp * ppw + pslot, it.len - 1);
+    R tm_next[D];
+    int32_t val_next = a.vals[i_next];
+    cplx<R> ph_next = ph[i_next];
+#pragma unroll
+    for (int d = 0; d < D; ++d) tm_next[d] = tm[d * a.n + i_next];
     for (int r = 0; r < nrounds; ++r) {
       const int s = r * ppb + warp * ppw + pslot;
       const bool active = s < it.len;
-      const int64_t i = it.start + (active ? s : 0);
       R tmv[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) tmv[d] = tm_next[d];
+      const int32_t val = val_next;
+      const cplx<R> phv = ph_next;
+      if (r + 1 < nrounds) {
+        i_next = it.start + min(s + ppb, it.len - 1);
+        val_next = a.vals[i_next];
+        ph_next = ph[i_next];
+#pragma unroll
+        for (int d = 0; d < D; ++d) tm_next[d] = tm[d * a.n + i_next];
+      }
       int base[D], local[D];
-      const bool ok = point_base<R, D>(geo, tm, a.n, i, jc.origin, tmv, base, local);
+      const bool ok = point_base_at<R, D>(geo, tmv, jc.origin, base, local);
       cplx<R> h[D][NJ];
       table_factors<R, D, JC>(geo, tmv, base, c, a.Cc, coop, scr, h);
       if (active && c < jc.ncl) {
-        const int64_t m = a.vals[i] - jc.t * a.M;
+        const int64_t m = val - jc.t * a.M;
         cplx<R> y;
         if (ok) {
-          y = cmul<R>(gather_point<R, D, JC>(geo, h, local, patch + c * a.ps), ph[i]);
+          y = cmul<R>(gather_point<R, D, JC>(geo, h, local, patch + c * a.ps), phv);
         } else {
           y = mk<R>(R(NAN), R(NAN));
         }
@@ -577,7 +613,8 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
           const int base = 1 + (int)floor(sub_rn(tv, sel<R, 3>(geo.halfJ, d)));
           const int k = table_bin<R>(tv, base + j, sel<R, 3>(geo.Lr, d), sel<int, 3>(geo.center, d),
                                      sel<int, 3>(geo.tmax, d));
-          v = cconj<R>(__ldg(&sel<const cplx<R>*, 3>(geo.tab, d)[k]));
+          v = cconj<R>(table_entry<R>(sel<const cplx<R>*, 3>(geo.tab, d), k, sel<int, 3>(geo.center, d),
+                                      sel<bool, 3>(geo.half, d)));
         }
         sfac[e] = v;
       }
@@ -593,8 +630,38 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
         sv[e] = v;
       }
       __syncthreads();
-      // B: each warp applies the staged points to its rows
-      for (int p = 0; p < nv; ++p) {
+      // B: each warp applies the staged points that touch its rows. A ballot
+      // over the staged points (one lane per point) builds the warp's list.
+      unsigned touch[kNB / 32];
+#pragma unroll
+      for (int h = 0; h < kNB / 32; ++h) {
+        const int p = h * 32 + lane;
+        bool tch = false;
+        if (p < nv) {
+          const int* loc = sloc + p * D;
+          if (D == 1) {
+            tch = warp == 0;
+          } else if (D == 2) {
+            const int JY = JC > 0 ? JC : geo.J[0];
+            tch = max(0, r_lo - loc[0]) < min(JY, min(r_hi, ext[0]) - loc[0]);
+          } else {
+            const int JZ = JC > 0 ? JC : geo.J[0];
+            const int JY = JC > 0 ? JC : geo.J[1 % D];
+            const int T1 = geo.T[1 % D];
+            const int y0 = max(loc[1 % D], 0), y1 = min(loc[1 % D] + JY, ext[1 % D]);
+            for (int jz = 0; jz < JZ && !tch; ++jz) {
+              const int z = loc[0] + jz;
+              if (z < 0 || z >= ext[0] || y0 >= y1) continue;
+              tch = max(z * T1 + y0, r_lo) < min(z * T1 + y1, r_hi);
+            }
+          }
+        }
+        touch[h] = __ballot_sync(0xffffffffu, tch);
+      }
+#pragma unroll
+      for (int h = 0; h < kNB / 32; ++h)
+      for (unsigned msk = touch[h]; msk; msk &= msk - 1) {
+        const int p = h * 32 + __ffs(msk) - 1;
         const int* loc = sloc + p * D;
         const cplx<R>* fp = sfac + p * D * NJ;
         const cplx<R> v = sv[p * a.Cc + c];

@@ -111,6 +111,7 @@ struct Geo {
   R nshift[kMaxDim];
   const cplx<R>* tab[kMaxDim];
   const cplx<R>* dtab[kMaxDim];
+  bool half[kMaxDim];    // table read through its conjugate symmetry (J*L even)
 };
 
 // Work item of the sorted layout: points [start, start+len) of tile `key`.
@@ -188,6 +189,19 @@ __device__ __forceinline__ int table_bin(R tm, int g, R Lr, int center, int tmax
   R s = mul_rn(sub_rn(tm, (R)g), Lr);
   int k = (int)rint(s) + center;
   return min(max(k, 0), tmax);
+}
+
+// Table entry k. The tabulated kernel is KB(u) exp(-i r u) at u = k/L - J/2
+// with KB even, so entry center + d is the conjugate of entry center - d
+// (exactly, when J*L is even): only the first half of the table is read, which
+// halves its cache footprint. `half` selects this mode.
+template <typename R>
+__device__ __forceinline__ cplx<R> table_entry(const cplx<R>* __restrict__ tab, int k, int center, bool half) {
+  if (half && k > center) {
+    const cplx<R> v = __ldg(&tab[2 * center - k]);
+    return mk<R>(v.x, -v.y);
+  }
+  return __ldg(&tab[k]);
 }
 
 // fftshift phase argument sum_d omega_d * n_shift_d with each product rounded
