@@ -483,21 +483,72 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj(Geo<R> geo, Launch a, c
 constexpr int kNB = 64;
 
 struct OwnLaunch {
-  const int32_t* order;     // output tile keys, heaviest first
+  const Item* jobs;         // sub-jobs {tile key, first candidate, candidates, split}, longest first
+  const int64_t* hdr;       // hdr[1] = number of sub-jobs
   const int32_t* counts;    // points per key
   const int32_t* tile_off;  // first sorted point of each key
   const int32_t* vals;
   int64_t n, M, ntraj, B, C;
   int Cc, ncc;
   int64_t nbpt;
-  int64_t nkeys;  // ntraj * ntiles
-  int tcells;     // prod T
-  int aps;        // accumulator plane stride (complex elements)
+  int aps;  // accumulator plane stride (complex elements)
   int64_t gtot;
   SrcSpan span;
 };
 
-template <typename R, int D, int JC>
+template <typename R, int D>
+__device__ __forceinline__ void own_tile_geometry(const Geo<R>& geo, int key, int64_t* t, int* td, int* origin,
+                                                  int* ext) {
+  *t = key / geo.ntiles;
+  int rem = (int)(key - *t * geo.ntiles);
+#pragma unroll
+  for (int d = kMaxDim - 1; d >= 0; --d) {
+    td[d] = 0;
+    origin[d] = 0;
+    ext[d] = 1;
+    if (d < D) {
+      td[d] = rem % geo.ntile[d];
+      rem /= geo.ntile[d];
+      origin[d] = td[d] * geo.T[d];
+      ext[d] = min(geo.T[d], geo.K[d] - origin[d]);
+    }
+  }
+}
+
+// Zero the output tiles that are split over several sub-jobs (they are
+// accumulated with atomics); every plane of the batch items the tile serves.
+template <typename R, int D>
+__global__ void k_zero_split_tiles(Geo<R> geo, OwnLaunch a, cplx<R>* __restrict__ grid) {
+  const int64_t nsj = a.hdr[1];
+  for (int64_t j = blockIdx.x; j < nsj; j += gridDim.x) {
+    const Item it = a.jobs[j];
+    if (!(it.pad && it.start == 0)) continue;
+    int64_t t;
+    int td[kMaxDim], origin[kMaxDim], ext[kMaxDim];
+    own_tile_geometry<R, D>(geo, it.key, &t, td, origin, ext);
+    const int64_t b0 = a.ntraj == 1 ? 0 : t, b1 = a.ntraj == 1 ? a.B : t + 1;
+    int rows = 1;
+#pragma unroll
+    for (int d = 0; d < D - 1; ++d) rows *= ext[d];
+    const int64_t nrow = (b1 - b0) * a.C * rows;
+    for (int64_t r = threadIdx.x / 32; r < nrow; r += blockDim.x / 32) {
+      const int64_t plane = b0 * a.C + r / rows;
+      int rr = (int)(r % rows);
+      int64_t off = 0;
+      if (D == 2) off = (int64_t)(origin[0] + rr) * geo.K[1];
+      if (D == 3) {
+        const int y = rr % ext[1 % D], z = rr / ext[1 % D];
+        off = ((int64_t)(origin[0] + z) * geo.K[1 % D] + origin[1 % D] + y) * geo.K[2 % D];
+      }
+      cplx<R>* dst = grid + plane * a.gtot + off + origin[D - 1];
+      for (int x = threadIdx.x & 31; x < ext[D - 1]; x += 32) dst[x] = mk<R>(0, 0);
+    }
+  }
+}
+
+// FAST: D == 2, J == 6, Cc == 16 and 16-row tiles — each warp owns two rows,
+// lanes are (coil, row) and the six footprint columns are unrolled.
+template <typename R, int D, int JC, bool FAST>
 __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaunch a, const R* __restrict__ tm,
                                                              const cplx<R>* __restrict__ ph,
                                                              const cplx<R>* __restrict__ kdata,
@@ -515,39 +566,30 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
   int* snv = spre + MAXCOMBO + 1;                        // [2] valid count per staging warp
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t njobs = a.nkeys * a.nbpt * a.ncc;
+  const int64_t per_sj = a.nbpt * a.ncc;
+  const int64_t njobs = a.hdr[1] * per_sj;
   const int G = 32 / a.Cc;                       // lane groups per coil
-  const int c = lane % a.Cc, grp = lane / a.Cc;  // this lane's coil and x-group
+  const int c = lane % a.Cc, grp = lane / a.Cc;  // this lane's coil and group
   const int JX = JC > 0 ? JC : geo.J[D - 1];
-  const int cpg = (JX + G - 1) / G;              // footprint columns per group
-  // rows of the tile (outer coordinates) owned by this warp: [r_lo, r_hi)
+  const int cpg = (JX + G - 1) / G;              // footprint columns per group (generic path)
   int trows = 1;
 #pragma unroll
   for (int d = 0; d < D - 1; ++d) trows *= geo.T[d];
-  const int r_lo = (warp * trows) / kWarps, r_hi = ((warp + 1) * trows) / kWarps;
+  const int r_lo = FAST ? 2 * warp : (warp * trows) / kWarps;
+  const int r_hi = FAST ? 2 * warp + 2 : ((warp + 1) * trows) / kWarps;
   const int TX = geo.T[D - 1];
 
   for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x) {
-    const int64_t kidx = job % a.nkeys;
-    const int64_t rest = job / a.nkeys;
+    const Item it = a.jobs[job / per_sj];
+    const int64_t rest = job % per_sj;
     const int cc = (int)(rest % a.ncc);
     const int64_t bb = rest / a.ncc;
-    const int key = a.order[kidx];
-    const int64_t t = key / geo.ntiles;
+    int64_t t;
+    int td[kMaxDim], origin[kMaxDim], ext[kMaxDim];
+    own_tile_geometry<R, D>(geo, it.key, &t, td, origin, ext);
     const int64_t b = a.ntraj == 1 ? bb : t;
     const int c0 = cc * a.Cc;
     const int ncl = (int)min((int64_t)a.Cc, a.C - c0);
-    int td[kMaxDim] = {0, 0, 0}, origin[kMaxDim] = {0, 0, 0}, ext[kMaxDim] = {1, 1, 1};
-    {
-      int rem = (int)(key - t * geo.ntiles);
-#pragma unroll
-      for (int d = D - 1; d >= 0; --d) {
-        td[d] = rem % geo.ntile[d];
-        rem /= geo.ntile[d];
-        origin[d] = td[d] * geo.T[d];
-        ext[d] = min(geo.T[d], geo.K[d] - origin[d]);
-      }
-    }
     __syncthreads();  // previous job's write-out done with acc / lists
     if (threadIdx.x < a.span.ncombo) {
       const int skey = (int)(t * geo.ntiles) + source_tile(geo, a.span, td, threadIdx.x);
@@ -560,15 +602,15 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
     if (threadIdx.x == 0)
       for (int l = 0; l < a.span.ncombo; ++l) spre[l + 1] += spre[l];
     __syncthreads();
-    const int total = spre[a.span.ncombo];
+    const int qend = it.start + it.len;
 
-    for (int q0 = 0; q0 < total; q0 += kNB) {
+    for (int q0 = it.start; q0 < qend; q0 += kNB) {
       // A1: which candidates reach the tile; compact them (two staging warps)
       if (warp < kNB / 32) {
         const int q = q0 + threadIdx.x;
         bool valid = false;
         int i = 0, rel[kMaxDim] = {0, 0, 0};
-        if (q < total) {
+        if (q < qend) {
           int l = 0;
           while (spre[l + 1] <= q) ++l;
           i = slist[l] + (q - spre[l]);
@@ -589,7 +631,6 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
         const unsigned bal = __ballot_sync(0xffffffffu, valid);
         if (lane == 0) snv[warp] = __popc(bal);
         __syncwarp();
-        // positions: warp 0 first, then warp 1 (written after both counts are known)
         asm volatile("bar.sync 1, 64;");
         const int pos = (warp == 0 ? 0 : snv[0]) + __popc(bal & ((1u << lane) - 1));
         if (valid) {
@@ -630,7 +671,7 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
         sv[e] = v;
       }
       __syncthreads();
-      // B: each warp applies the staged points that touch its rows. A ballot
+      // B: each warp applies the staged points that touch its rows; a ballot
       // over the staged points (one lane per point) builds the warp's list.
       unsigned touch[kNB / 32];
 #pragma unroll
@@ -658,63 +699,84 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
         }
         touch[h] = __ballot_sync(0xffffffffu, tch);
       }
+      if (FAST) {
+        const int myrow = r_lo + grp;
+        const bool rowok = myrow < ext[0];
 #pragma unroll
-      for (int h = 0; h < kNB / 32; ++h)
-      for (unsigned msk = touch[h]; msk; msk &= msk - 1) {
-        const int p = h * 32 + __ffs(msk) - 1;
-        const int* loc = sloc + p * D;
-        const cplx<R>* fp = sfac + p * D * NJ;
-        const cplx<R> v = sv[p * a.Cc + c];
-        if (D == 1) {
-          if (warp == 0) {
-            for (int k = 0; k < cpg; ++k) {
-              const int jx = grp * cpg + k;
-              const int x = loc[0] + jx;
-              if (jx < JX && x >= 0 && x < ext[0]) {
-                cplx<R>* cell = acc + c * a.aps + x;
-                *cell = cfma<R>(v, fp[jx], *cell);
+        for (int h = 0; h < kNB / 32; ++h)
+          for (unsigned msk = touch[h]; msk; msk &= msk - 1) {
+            const int p = h * 32 + __ffs(msk) - 1;
+            const int ly = sloc[p * 2], lx = sloc[p * 2 + 1];
+            const int jy = myrow - ly;
+            if (rowok && (unsigned)jy < 6u) {
+              const cplx<R>* fp = sfac + p * 12;
+              const cplx<R> vy = cmul<R>(sv[p * 16 + c], fp[jy]);
+              cplx<R>* row = acc + c * a.aps + myrow * TX;
+#pragma unroll
+              for (int jx = 0; jx < 6; ++jx) {
+                const int x = lx + jx;
+                if ((unsigned)x < (unsigned)ext[1]) row[x] = cfma<R>(vy, fp[6 + jx], row[x]);
               }
             }
           }
-        } else if (D == 2) {
-          const int JY = JC > 0 ? JC : geo.J[0];
-          const int jlo = max(0, r_lo - loc[0]);
-          const int jhi = min(JY, min(r_hi, ext[0]) - loc[0]);
-          for (int jy = jlo; jy < jhi; ++jy) {
-            const cplx<R> vy = cmul<R>(v, fp[jy]);
-            cplx<R>* row = acc + c * a.aps + (loc[0] + jy) * TX;
-            for (int k = 0; k < cpg; ++k) {
-              const int jx = grp * cpg + k;
-              const int x = loc[1] + jx;
-              if (jx < JX && x >= 0 && x < ext[1]) row[x] = cfma<R>(vy, fp[NJ + jx], row[x]);
-            }
-          }
-        } else {
-          const int JZ = JC > 0 ? JC : geo.J[0];
-          const int JY = JC > 0 ? JC : geo.J[1 % D];
-          const int T1 = geo.T[1 % D];
-          for (int jz = 0; jz < JZ; ++jz) {
-            const int z = loc[0] + jz;
-            if (z < 0 || z >= ext[0]) continue;
-            const cplx<R> vz = cmul<R>(v, fp[jz]);
-            for (int jy = 0; jy < JY; ++jy) {
-              const int y = loc[1 % D] + jy;
-              const int rr = z * T1 + y;
-              if (y < 0 || y >= ext[1 % D] || rr < r_lo || rr >= r_hi) continue;
-              const cplx<R> vy = cmul<R>(vz, fp[NJ + jy]);
-              cplx<R>* row = acc + c * a.aps + rr * TX;
+      } else {
+#pragma unroll
+        for (int h = 0; h < kNB / 32; ++h)
+          for (unsigned msk = touch[h]; msk; msk &= msk - 1) {
+            const int p = h * 32 + __ffs(msk) - 1;
+            const int* loc = sloc + p * D;
+            const cplx<R>* fp = sfac + p * D * NJ;
+            const cplx<R> v = sv[p * a.Cc + c];
+            if (D == 1) {
               for (int k = 0; k < cpg; ++k) {
                 const int jx = grp * cpg + k;
-                const int x = loc[2 % D] + jx;
-                if (jx < JX && x >= 0 && x < ext[2 % D]) row[x] = cfma<R>(vy, fp[2 * NJ + jx], row[x]);
+                const int x = loc[0] + jx;
+                if (jx < JX && x >= 0 && x < ext[0]) {
+                  cplx<R>* cell = acc + c * a.aps + x;
+                  *cell = cfma<R>(v, fp[jx], *cell);
+                }
+              }
+            } else if (D == 2) {
+              const int JY = JC > 0 ? JC : geo.J[0];
+              const int jlo = max(0, r_lo - loc[0]);
+              const int jhi = min(JY, min(r_hi, ext[0]) - loc[0]);
+              for (int jy = jlo; jy < jhi; ++jy) {
+                const cplx<R> vy = cmul<R>(v, fp[jy]);
+                cplx<R>* row = acc + c * a.aps + (loc[0] + jy) * TX;
+                for (int k = 0; k < cpg; ++k) {
+                  const int jx = grp * cpg + k;
+                  const int x = loc[1] + jx;
+                  if (jx < JX && x >= 0 && x < ext[1]) row[x] = cfma<R>(vy, fp[NJ + jx], row[x]);
+                }
+              }
+            } else {
+              const int JZ = JC > 0 ? JC : geo.J[0];
+              const int JY = JC > 0 ? JC : geo.J[1 % D];
+              const int T1 = geo.T[1 % D];
+              for (int jz = 0; jz < JZ; ++jz) {
+                const int z = loc[0] + jz;
+                if (z < 0 || z >= ext[0]) continue;
+                const cplx<R> vz = cmul<R>(v, fp[jz]);
+                for (int jy = 0; jy < JY; ++jy) {
+                  const int y = loc[1 % D] + jy;
+                  const int rr = z * T1 + y;
+                  if (y < 0 || y >= ext[1 % D] || rr < r_lo || rr >= r_hi) continue;
+                  const cplx<R> vy = cmul<R>(vz, fp[NJ + jy]);
+                  cplx<R>* row = acc + c * a.aps + rr * TX;
+                  for (int k = 0; k < cpg; ++k) {
+                    const int jx = grp * cpg + k;
+                    const int x = loc[2 % D] + jx;
+                    if (jx < JX && x >= 0 && x < ext[2 % D]) row[x] = cfma<R>(vy, fp[2 * NJ + jx], row[x]);
+                  }
+                }
               }
             }
           }
-        }
       }
       __syncthreads();
     }
-    // C: write the tile (rows of TX cells, coalesced)
+    // C: write the tile (rows of TX cells, coalesced); split tiles add atomically
+    const bool split = it.pad != 0;
     for (int r = warp; r < ncl * trows; r += kWarps) {
       const int cl = r / trows;
       const int rr = r - cl * trows;
@@ -731,7 +793,11 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
       if (!inside) continue;
       cplx<R>* dst = grid + (b * a.C + c0 + cl) * a.gtot + off + origin[D - 1];
       const cplx<R>* src = acc + cl * a.aps + rr * TX;
-      for (int x = lane; x < ext[D - 1]; x += 32) dst[x] = src[x];
+      if (split) {
+        for (int x = lane; x < ext[D - 1]; x += 32) atomic_add_global(&dst[x], src[x]);
+      } else {
+        for (int x = lane; x < ext[D - 1]; x += 32) dst[x] = src[x];
+      }
     }
   }
 }
@@ -1069,7 +1135,8 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
                             cudaStream_t s) {
   constexpr int NJ = NJOf<JC>::N;
   OwnLaunch o;
-  o.order = (const int32_t*)(ws + ip.L.off_tile_order);
+  o.jobs = (const Item*)(ws + ip.L.off_adj_jobs);
+  o.hdr = ip.a.hdr;
   o.counts = (const int32_t*)(ws + ip.L.off_counts);
   o.tile_off = (const int32_t*)(ws + ip.L.off_tile_off);
   o.vals = ip.a.vals;
@@ -1081,18 +1148,26 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
   o.Cc = ip.a.Cc;
   o.ncc = ip.a.ncc;
   o.nbpt = ip.a.nbpt;
-  o.nkeys = ip.L.nkeys;
-  o.tcells = 1;
-  for (int d = 0; d < D; ++d) o.tcells *= ip.L.tile[d];
-  o.aps = o.tcells | 1;
+  int tcells = 1;
+  for (int d = 0; d < D; ++d) tcells *= ip.L.tile[d];
+  o.aps = tcells | 1;
   o.gtot = ip.a.gtot;
   o.span = ip.L.span;
   const size_t smem = (size_t)o.Cc * o.aps * sizeof(cplx<R>) + (size_t)kNB * D * NJ * sizeof(cplx<R>) +
                       (size_t)kNB * o.Cc * sizeof(cplx<R>) + sizeof(int) * ((size_t)kNB * D + kNB + 2 * max_combo<D>() + 3);
   if (smem > 220 * 1024) return set_error(TKBN_ERR_UNSUPPORTED, "adjoint tile needs %zu bytes of shared memory", smem);
-  auto k = k_interp_adj_own<R, D, JC>;
+  const int64_t max_jobs = ip.L.max_subjobs * o.nbpt * o.ncc;
+  // split tiles are accumulated atomically: zero them first
+  {
+    int64_t zb = ip.L.max_subjobs < 152 * 8 ? ip.L.max_subjobs : 152 * 8;
+    k_zero_split_tiles<R, D><<<(int)(zb < 1 ? 1 : zb), 256, 0, s>>>(geo, o, (cplx<R>*)grid);
+    int rc = check_cuda(cudaGetLastError(), "zero split tiles launch");
+    if (rc) return rc;
+  }
+  const bool fast = D == 2 && JC == 6 && o.Cc == 16 && ip.L.tile[0] == 2 * kWarps;
+  auto k = fast ? k_interp_adj_own<R, D, JC, true> : k_interp_adj_own<R, D, JC, false>;
   int blocks;
-  int rc = resident_blocks(k, smem, o.nkeys * o.nbpt * o.ncc, &blocks);
+  int rc = resident_blocks(k, smem, max_jobs, &blocks);
   if (rc) return rc;
   k<<<blocks, kThreads, smem, s>>>(geo, o, (const R*)(ws + ip.L.off_coords), (const cplx<R>*)(ws + ip.L.off_phase),
                                    (const cplx<R>*)kdata, (cplx<R>*)grid);

@@ -97,8 +97,8 @@ __global__ void k_gather_items(const Item* __restrict__ items, const int32_t* __
 // sort key is the bitwise complement, so an ascending sort puts the heaviest
 // tile first.
 template <typename R>
-__global__ void k_tile_work(Geo<R> geo, const int32_t* __restrict__ counts, int64_t nkeys, SrcSpan span,
-                            uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+__global__ void k_tile_work(Geo<R> geo, const int32_t* __restrict__ counts, int64_t nkeys, SrcSpan span, int W,
+                            int32_t* __restrict__ work, int32_t* __restrict__ nsub) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nkeys; k += (int64_t)gridDim.x * blockDim.x) {
     const int64_t t = k / geo.ntiles;
     int rem = (int)(k - t * geo.ntiles);
@@ -107,12 +107,39 @@ __global__ void k_tile_work(Geo<R> geo, const int32_t* __restrict__ counts, int6
       td[d] = rem % geo.ntile[d];
       rem /= geo.ntile[d];
     }
-    int64_t work = 0;
-    for (int combo = 0; combo < span.ncombo; ++combo) {
-      work += counts[t * geo.ntiles + source_tile(geo, span, td, combo)];
+    int64_t w = 0;
+    for (int combo = 0; combo < span.ncombo; ++combo) w += counts[t * geo.ntiles + source_tile(geo, span, td, combo)];
+    work[k] = (int32_t)w;
+    nsub[k] = w > W ? (int32_t)((w + W - 1) / W) : 1;
+  }
+}
+
+// Adjoint sub-jobs: candidates [start, start+len) of output tile `key`; pad = 1
+// when the tile is split over several sub-jobs (their results are added with
+// atomics into a pre-zeroed tile; unsplit tiles are written with plain stores).
+__global__ void k_fill_subjobs(const int32_t* __restrict__ work, const int32_t* __restrict__ nsub,
+                               const int32_t* __restrict__ suboff, int64_t nkeys, int W, Item* __restrict__ jobs,
+                               int64_t* __restrict__ hdr) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nkeys; k += (int64_t)gridDim.x * blockDim.x) {
+    const int ns = nsub[k];
+    for (int q = 0; q < ns; ++q) {
+      Item it;
+      it.key = (int)k;
+      it.start = q * W;
+      it.len = min(W, work[k] - q * W);
+      it.pad = ns > 1 ? 1 : 0;
+      jobs[suboff[k] + q] = it;
     }
-    keys[k] = ~(uint32_t)(work > 0x7fffffff ? 0x7fffffff : work);
-    vals[k] = (int32_t)k;
+    if (k == nkeys - 1) hdr[1] = (int64_t)suboff[k] + ns;
+  }
+}
+
+__global__ void k_subjob_keys(const Item* __restrict__ jobs, const int64_t* __restrict__ hdr, int64_t max_jobs, int W,
+                              uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+  const int64_t n = hdr[1];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < max_jobs; i += (int64_t)gridDim.x * blockDim.x) {
+    keys[i] = i < n ? (uint32_t)(W - jobs[i].len) : (uint32_t)(W + 1);
+    vals[i] = (int32_t)i;
   }
 }
 
@@ -168,8 +195,8 @@ void default_tiles(const tkbn_geometry* g, int tile[3], int* chunk) {
     // 14 x 16 cells: a 19 x 21 forward patch of 16 complex64 coil planes is
     // 51 KB, so four 256-thread CTAs fit an SM; 14 rows split evenly enough
     // over the 8 warps of the adjoint's row ownership.
-    tile[0] = 14;
-    tile[1] = 16;
+    tile[0] = 16;
+    tile[1] = 14;
   } else {
     tile[0] = tile[1] = tile[2] = 4;
   }
@@ -242,6 +269,16 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
     L->span.ncombo *= ns;
     if (g->grid_size[d] < (int64_t)T + g->numpoints[d] - 1) L->owned_ok = false;
   }
+  // adjoint sub-jobs: at most adj_chunk candidates each
+  L->adj_chunk = 1024;
+  L->max_subjobs = 2 * L->nkeys + (L->span.ncombo * L->npts_total + L->adj_chunk - 1) / L->adj_chunk;
+  int sbits = 1;
+  while (((int64_t)1 << sbits) <= L->adj_chunk + 1) ++sbits;
+  L->sj_key_bits = sbits;
+  size_t cub_ssort = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, cub_ssort, (uint32_t*)nullptr, (uint32_t*)nullptr, (int32_t*)nullptr,
+                                  (int32_t*)nullptr, (int)L->max_subjobs, 0, sbits);
+  if (cub_ssort > L->cub_bytes) L->cub_bytes = cub_ssort;
 
   size_t o = 0;
   L->off_hdr = o;
@@ -274,8 +311,24 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   o = align_up(o + 4 * L->max_items);
   L->off_ivals = o;
   o = align_up(o + 4 * L->max_items);
-  L->off_tile_order = o;
+  L->off_tile_work = o;
   o = align_up(o + 4 * L->nkeys);
+  L->off_tile_nsub = o;
+  o = align_up(o + 4 * L->nkeys);
+  L->off_tile_suboff = o;
+  o = align_up(o + 4 * (L->nkeys + 1));
+  L->off_sj_raw = o;
+  o = align_up(o + sizeof(tkbn::Item) * L->max_subjobs);
+  L->off_adj_jobs = o;
+  o = align_up(o + sizeof(tkbn::Item) * L->max_subjobs);
+  L->off_sj_keys_in = o;
+  o = align_up(o + 4 * L->max_subjobs);
+  L->off_sj_keys = o;
+  o = align_up(o + 4 * L->max_subjobs);
+  L->off_sj_vals_in = o;
+  o = align_up(o + 4 * L->max_subjobs);
+  L->off_sj_vals = o;
+  o = align_up(o + 4 * L->max_subjobs);
   L->off_coords = o;
   o = align_up(o + rsize * g->ndim * n);
   L->off_phase = o;
@@ -343,12 +396,30 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
                                       L.item_key_bits, s) != cudaSuccess)
     return set_error(TKBN_ERR_CUDA, "item sort failed");
   k_gather_items<<<blocks_for(L.max_items), threads, 0, s>>>(items_raw, ivals, L.max_items, items);
-  // adjoint tile order, heaviest first (reuses the item sort buffers; nkeys <= max_items)
-  k_tile_work<R><<<blocks_for(L.nkeys), threads, 0, s>>>(geo, counts, L.nkeys, L.span, ikeys_in, ivals_in);
-  tb = L.cub_bytes;
-  if (cub::DeviceRadixSort::SortPairs(cubtmp, tb, ikeys_in, ikeys, ivals_in, (int32_t*)(ws + L.off_tile_order),
-                                      (int)L.nkeys, 0, 32, s) != cudaSuccess)
-    return set_error(TKBN_ERR_CUDA, "tile sort failed");
+  // adjoint sub-jobs (output tiles, heavy ones split), longest first
+  {
+    int32_t* work = (int32_t*)(ws + L.off_tile_work);
+    int32_t* nsub = (int32_t*)(ws + L.off_tile_nsub);
+    int32_t* suboff = (int32_t*)(ws + L.off_tile_suboff);
+    Item* sj_raw = (Item*)(ws + L.off_sj_raw);
+    uint32_t* sk_in = (uint32_t*)(ws + L.off_sj_keys_in);
+    uint32_t* sk = (uint32_t*)(ws + L.off_sj_keys);
+    int32_t* sv_in = (int32_t*)(ws + L.off_sj_vals_in);
+    int32_t* sv = (int32_t*)(ws + L.off_sj_vals);
+    k_tile_work<R><<<blocks_for(L.nkeys), threads, 0, s>>>(geo, counts, L.nkeys, L.span, L.adj_chunk, work, nsub);
+    tb = L.cub_bytes;
+    if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, nsub, suboff, (int)L.nkeys, s) != cudaSuccess)
+      return set_error(TKBN_ERR_CUDA, "scan failed");
+    k_fill_subjobs<<<blocks_for(L.nkeys), threads, 0, s>>>(work, nsub, suboff, L.nkeys, L.adj_chunk, sj_raw, hdr);
+    k_subjob_keys<<<blocks_for(L.max_subjobs), threads, 0, s>>>(sj_raw, hdr, L.max_subjobs, L.adj_chunk, sk_in,
+                                                                 sv_in);
+    tb = L.cub_bytes;
+    if (cub::DeviceRadixSort::SortPairs(cubtmp, tb, sk_in, sk, sv_in, sv, (int)L.max_subjobs, 0, L.sj_key_bits, s) !=
+        cudaSuccess)
+      return set_error(TKBN_ERR_CUDA, "sub-job sort failed");
+    k_gather_items<<<blocks_for(L.max_subjobs), threads, 0, s>>>(sj_raw, sv, L.max_subjobs,
+                                                                  (Item*)(ws + L.off_adj_jobs));
+  }
   if (n > 0)
     k_sorted_points<R><<<blocks_for(n), threads, 0, s>>>(geo, (const R*)omega, vals, p->npts, n, coords,
                                                          (cplx<R>*)(ws + L.off_phase));

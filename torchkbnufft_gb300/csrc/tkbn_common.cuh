@@ -232,11 +232,15 @@ struct PointsLayout {
   int tile[3];
   int ntile[3];
   int chunk;
-  tkbn::SrcSpan span;  // source tiles of an output tile (adjoint)
-  bool owned_ok;       // every K_d >= T_d + J_d - 1: a footprint meets a tile in one contiguous run
+  tkbn::SrcSpan span;   // source tiles of an output tile (adjoint)
+  bool owned_ok;        // every K_d >= T_d + J_d - 1: a footprint meets a tile in one contiguous run
+  int adj_chunk;        // max candidates per adjoint sub-job
+  int64_t max_subjobs;  // upper bound on adjoint sub-jobs
+  int sj_key_bits;
   size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
-      off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_phase, off_tile_order,
-      off_cub;
+      off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_phase,
+      off_tile_work, off_tile_nsub, off_tile_suboff, off_sj_raw, off_adj_jobs, off_sj_keys_in, off_sj_keys,
+      off_sj_vals_in, off_sj_vals, off_cub;
   size_t cub_bytes;
   size_t total;
 };
