@@ -123,6 +123,18 @@ int tkbn_interp_grad_omega(const tkbn_geometry* g, const tkbn_points_desc* p, co
                            const void* const* tables, const void* const* dtables, const void* grid,
                            const void* v, int64_t nbatch, int64_t ncoil, void* grad_omega, void* stream);
 
+/* Forward interpolation that allocates no device memory (no counterpart in
+ * the reference). For callers that cannot allocate device memory after start
+ * (a fixed device-memory budget, or a plain-C host holding only raw pointers):
+ * the trajectory layout of omega (shared by all batch items, (d, npts)) is
+ * built in a library-owned array of TKBN_NOALLOC_SCRATCH_BYTES that each GPU
+ * holds until exit; larger trajectories are rejected with TKBN_ERR_INVALID.
+ * The first call on a device looks the array up (make it before any stream
+ * capture). All calls share the array: calls that overlap on the GPU race. */
+#define TKBN_NOALLOC_SCRATCH_BYTES ((size_t)8 << 20)
+int tkbn_interp_fwd_noalloc(const tkbn_geometry* g, const void* const* tables, const void* omega, int64_t npts,
+                            const void* grid, int64_t nbatch, int64_t ncoil, void* kdata, void* stream);
+
 /* ---- FFT stages --------------------------------------------------------- */
 /* cuFFT plan for nbatch*ncoil transforms of size grid_size (in place). */
 int tkbn_fft_plan_create(const tkbn_geometry* g, int64_t nbatch, int64_t ncoil, tkbn_fft_plan* plan);
