@@ -480,7 +480,7 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj(Geo<R> geo, Launch a, c
 // once with coalesced stores, so the grid needs no zeroing.
 // Requires K_d >= T_d + J_d - 1 (a footprint meets a tile in one run).
 
-constexpr int kNB = 64;
+constexpr int kNB = 96;  // staged points per batch (multiple of 32, <= kThreads)
 
 struct OwnLaunch {
   const Item* jobs;         // sub-jobs {tile key, first candidate, candidates, split}, longest first
@@ -563,7 +563,7 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
   int* spt = sloc + kNB * D;                             // [kNB] sorted point index
   int* slist = spt + kNB;                                // [MAXCOMBO] list starts
   int* spre = slist + MAXCOMBO;                          // [MAXCOMBO + 1] candidate prefix
-  int* snv = spre + MAXCOMBO + 1;                        // [2] valid count per staging warp
+  int* snv = spre + MAXCOMBO + 1;                        // [kNB/32] valid count per staging warp
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t per_sj = a.nbpt * a.ncc;
@@ -631,8 +631,10 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
         const unsigned bal = __ballot_sync(0xffffffffu, valid);
         if (lane == 0) snv[warp] = __popc(bal);
         __syncwarp();
-        asm volatile("bar.sync 1, 64;");
-        const int pos = (warp == 0 ? 0 : snv[0]) + __popc(bal & ((1u << lane) - 1));
+        // named barrier 1 over the kNB staging threads only
+        asm volatile("bar.sync 1, %0;" ::"r"(kNB));
+        int pos = __popc(bal & ((1u << lane) - 1));
+        for (int w = 0; w < warp; ++w) pos += snv[w];
         if (valid) {
           spt[pos] = i;
 #pragma unroll
@@ -640,24 +642,28 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
         }
       }
       __syncthreads();
-      const int nv = snv[0] + snv[1];
-      // A2: conjugated table factors and conj(phase) * kdata of the staged points
-      for (int e = threadIdx.x; e < nv * D * NJ; e += kThreads) {
-        const int p = e / (D * NJ);
-        const int f = e - p * (D * NJ);
-        const int d = f / NJ, j = f - d * NJ;
+      int nv = 0;
+#pragma unroll
+      for (int w = 0; w < kNB / 32; ++w) nv += snv[w];
+      // A2: conjugated table factors (one thread per point and dim) and
+      // conj(phase) * kdata of the staged points
+      for (int e = threadIdx.x; e < nv * D; e += kThreads) {
+        const int p = e / D;
+        const int d = e - p * D;
         const int J = JC > 0 ? JC : sel<int, 3>(geo.J, d);
-        cplx<R> v = mk<R>(0, 0);
-        if (j < J) {
-          const int i = spt[p];
-          const R tv = tm[d * a.n + i];
-          const int base = 1 + (int)floor(sub_rn(tv, sel<R, 3>(geo.halfJ, d)));
-          const int k = table_bin<R>(tv, base + j, sel<R, 3>(geo.Lr, d), sel<int, 3>(geo.center, d),
-                                     sel<int, 3>(geo.tmax, d));
-          v = cconj<R>(table_entry<R>(sel<const cplx<R>*, 3>(geo.tab, d), k, sel<int, 3>(geo.center, d),
-                                      sel<bool, 3>(geo.half, d)));
+        const R tv = tm[d * a.n + spt[p]];
+        const int base = 1 + (int)floor(sub_rn(tv, sel<R, 3>(geo.halfJ, d)));
+        const R Lr = sel<R, 3>(geo.Lr, d);
+        const int center = sel<int, 3>(geo.center, d), tmax = sel<int, 3>(geo.tmax, d);
+        const cplx<R>* tab = sel<const cplx<R>*, 3>(geo.tab, d);
+        const bool half = sel<bool, 3>(geo.half, d);
+        cplx<R>* out = sfac + e * NJ;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+          cplx<R> v = mk<R>(0, 0);
+          if (JC > 0 || j < J) v = cconj<R>(table_entry<R>(tab, table_bin<R>(tv, base + j, Lr, center, tmax), center, half));
+          out[j] = v;
         }
-        sfac[e] = v;
       }
       for (int e = threadIdx.x; e < nv * a.Cc; e += kThreads) {
         const int p = e / a.Cc;
@@ -711,11 +717,14 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
             if (rowok && (unsigned)jy < 6u) {
               const cplx<R>* fp = sfac + p * 12;
               const cplx<R> vy = cmul<R>(sv[p * 16 + c], fp[jy]);
-              cplx<R>* row = acc + c * a.aps + myrow * TX;
+              cplx<R>* row = acc + c * a.aps + myrow * TX + lx;
+              if (lx >= 0 && lx + 6 <= ext[1]) {  // footprint row fully inside the tile
 #pragma unroll
-              for (int jx = 0; jx < 6; ++jx) {
-                const int x = lx + jx;
-                if ((unsigned)x < (unsigned)ext[1]) row[x] = cfma<R>(vy, fp[6 + jx], row[x]);
+                for (int jx = 0; jx < 6; ++jx) row[jx] = cfma<R>(vy, fp[6 + jx], row[jx]);
+              } else {
+#pragma unroll
+                for (int jx = 0; jx < 6; ++jx)
+                  if ((unsigned)(lx + jx) < (unsigned)ext[1]) row[jx] = cfma<R>(vy, fp[6 + jx], row[jx]);
               }
             }
           }
@@ -1154,7 +1163,8 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
   o.gtot = ip.a.gtot;
   o.span = ip.L.span;
   const size_t smem = (size_t)o.Cc * o.aps * sizeof(cplx<R>) + (size_t)kNB * D * NJ * sizeof(cplx<R>) +
-                      (size_t)kNB * o.Cc * sizeof(cplx<R>) + sizeof(int) * ((size_t)kNB * D + kNB + 2 * max_combo<D>() + 3);
+                      (size_t)kNB * o.Cc * sizeof(cplx<R>) +
+                      sizeof(int) * ((size_t)kNB * D + kNB + 2 * max_combo<D>() + 1 + kNB / 32);
   if (smem > 220 * 1024) return set_error(TKBN_ERR_UNSUPPORTED, "adjoint tile needs %zu bytes of shared memory", smem);
   const int64_t max_jobs = ip.L.max_subjobs * o.nbpt * o.ncc;
   // split tiles are accumulated atomically: zero them first
