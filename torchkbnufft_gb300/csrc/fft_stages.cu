@@ -37,94 +37,148 @@ struct Shape {
   int64_t ntot, gtot;
 };
 
-// Grid element -> image flat index, or -1 when the element is padding.
-__device__ __forceinline__ int64_t grid_to_image(const Shape& s, int64_t g) {
-  int64_t nflat = 0, nstride = 1;
-  for (int d = s.ndim - 1; d >= 0; --d) {
-    const int64_t gd = g % s.K[d];
-    g /= s.K[d];
+// The elementwise stages work on "units": one chunk of up to kChunk elements
+// of one row along the last dim. Each unit decomposes its row index once, so
+// the per-element work is a load, a few complex multiplies and a store.
+constexpr int kChunk = 1024;
+constexpr int kStageThreads = 128;
+
+__host__ __device__ __forceinline__ int64_t chunks_of(int64_t n) { return (n + kChunk - 1) / kChunk; }
+
+// Row q (over the leading dims of the grid, row-major) -> image row index, or
+// -1 when the row lies in the zero padding.
+__device__ __forceinline__ int64_t grid_row_to_image_row(const Shape& s, int64_t q) {
+  int64_t nrow = 0, stride = 1;
+  for (int d = s.ndim - 2; d >= 0; --d) {
+    const int64_t gd = q % s.K[d];
+    q /= s.K[d];
     if (gd >= s.N[d]) return -1;
-    nflat += gd * nstride;
-    nstride *= s.N[d];
+    nrow += gd * stride;
+    stride *= s.N[d];
   }
-  return nflat;
+  return nrow;
 }
 
-// Image flat index -> grid flat index.
-__device__ __forceinline__ int64_t image_to_grid(const Shape& s, int64_t n) {
-  int64_t gflat = 0, gstride = 1;
-  for (int d = s.ndim - 1; d >= 0; --d) {
-    const int64_t nd = n % s.N[d];
-    n /= s.N[d];
-    gflat += nd * gstride;
-    gstride *= s.K[d];
+// Image row p (over the leading dims of the image) -> grid row index.
+__device__ __forceinline__ int64_t image_row_to_grid_row(const Shape& s, int64_t p) {
+  int64_t grow = 0, stride = 1;
+  for (int d = s.ndim - 2; d >= 0; --d) {
+    const int64_t nd = p % s.N[d];
+    p /= s.N[d];
+    grow += nd * stride;
+    stride *= s.K[d];
   }
-  return gflat;
+  return grow;
 }
 
-// K2. One thread per grid element of (B, C, K...). image has `ci` channels
+// K2. Units over the grid rows of (B, C, K...). image has `ci` channels
 // (1 with smaps, C without); smaps has `sb` batch entries (1 or B).
 template <typename R>
-__global__ void k_pad_scale(Shape s, int64_t B, int64_t C, int64_t ci, const cplx<R>* __restrict__ image,
-                            const cplx<R>* __restrict__ smaps, int64_t sb, const cplx<R>* __restrict__ scaling,
-                            R scale, cplx<R>* __restrict__ grid) {
-  const int64_t total = B * C * s.gtot;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t bc = e / s.gtot;
-    const int64_t g = e - bc * s.gtot;
-    const int64_t n = grid_to_image(s, g);
-    cplx<R> v = mk<R>(0, 0);
-    if (n >= 0) {
-      const int64_t b = bc / C, c = bc - (bc / C) * C;
-      v = image[(b * ci + (ci == 1 ? 0 : c)) * s.ntot + n];
-      if (smaps) v = cmul<R>(v, smaps[((sb == 1 ? 0 : b) * C + c) * s.ntot + n]);
-      if (scaling) v = cmul<R>(v, scaling[n]);
-      v = cscale<R>(v, scale);
+__global__ void __launch_bounds__(kStageThreads) k_pad_scale(Shape s, int64_t B, int64_t C, int64_t ci,
+                                                             const cplx<R>* __restrict__ image,
+                                                             const cplx<R>* __restrict__ smaps, int64_t sb,
+                                                             const cplx<R>* __restrict__ scaling, R scale,
+                                                             cplx<R>* __restrict__ grid) {
+  const int KX = s.K[s.ndim - 1], NX = s.N[s.ndim - 1];
+  const int64_t nchunk = chunks_of(KX);
+  const int64_t rows = s.gtot / KX;  // grid rows per (b, c) plane
+  const int64_t units = B * C * rows * nchunk;
+  for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const int64_t r = u / nchunk;
+    const int x0 = (int)(u - r * nchunk) * kChunk;
+    const int x1 = min(KX, x0 + kChunk);
+    const int64_t bc = r / rows;
+    const int64_t nrow = grid_row_to_image_row(s, r - bc * rows);
+    cplx<R>* out = grid + r * KX;
+    if (nrow < 0) {
+      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) out[x] = mk<R>(0, 0);
+      continue;
     }
-    grid[e] = v;
+    const int64_t b = bc / C, c = bc - b * C;
+    const int64_t n0 = nrow * NX;
+    const cplx<R>* im = image + (b * ci + (ci == 1 ? 0 : c)) * s.ntot + n0;
+    const cplx<R>* sm = smaps ? smaps + ((sb == 1 ? 0 : b) * C + c) * s.ntot + n0 : nullptr;
+    const cplx<R>* sc = scaling ? scaling + n0 : nullptr;
+    for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
+      cplx<R> v = mk<R>(0, 0);
+      if (x < NX) {
+        v = im[x];
+        if (sm) v = cmul<R>(v, sm[x]);
+        if (sc) v = cmul<R>(v, sc[x]);
+        v = cscale<R>(v, scale);
+      }
+      out[x] = v;
+    }
   }
 }
 
-// K5. One thread per output element: (B, 1, N...) with smaps, else (B, C, N...).
+// K5. Units over the output rows: (B, 1, N...) with smaps, else (B, C, N...).
+// A unit is kStageThreads elements of one row (one element per thread, so
+// that the coil sum of every element runs in its own thread).
 template <typename R>
-__global__ void k_crop_scale(Shape s, int64_t B, int64_t C, const cplx<R>* __restrict__ grid,
-                             const cplx<R>* __restrict__ smaps, int64_t sb, const cplx<R>* __restrict__ scaling,
-                             R scale, cplx<R>* __restrict__ out) {
+__global__ void __launch_bounds__(kStageThreads) k_crop_scale(Shape s, int64_t B, int64_t C,
+                                                              const cplx<R>* __restrict__ grid,
+                                                              const cplx<R>* __restrict__ smaps, int64_t sb,
+                                                              const cplx<R>* __restrict__ scaling, R scale,
+                                                              cplx<R>* __restrict__ out) {
+  const int KX = s.K[s.ndim - 1], NX = s.N[s.ndim - 1];
   const int64_t co = smaps ? 1 : C;
-  const int64_t total = B * co * s.ntot;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t bc = e / s.ntot;
-    const int64_t n = e - bc * s.ntot;
-    const int64_t g = image_to_grid(s, n);
-    cplx<R> sc = scaling ? cconj<R>(scaling[n]) : mk<R>(1, 0);
-    sc = cscale<R>(sc, scale);
+  const int64_t nchunk = (NX + kStageThreads - 1) / kStageThreads;
+  const int64_t rows = s.ntot / NX;  // image rows per plane
+  const int64_t units = B * co * rows * nchunk;
+  for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const int64_t r = u / nchunk;
+    const int x0 = (int)(u - r * nchunk) * kStageThreads;
+    const int x1 = min(NX, x0 + kStageThreads);
+    const int64_t bc = r / rows;
+    const int64_t p = r - bc * rows;
+    const int64_t n0 = p * NX;
+    const int64_t g0 = image_row_to_grid_row(s, p) * KX;
+    cplx<R>* o = out + r * NX;
     if (smaps) {
       const int64_t b = bc;
-      const cplx<R>* sm = smaps + (sb == 1 ? 0 : b) * C * s.ntot + n;
-      cplx<R> acc = mk<R>(0, 0);
-      for (int64_t c = 0; c < C; ++c) {
-        const cplx<R> v = cmul<R>(grid[(b * C + c) * s.gtot + g], sc);
-        acc = cfma<R>(v, cconj<R>(sm[c * s.ntot]), acc);
+      const cplx<R>* gb = grid + b * C * s.gtot + g0;
+      const cplx<R>* sm = smaps + (sb == 1 ? 0 : b) * C * s.ntot + n0;
+      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
+        cplx<R> sc = scaling ? cconj<R>(scaling[n0 + x]) : mk<R>(1, 0);
+        sc = cscale<R>(sc, scale);
+        cplx<R> acc = mk<R>(0, 0);
+#pragma unroll 4
+        for (int64_t c = 0; c < C; ++c) {
+          const cplx<R> v = cmul<R>(gb[c * s.gtot + x], sc);
+          acc = cfma<R>(v, cconj<R>(sm[c * s.ntot + x]), acc);
+        }
+        o[x] = acc;
       }
-      out[e] = acc;
     } else {
-      out[e] = cmul<R>(grid[bc * s.gtot + g], sc);
+      const cplx<R>* gp = grid + bc * s.gtot + g0;
+      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
+        cplx<R> sc = scaling ? cconj<R>(scaling[n0 + x]) : mk<R>(1, 0);
+        sc = cscale<R>(sc, scale);
+        o[x] = cmul<R>(gp[x], sc);
+      }
     }
   }
 }
 
 // K6. grid[b, c, g] *= kernel[k, g] * scale with k = 0 (shared kernel), b
 // (one kernel per batch item) or c (one kernel per channel: torch
-// broadcasting of a (K, *grid) kernel against (B, C, *grid)).
+// broadcasting of a (K, *grid) kernel against (B, C, *grid)). Units are
+// kChunk-element chunks of one (b, c) plane.
 template <typename R>
-__global__ void k_kernel_mul(int64_t gtot, int64_t B, int64_t C, const cplx<R>* __restrict__ kernel, int64_t kbatch,
-                             int by_channel, R scale, cplx<R>* __restrict__ grid) {
-  const int64_t total = B * C * gtot;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t bc = e / gtot;
-    const int64_t g = e - bc * gtot;
+__global__ void __launch_bounds__(kStageThreads) k_kernel_mul(int64_t gtot, int64_t B, int64_t C,
+                                                              const cplx<R>* __restrict__ kernel, int64_t kbatch,
+                                                              int by_channel, R scale, cplx<R>* __restrict__ grid) {
+  const int64_t nchunk = chunks_of(gtot);
+  const int64_t units = B * C * nchunk;
+  for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const int64_t bc = u / nchunk;
+    const int64_t g0 = (u - bc * nchunk) * kChunk;
+    const int n = (int)min((int64_t)kChunk, gtot - g0);
     const int64_t k = kbatch == 1 ? 0 : (by_channel ? bc % C : bc / C);
-    grid[e] = cscale<R>(cmul<R>(grid[e], kernel[k * gtot + g]), scale);
+    cplx<R>* gp = grid + bc * gtot + g0;
+    const cplx<R>* kp = kernel + k * gtot + g0;
+    for (int x = threadIdx.x; x < n; x += blockDim.x) gp[x] = cscale<R>(cmul<R>(gp[x], kp[x]), scale);
   }
 }
 
@@ -136,8 +190,10 @@ namespace tkbn_host {
 
 using namespace tkbn;
 
-static int grid_blocks(int64_t work) {
-  int64_t b = (work + 255) / 256;
+// Blocks for `units` work units: at most 16 resident 128-thread blocks on
+// each of the 152 SMs, the rest taken by the grid-stride loop.
+static int stage_blocks(int64_t units) {
+  int64_t b = units;
   if (b > 152 * 16) b = 152 * 16;
   if (b < 1) b = 1;
   return (int)b;
@@ -228,9 +284,10 @@ static double ortho_scale(const Shape& s, int norm) { return norm == TKBN_NORM_O
 template <typename R>
 static int pad_scale_r(const Shape& s, int64_t B, int64_t C, int64_t ci, const void* image, const void* smaps,
                        int64_t sb, const void* scaling, double scale, void* grid, cudaStream_t st) {
-  k_pad_scale<R><<<grid_blocks(B * C * s.gtot), 256, 0, st>>>(s, B, C, ci, (const cplx<R>*)image,
-                                                                (const cplx<R>*)smaps, sb, (const cplx<R>*)scaling,
-                                                                (R)scale, (cplx<R>*)grid);
+  const int64_t kx = s.K[s.ndim - 1];
+  const int blocks = stage_blocks(B * C * (s.gtot / kx) * chunks_of(kx));
+  k_pad_scale<R><<<blocks, kStageThreads, 0, st>>>(s, B, C, ci, (const cplx<R>*)image, (const cplx<R>*)smaps, sb,
+                                                   (const cplx<R>*)scaling, (R)scale, (cplx<R>*)grid);
   return check_cuda(cudaGetLastError(), "pad_scale launch");
 }
 
@@ -238,9 +295,10 @@ template <typename R>
 static int crop_scale_r(const Shape& s, int64_t B, int64_t C, const void* grid, const void* smaps, int64_t sb,
                         const void* scaling, double scale, void* out, cudaStream_t st) {
   const int64_t co = smaps ? 1 : C;
-  k_crop_scale<R><<<grid_blocks(B * co * s.ntot), 256, 0, st>>>(s, B, C, (const cplx<R>*)grid,
-                                                                  (const cplx<R>*)smaps, sb, (const cplx<R>*)scaling,
-                                                                  (R)scale, (cplx<R>*)out);
+  const int64_t nx = s.N[s.ndim - 1];
+  const int blocks = stage_blocks(B * co * (s.ntot / nx) * ((nx + kStageThreads - 1) / kStageThreads));
+  k_crop_scale<R><<<blocks, kStageThreads, 0, st>>>(s, B, C, (const cplx<R>*)grid, (const cplx<R>*)smaps, sb,
+                                                    (const cplx<R>*)scaling, (R)scale, (cplx<R>*)out);
   return check_cuda(cudaGetLastError(), "crop_scale launch");
 }
 
@@ -294,16 +352,16 @@ int toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, co
   if (g->dtype == TKBN_C64) {
     if ((rc = pad_scale_r<float>(s, B, C, ci, image, smaps, smaps_batch, nullptr, sc, grid, st))) return rc;
     if ((rc = fft_exec(plan, grid, CUFFT_FORWARD, st))) return rc;
-    k_kernel_mul<float><<<grid_blocks(B * C * s.gtot), 256, 0, st>>>(s.gtot, B, C, (const float2*)kernel, kbatch,
-                                                                       by_channel, (float)sc, (float2*)grid);
+    k_kernel_mul<float><<<stage_blocks(B * C * chunks_of(s.gtot)), kStageThreads, 0, st>>>(
+        s.gtot, B, C, (const float2*)kernel, kbatch, by_channel, (float)sc, (float2*)grid);
     if ((rc = check_cuda(cudaGetLastError(), "kernel_mul launch"))) return rc;
     if ((rc = fft_exec(plan, grid, CUFFT_INVERSE, st))) return rc;
     return crop_scale_r<float>(s, B, C, grid, smaps, smaps_batch, nullptr, 1.0, out, st);
   }
   if ((rc = pad_scale_r<double>(s, B, C, ci, image, smaps, smaps_batch, nullptr, sc, grid, st))) return rc;
   if ((rc = fft_exec(plan, grid, CUFFT_FORWARD, st))) return rc;
-  k_kernel_mul<double><<<grid_blocks(B * C * s.gtot), 256, 0, st>>>(s.gtot, B, C, (const double2*)kernel, kbatch,
-                                                                      by_channel, sc, (double2*)grid);
+  k_kernel_mul<double><<<stage_blocks(B * C * chunks_of(s.gtot)), kStageThreads, 0, st>>>(
+      s.gtot, B, C, (const double2*)kernel, kbatch, by_channel, sc, (double2*)grid);
   if ((rc = check_cuda(cudaGetLastError(), "kernel_mul launch"))) return rc;
   if ((rc = fft_exec(plan, grid, CUFFT_INVERSE, st))) return rc;
   return crop_scale_r<double>(s, B, C, grid, smaps, smaps_batch, nullptr, 1.0, out, st);

@@ -18,6 +18,8 @@
 // The separable sums group the products per dimension; the table bins, cell
 // indices and phase argument are computed exactly as the reference does.
 
+#include <type_traits>
+
 #include "geo_host.cuh"
 #include "tkbn_common.cuh"
 
@@ -494,6 +496,8 @@ struct OwnLaunch {
   int aps;  // accumulator plane stride (complex elements)
   int64_t gtot;
   SrcSpan span;
+  const int4* vlist;     // 2D: per-tile lists of the points that reach the tile (else null)
+  const int32_t* voff;   // first list entry of each tile key
 };
 
 template <typename R, int D>
@@ -518,10 +522,13 @@ __device__ __forceinline__ void own_tile_geometry(const Geo<R>& geo, int key, in
 // Zero the output tiles that are split over several sub-jobs (they are
 // accumulated with atomics); every plane of the batch items the tile serves.
 template <typename R, int D>
-__global__ void k_zero_split_tiles(Geo<R> geo, OwnLaunch a, cplx<R>* __restrict__ grid) {
+__global__ void k_zero_split_tiles(Geo<R> geo, OwnLaunch a, int W, cplx<R>* __restrict__ grid) {
   const int64_t nsj = a.hdr[1];
   for (int64_t j = blockIdx.x; j < nsj; j += gridDim.x) {
     const Item it = a.jobs[j];
+    // sub-jobs are sorted longest first and a split tile's first sub-job
+    // has the full length W: nothing after the first shorter job is one
+    if (it.len < W) break;
     if (!(it.pad && it.start == 0)) continue;
     int64_t t;
     int td[kMaxDim], origin[kMaxDim], ext[kMaxDim];
@@ -531,7 +538,8 @@ __global__ void k_zero_split_tiles(Geo<R> geo, OwnLaunch a, cplx<R>* __restrict_
 #pragma unroll
     for (int d = 0; d < D - 1; ++d) rows *= ext[d];
     const int64_t nrow = (b1 - b0) * a.C * rows;
-    for (int64_t r = threadIdx.x / 32; r < nrow; r += blockDim.x / 32) {
+    const int64_t wstride = (int64_t)gridDim.y * (blockDim.x / 32);
+    for (int64_t r = (int64_t)blockIdx.y * (blockDim.x / 32) + threadIdx.x / 32; r < nrow; r += wstride) {
       const int64_t plane = b0 * a.C + r / rows;
       int rr = (int)(r % rows);
       int64_t off = 0;
@@ -604,47 +612,60 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
     __syncthreads();
     const int qend = it.start + it.len;
 
+    const int64_t vbase = a.vlist ? (int64_t)a.voff[it.key] : 0;
     for (int q0 = it.start; q0 < qend; q0 += kNB) {
-      // A1: which candidates reach the tile; compact them (two staging warps)
-      if (warp < kNB / 32) {
-        const int q = q0 + threadIdx.x;
-        bool valid = false;
-        int i = 0, rel[kMaxDim] = {0, 0, 0};
-        if (q < qend) {
-          int l = 0;
-          while (spre[l + 1] <= q) ++l;
-          i = slist[l] + (q - spre[l]);
-          valid = true;
+      int nv = 0;
+      if (D == 2 && a.vlist) {
+        // A1 (2D): the tile's list holds only points that reach it
+        nv = min(kNB, qend - q0);
+        for (int e = threadIdx.x; e < nv; e += kThreads) {
+          const int4 ent = a.vlist[vbase + q0 + e];
+          spt[e] = ent.x;
+          sloc[e * D] = ent.z;
+          sloc[e * D + (D - 1)] = ent.w;
+        }
+        __syncthreads();
+      } else {
+        // A1: which candidates reach the tile; compact them (two staging warps)
+        if (warp < kNB / 32) {
+          const int q = q0 + threadIdx.x;
+          bool valid = false;
+          int i = 0, rel[kMaxDim] = {0, 0, 0};
+          if (q < qend) {
+            int l = 0;
+            while (spre[l + 1] <= q) ++l;
+            i = slist[l] + (q - spre[l]);
+            valid = true;
 #pragma unroll
-          for (int d = 0; d < D; ++d) {
-            const R tv = tm[d * a.n + i];
-            const R f = floor(sub_rn(tv, geo.halfJ[d]));
-            const bool fin = fabs(f) < R(1 << 30);
-            const int w = fin ? wrap_cell(1 + (int)f, geo.K[d]) : 0;
-            int r = w - origin[d];
-            if (r >= geo.T[d]) r -= geo.K[d];
-            const int J = JC > 0 ? JC : geo.J[d];
-            valid = valid && fin && (r > -J) && (r < ext[d]);
-            rel[d] = r;
+            for (int d = 0; d < D; ++d) {
+              const R tv = tm[d * a.n + i];
+              const R f = floor(sub_rn(tv, geo.halfJ[d]));
+              const bool fin = fabs(f) < R(1 << 30);
+              const int w = fin ? wrap_cell(1 + (int)f, geo.K[d]) : 0;
+              int r = w - origin[d];
+              if (r >= geo.T[d]) r -= geo.K[d];
+              const int J = JC > 0 ? JC : geo.J[d];
+              valid = valid && fin && (r > -J) && (r < ext[d]);
+              rel[d] = r;
+            }
+          }
+          const unsigned bal = __ballot_sync(0xffffffffu, valid);
+          if (lane == 0) snv[warp] = __popc(bal);
+          __syncwarp();
+          // named barrier 1 over the kNB staging threads only
+          asm volatile("bar.sync 1, %0;" ::"r"(kNB));
+          int pos = __popc(bal & ((1u << lane) - 1));
+          for (int w = 0; w < warp; ++w) pos += snv[w];
+          if (valid) {
+            spt[pos] = i;
+#pragma unroll
+            for (int d = 0; d < D; ++d) sloc[pos * D + d] = rel[d];
           }
         }
-        const unsigned bal = __ballot_sync(0xffffffffu, valid);
-        if (lane == 0) snv[warp] = __popc(bal);
-        __syncwarp();
-        // named barrier 1 over the kNB staging threads only
-        asm volatile("bar.sync 1, %0;" ::"r"(kNB));
-        int pos = __popc(bal & ((1u << lane) - 1));
-        for (int w = 0; w < warp; ++w) pos += snv[w];
-        if (valid) {
-          spt[pos] = i;
+        __syncthreads();
 #pragma unroll
-          for (int d = 0; d < D; ++d) sloc[pos * D + d] = rel[d];
-        }
+        for (int w = 0; w < kNB / 32; ++w) nv += snv[w];
       }
-      __syncthreads();
-      int nv = 0;
-#pragma unroll
-      for (int w = 0; w < kNB / 32; ++w) nv += snv[w];
       // A2: conjugated table factors (one thread per point and dim) and
       // conj(phase) * kdata of the staged points
       for (int e = threadIdx.x; e < nv * D; e += kThreads) {
@@ -813,6 +834,164 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
 
 // Smooth table lookup for the gradient: linear interpolation of value and
 // derivative tables at the exact (unrounded) position.
+// K4 (owned tiles, registers): the common 2D case — J = 6 in both dims,
+// 16 coils per job, 16 x 14 tiles, complex64. Lane (coil c, row 2*warp + g)
+// keeps the 14 cells of its row of its coil plane in registers. A staged
+// point's column offset within the tile is the same for every lane of the
+// warp, so a switch on it selects fully unrolled code with static register
+// indices; accumulation needs no shared-memory read-modify-write. Points are
+// staged 256 at a time (every thread stages one candidate), two barriers per
+// batch. Cells outside the tile (edge tiles narrower than 14) accumulate
+// contributions that are never written; those cells belong to the wrapped
+// tile, which gets the same points with its own column offsets.
+constexpr int kNBR = 256;  // staged points per batch (== kThreads)
+constexpr int kRegTileY = 16, kRegTileX = 14, kRegCoils = 16;
+
+template <int LX>
+__device__ __forceinline__ void reg_add_cols(float2 (&racc)[kRegTileX], float2 vy, const float2 (&fx)[6]) {
+#pragma unroll
+  for (int jx = 0; jx < 6; ++jx)
+    if (LX + jx >= 0 && LX + jx < kRegTileX) racc[LX + jx] = cfma<float>(vy, fx[jx], racc[LX + jx]);
+}
+
+__device__ __forceinline__ void reg_add_point(int lx, float2 (&racc)[kRegTileX], float2 vy, const float2 (&fx)[6]) {
+  switch (lx) {
+#define TKBN_REG_CASE(L) \
+  case L:                \
+    reg_add_cols<L>(racc, vy, fx); \
+    break;
+    TKBN_REG_CASE(-5) TKBN_REG_CASE(-4) TKBN_REG_CASE(-3) TKBN_REG_CASE(-2) TKBN_REG_CASE(-1)
+    TKBN_REG_CASE(0) TKBN_REG_CASE(1) TKBN_REG_CASE(2) TKBN_REG_CASE(3) TKBN_REG_CASE(4) TKBN_REG_CASE(5)
+    TKBN_REG_CASE(6) TKBN_REG_CASE(7) TKBN_REG_CASE(8) TKBN_REG_CASE(9) TKBN_REG_CASE(10) TKBN_REG_CASE(11)
+    TKBN_REG_CASE(12) TKBN_REG_CASE(13)
+#undef TKBN_REG_CASE
+    default:
+      break;
+  }
+}
+
+// vec_ok: the grid pointer is 16-byte aligned and K1 is even, so every
+// tile row starts 16-byte aligned and pairs of cells go out as one float4.
+__global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg(Geo<float> geo, OwnLaunch a,
+                                                                const float* __restrict__ tm,
+                                                                const float2* __restrict__ ph,
+                                                                const float2* __restrict__ kdata,
+                                                                float2* __restrict__ grid, int vec_ok) {
+  constexpr int D = 2, NJ = 6;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* sfac = reinterpret_cast<float2*>(smem_raw);  // [kNBR][12]: conj y factors, conj x factors
+  float2* sv = sfac + kNBR * D * NJ;                   // [kNBR][16] conj(phase) * kdata per coil
+  int2* sloc = reinterpret_cast<int2*>(sv + kNBR * kRegCoils);  // [kNBR] footprint start (y, x) in the tile
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int c = lane & 15, myrow = 2 * warp + (lane >> 4);
+  const int64_t per_sj = a.nbpt * a.ncc;
+  const int64_t njobs = a.hdr[1] * per_sj;
+
+  for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x) {
+    const Item it = a.jobs[job / per_sj];
+    const int64_t rest = job % per_sj;
+    const int cc = (int)(rest % a.ncc);
+    const int64_t bb = rest / a.ncc;
+    int64_t t;
+    int td[kMaxDim], origin[kMaxDim], ext[kMaxDim];
+    own_tile_geometry<float, D>(geo, it.key, &t, td, origin, ext);
+    const int64_t b = a.ntraj == 1 ? bb : t;
+    const int c0 = cc * kRegCoils;
+    const int ncl = (int)min((int64_t)kRegCoils, a.C - c0);
+    const bool rowok = myrow < ext[0];
+    const int64_t vbase = a.voff[it.key];
+    float2 racc[kRegTileX];
+#pragma unroll
+    for (int x = 0; x < kRegTileX; ++x) racc[x] = make_float2(0.f, 0.f);
+    const int qend = it.start + it.len;
+    // The staging buffers are free here: the previous batch ended with a barrier.
+    for (int q0 = it.start; q0 < qend; q0 += kNBR) {
+      const int nv = min(kNBR, qend - q0);
+      const int4* ents = a.vlist + vbase + q0;
+      // A: conjugated table factors and footprint offsets (one thread per
+      // point and dim); conj(phase) * kdata (one thread per point and coil)
+      for (int e = threadIdx.x; e < nv * D; e += kThreads) {
+        const int pt = e >> 1, d = e & 1;
+        const int4 ent = ents[pt];
+        if (d == 0) sloc[pt] = make_int2(ent.z, ent.w);
+        const float tv = tm[d * a.n + ent.x];
+        const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
+        const float Lr = sel<float, D>(geo.Lr, d);
+        const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
+        const float2* tab = sel<const float2*, D>(geo.tab, d);
+        const bool half = sel<bool, D>(geo.half, d);
+        float2* out = sfac + e * NJ;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j)
+          out[j] = cconj<float>(table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half));
+      }
+#pragma unroll 4
+      for (int e = threadIdx.x; e < nv * kRegCoils; e += kThreads) {
+        const int pt = e >> 4, cl = e & 15;
+        float2 v = make_float2(0.f, 0.f);
+        if (cl < ncl) {
+          const int4 ent = ents[pt];
+          v = cmulc<float>(kdata[(b * a.C + c0 + cl) * a.M + ent.y], ph[ent.x]);
+        }
+        sv[e] = v;
+      }
+      __syncthreads();
+      // B: each warp applies the staged points that touch its two rows
+      const int r_lo = 2 * warp, r_hi = min(2 * warp + 2, ext[0]);
+#pragma unroll 1
+      for (int h = 0; h < kNBR / 32; ++h) {
+        const int p = h * 32 + lane;
+        bool tch = false;
+        if (p < nv) {
+          const int ly = sloc[p].x;
+          tch = max(r_lo, ly) < min(r_hi, ly + NJ);
+        }
+        for (unsigned msk = __ballot_sync(0xffffffffu, tch); msk; msk &= msk - 1) {
+          const int pt = h * 32 + __ffs(msk) - 1;
+          const int2 loc = sloc[pt];
+          const int jy = myrow - loc.x;
+          if (rowok && (unsigned)jy < (unsigned)NJ) {
+            const float2* fp = sfac + pt * (D * NJ);
+            const float2 vy = cmul<float>(sv[pt * kRegCoils + c], fp[jy]);
+            const float4* fx4 = reinterpret_cast<const float4*>(fp + NJ);
+            const float4 f01 = fx4[0], f23 = fx4[1], f45 = fx4[2];
+            const float2 fx[6] = {make_float2(f01.x, f01.y), make_float2(f01.z, f01.w), make_float2(f23.x, f23.y),
+                                  make_float2(f23.z, f23.w), make_float2(f45.x, f45.y), make_float2(f45.z, f45.w)};
+            reg_add_point(loc.y, racc, vy, fx);
+          }
+        }
+        if ((h + 1) * 32 >= nv) break;
+      }
+      __syncthreads();
+    }
+    // C: write this lane's row of its coil plane; split tiles add atomically
+    if (rowok && c < ncl) {
+      float2* dst = grid + (b * a.C + c0 + c) * a.gtot + (int64_t)(origin[0] + myrow) * geo.K[1] + origin[1];
+      const int ex = ext[1];
+      if (it.pad == 0) {
+        if (vec_ok) {
+#pragma unroll
+          for (int x = 0; x < kRegTileX; x += 2) {
+            if (x + 1 < ex)
+              *reinterpret_cast<float4*>(dst + x) = make_float4(racc[x].x, racc[x].y, racc[x + 1].x, racc[x + 1].y);
+            else if (x < ex)
+              dst[x] = racc[x];
+          }
+        } else {
+#pragma unroll
+          for (int x = 0; x < kRegTileX; ++x)
+            if (x < ex) dst[x] = racc[x];
+        }
+      } else {
+#pragma unroll
+        for (int x = 0; x < kRegTileX; ++x)
+          if (x < ex) atomic_add_global(dst + x, racc[x]);
+      }
+    }
+  }
+}
+
 template <typename R>
 __device__ __forceinline__ void lerp_tables(const Geo<R>& geo, int d, R tm, int g, cplx<R>* val, cplx<R>* der) {
   const R s = (tm - (R)g) * geo.Lr[d] + (R)geo.center[d];
@@ -1162,17 +1341,35 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
   o.aps = tcells | 1;
   o.gtot = ip.a.gtot;
   o.span = ip.L.span;
+  o.vlist = ip.L.vlist ? (const int4*)(ws + ip.L.off_vlist) : nullptr;
+  o.voff = ip.L.vlist ? (const int32_t*)(ws + ip.L.off_voff) : nullptr;
   const size_t smem = (size_t)o.Cc * o.aps * sizeof(cplx<R>) + (size_t)kNB * D * NJ * sizeof(cplx<R>) +
                       (size_t)kNB * o.Cc * sizeof(cplx<R>) +
                       sizeof(int) * ((size_t)kNB * D + kNB + 2 * max_combo<D>() + 1 + kNB / 32);
   if (smem > 220 * 1024) return set_error(TKBN_ERR_UNSUPPORTED, "adjoint tile needs %zu bytes of shared memory", smem);
   const int64_t max_jobs = ip.L.max_subjobs * o.nbpt * o.ncc;
-  // split tiles are accumulated atomically: zero them first
+  // split tiles are accumulated atomically: zero them first. Blocks
+  // (x, y) take the split tiles x, x + gridDim.x, ... and within each the
+  // rows y*8 + warp, strided by 8*gridDim.y.
   {
-    int64_t zb = ip.L.max_subjobs < 152 * 8 ? ip.L.max_subjobs : 152 * 8;
-    k_zero_split_tiles<R, D><<<(int)(zb < 1 ? 1 : zb), 256, 0, s>>>(geo, o, (cplx<R>*)grid);
+    const int64_t zx = ip.L.max_subjobs < 152 ? ip.L.max_subjobs : 152;
+    k_zero_split_tiles<R, D><<<dim3((unsigned)(zx < 1 ? 1 : zx), 16), 256, 0, s>>>(geo, o, ip.L.adj_chunk,
+                                                                                  (cplx<R>*)grid);
     int rc = check_cuda(cudaGetLastError(), "zero split tiles launch");
     if (rc) return rc;
+  }
+  if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
+    if (o.vlist && o.Cc == kRegCoils && ip.L.tile[0] == kRegTileY && ip.L.tile[1] == kRegTileX) {
+      const size_t rsmem = (size_t)kNBR * (D * 6 + kRegCoils) * sizeof(float2) + (size_t)kNBR * sizeof(int2);
+      int blocks;
+      int rc = resident_blocks(k_interp_adj_reg, rsmem, max_jobs, &blocks);
+      if (rc) return rc;
+      const int vec_ok = ((uintptr_t)grid % 16 == 0) && (geo.K[1] % 2 == 0);
+      k_interp_adj_reg<<<blocks, kThreads, rsmem, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
+                                                       (const float2*)(ws + ip.L.off_phase), (const float2*)kdata,
+                                                       (float2*)grid, vec_ok);
+      return check_cuda(cudaGetLastError(), "interp_adj launch");
+    }
   }
   const bool fast = D == 2 && JC == 6 && o.Cc == 16 && ip.L.tile[0] == 2 * kWarps;
   auto k = fast ? k_interp_adj_own<R, D, JC, true> : k_interp_adj_own<R, D, JC, false>;

@@ -97,20 +97,83 @@ __global__ void k_gather_items(const Item* __restrict__ items, const int32_t* __
 // sort key is the bitwise complement, so an ascending sort puts the heaviest
 // tile first.
 template <typename R>
-__global__ void k_tile_work(Geo<R> geo, const int32_t* __restrict__ counts, int64_t nkeys, SrcSpan span, int W,
-                            int32_t* __restrict__ work, int32_t* __restrict__ nsub) {
+__global__ void k_tile_work(Geo<R> geo, const int32_t* __restrict__ counts, const int32_t* __restrict__ vcount,
+                            int64_t nkeys, SrcSpan span, int W, int32_t* __restrict__ work,
+                            int32_t* __restrict__ nsub) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nkeys; k += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t t = k / geo.ntiles;
-    int rem = (int)(k - t * geo.ntiles);
-    int td[kMaxDim] = {0, 0, 0};
-    for (int d = geo.ndim - 1; d >= 0; --d) {
-      td[d] = rem % geo.ntile[d];
-      rem /= geo.ntile[d];
-    }
     int64_t w = 0;
-    for (int combo = 0; combo < span.ncombo; ++combo) w += counts[t * geo.ntiles + source_tile(geo, span, td, combo)];
+    if (vcount) {
+      w = vcount[k];
+    } else {
+      const int64_t t = k / geo.ntiles;
+      int rem = (int)(k - t * geo.ntiles);
+      int td[kMaxDim] = {0, 0, 0};
+      for (int d = geo.ndim - 1; d >= 0; --d) {
+        td[d] = rem % geo.ntile[d];
+        rem /= geo.ntile[d];
+      }
+      for (int combo = 0; combo < span.ncombo; ++combo) w += counts[t * geo.ntiles + source_tile(geo, span, td, combo)];
+    }
     work[k] = (int32_t)w;
     nsub[k] = w > W ? (int32_t)((w + W - 1) / W) : 1;
+  }
+}
+
+// 2D owned tiles: one warp per output tile walks the points of its source
+// tiles (in source-tile order, then sorted order — the order the adjoint
+// accumulates them in) and keeps those whose footprint reaches the tile,
+// with the footprint's first row and column relative to the tile origin
+// (negative when the footprint starts in an earlier tile; periodic). The
+// first pass (voff == nullptr) counts, the second writes at voff[key].
+template <typename R>
+__global__ void k_tile_valid(Geo<R> geo, const int32_t* __restrict__ counts, const int32_t* __restrict__ tile_off,
+                             const R* __restrict__ tm, const int32_t* __restrict__ vals, int64_t n, int64_t M,
+                             int64_t nkeys, SrcSpan span, const int32_t* __restrict__ voff,
+                             int32_t* __restrict__ vcount, int4* __restrict__ vlist) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x / 32);
+  for (int64_t key = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; key < nkeys; key += nwarps) {
+    const int64_t t = key / geo.ntiles;
+    const int rem = (int)(key - t * geo.ntiles);
+    int td[kMaxDim] = {rem / geo.ntile[1], rem % geo.ntile[1], 0};
+    int origin[2], ext[2];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      origin[d] = td[d] * geo.T[d];
+      ext[d] = min(geo.T[d], geo.K[d] - origin[d]);
+    }
+    const int64_t out0 = voff ? voff[key] : 0;
+    int cnt = 0;
+    for (int combo = 0; combo < span.ncombo; ++combo) {
+      const int64_t skey = t * geo.ntiles + source_tile(geo, span, td, combo);
+      const int start = tile_off[skey], num = counts[skey];
+      for (int q0 = 0; q0 < num; q0 += 32) {
+        const int q = q0 + lane;
+        bool valid = false;
+        int r[2] = {0, 0};
+        int i = 0;
+        if (q < num) {
+          i = start + q;
+          valid = true;
+#pragma unroll
+          for (int d = 0; d < 2; ++d) {
+            const R f = floor(sub_rn(tm[d * n + i], geo.halfJ[d]));
+            const bool fin = fabs(f) < R(1 << 30);
+            const int w = fin ? wrap_cell(1 + (int)f, geo.K[d]) : 0;
+            int rr = w - origin[d];
+            if (rr >= geo.T[d]) rr -= geo.K[d];
+            valid = valid && fin && (rr > -geo.J[d]) && (rr < ext[d]);
+            r[d] = rr;
+          }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, valid);
+        if (voff && valid)
+          vlist[out0 + cnt + __popc(bal & lt_mask)] = make_int4(i, (int)(vals[i] - t * M), r[0], r[1]);
+        cnt += __popc(bal);
+      }
+    }
+    if (!voff && lane == 0) vcount[key] = cnt;
   }
 }
 
@@ -269,8 +332,10 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
     L->span.ncombo *= ns;
     if (g->grid_size[d] < (int64_t)T + g->numpoints[d] - 1) L->owned_ok = false;
   }
-  // adjoint sub-jobs: at most adj_chunk candidates each
+  // adjoint sub-jobs: at most adj_chunk candidates (list entries in 2D) each
   L->adj_chunk = 1024;
+  L->vlist = g->ndim == 2 && L->owned_ok;
+  L->max_valid = L->vlist ? L->span.ncombo * L->npts_total : 0;
   L->max_subjobs = 2 * L->nkeys + (L->span.ncombo * L->npts_total + L->adj_chunk - 1) / L->adj_chunk;
   int sbits = 1;
   while (((int64_t)1 << sbits) <= L->adj_chunk + 1) ++sbits;
@@ -329,6 +394,12 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   o = align_up(o + 4 * L->max_subjobs);
   L->off_sj_vals = o;
   o = align_up(o + 4 * L->max_subjobs);
+  L->off_vcount = o;
+  o = align_up(o + (L->vlist ? 4 * L->nkeys : 0));
+  L->off_voff = o;
+  o = align_up(o + (L->vlist ? 4 * (L->nkeys + 1) : 0));
+  L->off_vlist = o;
+  o = align_up(o + sizeof(int4) * L->max_valid);
   L->off_coords = o;
   o = align_up(o + rsize * g->ndim * n);
   L->off_phase = o;
@@ -396,6 +467,24 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
                                       L.item_key_bits, s) != cudaSuccess)
     return set_error(TKBN_ERR_CUDA, "item sort failed");
   k_gather_items<<<blocks_for(L.max_items), threads, 0, s>>>(items_raw, ivals, L.max_items, items);
+  if (n > 0)
+    k_sorted_points<R><<<blocks_for(n), threads, 0, s>>>(geo, (const R*)omega, vals, p->npts, n, coords,
+                                                         (cplx<R>*)(ws + L.off_phase));
+  // 2D: per output tile, the points that reach it
+  int32_t* vcount = nullptr;
+  if (L.vlist) {
+    vcount = (int32_t*)(ws + L.off_vcount);
+    int32_t* voff = (int32_t*)(ws + L.off_voff);
+    int4* vlist = (int4*)(ws + L.off_vlist);
+    const int wblocks = blocks_for(L.nkeys * 32);
+    k_tile_valid<R><<<wblocks, threads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys, L.span,
+                                                nullptr, vcount, vlist);
+    tb = L.cub_bytes;
+    if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, vcount, voff, (int)L.nkeys, s) != cudaSuccess)
+      return set_error(TKBN_ERR_CUDA, "scan failed");
+    k_tile_valid<R><<<wblocks, threads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys, L.span,
+                                                voff, vcount, vlist);
+  }
   // adjoint sub-jobs (output tiles, heavy ones split), longest first
   {
     int32_t* work = (int32_t*)(ws + L.off_tile_work);
@@ -406,7 +495,8 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
     uint32_t* sk = (uint32_t*)(ws + L.off_sj_keys);
     int32_t* sv_in = (int32_t*)(ws + L.off_sj_vals_in);
     int32_t* sv = (int32_t*)(ws + L.off_sj_vals);
-    k_tile_work<R><<<blocks_for(L.nkeys), threads, 0, s>>>(geo, counts, L.nkeys, L.span, L.adj_chunk, work, nsub);
+    k_tile_work<R><<<blocks_for(L.nkeys), threads, 0, s>>>(geo, counts, vcount, L.nkeys, L.span, L.adj_chunk, work,
+                                                           nsub);
     tb = L.cub_bytes;
     if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, nsub, suboff, (int)L.nkeys, s) != cudaSuccess)
       return set_error(TKBN_ERR_CUDA, "scan failed");
@@ -420,9 +510,6 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
     k_gather_items<<<blocks_for(L.max_subjobs), threads, 0, s>>>(sj_raw, sv, L.max_subjobs,
                                                                   (Item*)(ws + L.off_adj_jobs));
   }
-  if (n > 0)
-    k_sorted_points<R><<<blocks_for(n), threads, 0, s>>>(geo, (const R*)omega, vals, p->npts, n, coords,
-                                                         (cplx<R>*)(ws + L.off_phase));
   return check_cuda(cudaGetLastError(), "points build launch");
 }
 

@@ -237,10 +237,15 @@ struct PointsLayout {
   int adj_chunk;        // max candidates per adjoint sub-job
   int64_t max_subjobs;  // upper bound on adjoint sub-jobs
   int sj_key_bits;
+  // 2D owned tiles: per output tile, the list of points whose footprint
+  // reaches it ({sorted index, m, row offset, column offset}), built once
+  // per trajectory; the adjoint's sub-jobs are ranges of these lists.
+  bool vlist;
+  int64_t max_valid;  // upper bound on list entries (ncombo * npts_total)
   size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
       off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_phase,
       off_tile_work, off_tile_nsub, off_tile_suboff, off_sj_raw, off_adj_jobs, off_sj_keys_in, off_sj_keys,
-      off_sj_vals_in, off_sj_vals, off_cub;
+      off_sj_vals_in, off_sj_vals, off_vcount, off_voff, off_vlist, off_cub;
   size_t cub_bytes;
   size_t total;
 };
