@@ -41,6 +41,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 B, C, N, SPOKES, READ = 4, 16, 320, 404, 640
+# kernels of this library per timed step: forward FFT (row pass + column
+# pass), gather, adjoint (split-tile zeroing + owned-tile scatter), inverse
+# FFT (column pass + row pass)
+LAUNCHES_PER_STEP = 7
 METRIC = "NU points*coils/s (forward+adjoint SENSE NUFFT, 2D 320^2, 16 coils, batch 4)"
 UNIT = "points*coils/s"
 
@@ -349,6 +353,21 @@ def run_gpu(args):
         torch.cuda.synchronize()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
 
+    # Toeplitz normal operator (ToepNufft) on the same workload, reported beside the metric
+    with torch.no_grad():
+        kern = tkbn.calc_toeplitz_kernel(omega, (N, N))
+        toep = tkbn.ToepNufft()
+        for _ in range(args.warmup):
+            toep(image, kern, smaps=smaps)
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(args.steps):
+            toep(image, kern, smaps=smaps)
+        t1.record()
+        torch.cuda.synchronize()
+    toep_ms = max_over_ranks(t0.elapsed_time(t1) / args.steps, world, dev)
+
     work = B * C * M
     value = world * work / (ms * 1e-3)
     byts = algorithmic_bytes(M)
@@ -373,6 +392,7 @@ def run_gpu(args):
             "global_batch": B * world, "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)",
             "work_per_step": f"{work} points*coils per GPU (B*C*M, once per fwd+adj pair)",
             "stage_ms": {k: round(v, 4) for k, v in stage.items()},
+            "toep_nufft_ms": round(toep_ms, 4),
             "pipeline_gbs": round(pipeline_gbs, 1),
             "pipeline_algorithmic_bytes": byts["forward"] + byts["adjoint"],
             "parity_gate_rel_l2_staged_vs_module": gate,
@@ -383,7 +403,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "e2e": {"value": world * work / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(x_host.numel() * 8), "d2h_bytes_per_step": int(out_host.numel() * 8)},
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": LAUNCHES_PER_STEP * args.steps,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))

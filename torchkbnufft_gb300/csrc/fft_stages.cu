@@ -18,14 +18,19 @@
 #include <cmath>
 #include <new>
 
+#include "fft2d.cuh"
 #include "tkbn_common.cuh"
 
+// A plan is either the fused 2D passes of fft2d.cu (2D grids whose sizes
+// factor into radices 2..15 and fit shared memory) or a cuFFT plan.
 struct tkbn_fft_plan_s {
   cufftHandle handle;
   int ndim;
   int dtype;
   int64_t n[3];
   int64_t batch;
+  bool fused;
+  tkbn_host::Fft2d f2;
 };
 
 namespace tkbn {
@@ -219,6 +224,29 @@ int fft_plan_create(const tkbn_geometry* g, int64_t B, int64_t C, tkbn_fft_plan*
     n[d] = g->grid_size[d];
     p->n[d] = g->grid_size[d];
   }
+  p->fused = false;
+  if (g->ndim == 2 && g->grid_size[0] <= tkbn::kFftMaxN && g->grid_size[1] <= tkbn::kFftMaxN &&
+      fft1_plan((int)g->grid_size[0], &p->f2.p0) && fft1_plan((int)g->grid_size[1], &p->f2.p1)) {
+    p->f2.s.K0 = (int)g->grid_size[0];
+    p->f2.s.K1 = (int)g->grid_size[1];
+    p->f2.s.N0 = p->f2.s.K0;
+    p->f2.s.N1 = p->f2.s.K1;
+    const bool dbl = g->dtype == TKBN_C128;
+    if (fft2d_smem(p->f2, dbl) <= 200 * 1024) {
+      p->f2.tw0 = p->f2.tw1 = nullptr;
+      int rc = fft1_twiddles(p->f2.s.K0, dbl, &p->f2.tw0);
+      if (!rc) rc = fft1_twiddles(p->f2.s.K1, dbl, &p->f2.tw1);
+      if (rc) {
+        cudaFree(p->f2.tw0);
+        cudaFree(p->f2.tw1);
+        delete p;
+        return rc;
+      }
+      p->fused = true;
+      *out = p;
+      return TKBN_OK;
+    }
+  }
   int rc = check_cufft(cufftCreate(&p->handle), "cufftCreate");
   if (rc) {
     delete p;
@@ -239,9 +267,24 @@ int fft_plan_create(const tkbn_geometry* g, int64_t B, int64_t C, tkbn_fft_plan*
 
 int fft_plan_destroy(tkbn_fft_plan p) {
   if (!p) return TKBN_OK;
-  int rc = check_cufft(cufftDestroy(p->handle), "cufftDestroy");
+  int rc;
+  if (p->fused) {
+    rc = check_cuda(cudaFree(p->f2.tw0), "free twiddles");
+    const int rc1 = check_cuda(cudaFree(p->f2.tw1), "free twiddles");
+    if (!rc) rc = rc1;
+  } else {
+    rc = check_cufft(cufftDestroy(p->handle), "cufftDestroy");
+  }
   delete p;
   return rc;
+}
+
+// The fused passes of a plan with this call's image size.
+static Fft2d fused_for(const tkbn_fft_plan p, const Shape& s) {
+  Fft2d f = p->f2;
+  f.s.N0 = s.N[0];
+  f.s.N1 = s.N[1];
+  return f;
 }
 
 static int check_plan(const tkbn_geometry* g, tkbn_fft_plan p, int64_t B, int64_t C) {
@@ -313,6 +356,8 @@ int fft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image,
   if (norm != TKBN_NORM_NONE && norm != TKBN_NORM_ORTHO) return set_error(TKBN_ERR_INVALID, "Only option for norm is 'ortho'.");
   const int64_t ci = smaps ? 1 : C;
   const double sc = ortho_scale(s, norm);
+  if (plan->fused)
+    return fft2d_forward(fused_for(plan, s), g->dtype, B, C, ci, image, smaps, smaps_batch, scaling, sc, grid, st);
   rc = g->dtype == TKBN_C64 ? pad_scale_r<float>(s, B, C, ci, image, smaps, smaps_batch, scaling, sc, grid, st)
                             : pad_scale_r<double>(s, B, C, ci, image, smaps, smaps_batch, scaling, sc, grid, st);
   if (rc) return rc;
@@ -327,9 +372,11 @@ int ifft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, void* grid, const
   if (!image || !grid) return set_error(TKBN_ERR_INVALID, "null image or grid");
   if (smaps && smaps_batch != 1 && smaps_batch != B) return set_error(TKBN_ERR_INVALID, "smaps batch must be 1 or B");
   if (norm != TKBN_NORM_NONE && norm != TKBN_NORM_ORTHO) return set_error(TKBN_ERR_INVALID, "Only option for norm is 'ortho'.");
+  const double sc = ortho_scale(s, norm);
+  if (plan->fused)
+    return fft2d_inverse(fused_for(plan, s), g->dtype, B, C, grid, smaps, smaps_batch, scaling, sc, image, st);
   rc = fft_exec(plan, grid, CUFFT_INVERSE, st);
   if (rc) return rc;
-  const double sc = ortho_scale(s, norm);
   return g->dtype == TKBN_C64 ? crop_scale_r<float>(s, B, C, grid, smaps, smaps_batch, scaling, sc, image, st)
                               : crop_scale_r<double>(s, B, C, grid, smaps, smaps_batch, scaling, sc, image, st);
 }
@@ -349,6 +396,9 @@ int toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, co
   if (norm != TKBN_NORM_NONE && norm != TKBN_NORM_ORTHO) return set_error(TKBN_ERR_INVALID, "Only option for norm is 'ortho'.");
   const double sc = ortho_scale(s, norm);
   const int64_t ci = smaps ? 1 : C;
+  if (plan->fused)
+    return fft2d_toeplitz(fused_for(plan, s), g->dtype, B, C, ci, image, kernel, kbatch, by_channel, smaps,
+                          smaps_batch, sc, grid, out, st);
   if (g->dtype == TKBN_C64) {
     if ((rc = pad_scale_r<float>(s, B, C, ci, image, smaps, smaps_batch, nullptr, sc, grid, st))) return rc;
     if ((rc = fft_exec(plan, grid, CUFFT_FORWARD, st))) return rc;

@@ -174,6 +174,19 @@ __device__ __forceinline__ int64_t patch_row_base(const Geo<R>& geo, int rr, con
 // Stage Cc coil planes of the periodic patch [origin, origin + P) into smem:
 // one warp per patch row, lanes along the innermost dimension; each lane
 // wraps its column offsets once per job.
+// Asynchronous global -> shared copy of one complex element (cp.async,
+// cached in L1): a thread issues all of its patch copies back to back and
+// waits once, instead of one load latency per element.
+__device__ __forceinline__ void cp_async_elem(float2* smem_dst, const float2* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_elem(double2* smem_dst, const double2* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 template <typename R, int D>
 __device__ __forceinline__ void load_patch(const Geo<R>& geo, const cplx<R>* __restrict__ grid, int64_t plane0,
                                            int64_t gtot, int ncl, int cells, int ps, const int* origin,
@@ -190,11 +203,13 @@ __device__ __forceinline__ void load_patch(const Geo<R>& geo, const cplx<R>* __r
       cplx<R>* dst = patch + c * ps + rr * PX;
       int gx = gx0;
       for (int px = lane; px < PX; px += 32) {
-        dst[px] = src[gx];
+        cp_async_elem(dst + px, src + gx);
         gx = wrap_up(gx + 32, KX);
       }
     }
   }
+  // every copy of this thread has landed; the caller's barrier publishes them
+  cp_async_wait_all();
 }
 
 template <typename R, int D, int JC>
