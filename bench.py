@@ -409,6 +409,99 @@ def run_gpu(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- ragged batch (64 independent problems)
+
+
+def ragged_spec(seed: int = 1005, nprob: int = 64):
+    """64 problems: image 128/192/256/320 squared (grid 2x), 20k-400k points
+    (uniform random in [-pi, pi)^2 or a variable-density spiral), 1-16 coils."""
+    rng = np.random.default_rng(seed)
+    spec = []
+    for _ in range(nprob):
+        n = int(rng.choice([128, 192, 256, 320]))
+        M = int(rng.integers(20000, 400001))
+        C = int(rng.integers(1, 17))
+        if rng.random() < 0.5:
+            om = rng.uniform(-np.pi, np.pi, size=(2, M))
+        else:
+            nil = max(1, M // 2048)
+            t = (np.arange(-(-M // nil)) / (-(-M // nil)))
+            ks = [np.pi * t ** 1.5 * np.exp(1j * (2 * np.pi * 16 * t + 2 * np.pi * j / nil)) for j in range(nil)]
+            k = np.concatenate(ks)[:M]
+            om = np.stack([k.imag, k.real])
+        spec.append(((n, n), om.astype(np.float32), C))
+    return spec
+
+
+def run_ragged(args):
+    import torch
+
+    import torchkbnufft_gb300 as tkbn
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    spec = ragged_spec()
+    rng = np.random.default_rng(7)
+    probs, images = [], []
+    for im, om, C in spec:
+        probs.append((im, torch.tensor(om, device=dev), C))
+        x = (rng.standard_normal((1, C) + im) + 1j * rng.standard_normal((1, C) + im)).astype(np.complex64)
+        images.append(torch.tensor(x, device=dev))
+    work = sum(C * om.shape[1] for _, om, C in spec)
+    rn = tkbn.RaggedNufft(probs, autotune_layout=True)
+    rn.set_images(images)
+    # plain: one module call per problem and direction (the reference's way)
+    mods = {}
+    for im, _, _ in spec:
+        if im not in mods:
+            mods[im] = (tkbn.KbNufft(im_size=im, device=dev), tkbn.KbNufftAdjoint(im_size=im, device=dev))
+
+    def plain_step():
+        for (im, om, _), x in zip(probs, images):
+            f, a = mods[im]
+            a(f(x, om), om)
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    with torch.no_grad():
+        # parity gate: ragged vs per-problem calls on three problems
+        rn.forward_adjoint()
+        gate = 0.0
+        for p in range(3):
+            im, om, _ = probs[p]
+            f, a = mods[im]
+            ref = a(f(images[p], om), om)
+            out = rn.output_view(p)
+            gate = max(gate, float((torch.linalg.vector_norm(out - ref) / torch.linalg.vector_norm(ref)).item()))
+        plain_ms = timed(plain_step, args.steps, args.warmup)
+        eager_ms = timed(rn.forward_adjoint, args.steps, args.warmup)
+        rn.capture()
+        graph_ms = timed(rn.replay, args.steps, args.warmup)
+    line = {
+        "metric": "NU points*coils/s (ragged batch fwd+adj, 64 problems, graph-captured)", "value": work / (graph_ms * 1e-3),
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": graph_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {"workload": "ragged batch: 64 problems, image 128/192/256/320 squared, grid 2x, 20k-400k points "
+                               "(uniform random or variable-density spiral), 1-16 coil images, J=6, L=1024",
+                   "work_per_step": work, "plain_ms_per_step": plain_ms, "eager_ms_per_step": eager_ms,
+                   "graph_ms_per_step": graph_ms, "speedup_graph_vs_plain": plain_ms / graph_ms,
+                   "tiles": {f"{k[0]}x{k[1]}": v for k, v in rn.tiles.items()},
+                   "parity_gate_rel_l2_vs_per_problem": gate},
+        "gpu_launches": None,
+    }
+    print(json.dumps(line))
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -417,11 +510,15 @@ def main():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--ref-coils", type=int, default=4)
+    p.add_argument("--workload", default="sense", choices=["sense", "ragged"],
+                   help="sense: the metric's workload (default); ragged: 64 independent problems")
     args = p.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "ragged":
+        run_ragged(args)
     else:
         run_gpu(args)
 

@@ -39,6 +39,8 @@
  *   tkbn_fft_filter        fft_filter                   torchkbnufft/_nufft/fft.py:121-173
  *   tkbn_toep_apply        ToepNufft.forward / toep_batch_loop
  *                          torchkbnufft/modules/kbnufft.py:441-547
+ *   tkbn_ragged_*          a loop of table_interp / table_interp_adjoint calls
+ *                          over independent problems (no single counterpart)
  */
 #ifndef TKBN_GB300_H
 #define TKBN_GB300_H
@@ -134,6 +136,36 @@ int tkbn_interp_grad_omega(const tkbn_geometry* g, const tkbn_points_desc* p, co
 #define TKBN_NOALLOC_SCRATCH_BYTES ((size_t)8 << 20)
 int tkbn_interp_fwd_noalloc(const tkbn_geometry* g, const void* const* tables, const void* omega, int64_t npts,
                             const void* grid, int64_t nbatch, int64_t ncoil, void* kdata, void* stream);
+
+/* ---- ragged batch (K8): many independent problems per launch ------------
+ * No single counterpart in the reference, where each problem is one call of
+ * table_interp / table_interp_adjoint (torchkbnufft/_nufft/interp.py:315-403,
+ * 587-726). Each problem has its own geometry (grid and image size, tables),
+ * trajectory layout (built by tkbn_points_build, ntraj = 1), coil count and
+ * device buffers; all share dtype, ndim and numpoints. The plan merges the
+ * problems' work into one longest-first job list per stage, so that one
+ * launch interpolates every problem; the buffers named here are the ones the
+ * launches read and write (a CUDA graph can capture them). */
+typedef struct tkbn_ragged_problem {
+  tkbn_geometry geom;        /* flags as for the single-problem calls */
+  tkbn_points_desc points;   /* ntraj must be 1 */
+  const void* workspace;     /* layout of this problem's omega */
+  const void* tables[3];     /* per-dim tables of this geometry */
+  int64_t ncoil;
+  void* grid;                /* (ncoil, K...) */
+  void* kdata;               /* (ncoil, M) */
+} tkbn_ragged_problem;
+
+typedef struct tkbn_ragged_plan_s* tkbn_ragged_plan;
+
+/* Reads the layouts' work lists (synchronises the device), allocates the
+ * merged job lists. Adjoints need grids with K_d >= T_d + J_d - 1. */
+int tkbn_ragged_plan_create(const tkbn_ragged_problem* problems, int64_t nproblems, tkbn_ragged_plan* plan);
+int tkbn_ragged_plan_destroy(tkbn_ragged_plan plan);
+/* kdata_p = interp(grid_p) for every problem p, one launch. */
+int tkbn_ragged_interp_fwd(tkbn_ragged_plan plan, void* stream);
+/* grid_p = interp^H(kdata_p) for every problem p (grids fully overwritten). */
+int tkbn_ragged_interp_adj(tkbn_ragged_plan plan, void* stream);
 
 /* ---- FFT stages --------------------------------------------------------- */
 /* cuFFT plan for nbatch*ncoil transforms of size grid_size (in place). */

@@ -13,7 +13,9 @@ from ._math import absolute, complex_mult, complex_sign, conj_complex_mult, imag
 from ._setup import init_fn
 from .dcomp import calc_density_compensation_function
 from .modules import KbInterp, KbInterpAdjoint, KbNufft, KbNufftAdjoint, ToepNufft
+from .ragged import RaggedNufft
 from .toep import calc_toeplitz_kernel
+from . import autotune
 from . import _setup as nufft_utils
 
 __version__ = "0.1.0"
@@ -29,6 +31,7 @@ __all__ = [
     "KbInterpAdjoint",
     "KbNufft",
     "KbNufftAdjoint",
+    "RaggedNufft",
     "ToepNufft",
     "absolute",
     "calc_density_compensation_function",

@@ -51,6 +51,18 @@ class PointsDesc(ctypes.Structure):
     ]
 
 
+class RaggedProblem(ctypes.Structure):
+    _fields_ = [
+        ("geom", Geometry),
+        ("points", PointsDesc),
+        ("workspace", ctypes.c_void_p),
+        ("tables", ctypes.c_void_p * 3),
+        ("ncoil", ctypes.c_int64),
+        ("grid", ctypes.c_void_p),
+        ("kdata", ctypes.c_void_p),
+    ]
+
+
 _P = ctypes.c_void_p
 _GP = ctypes.POINTER(Geometry)
 _DP = ctypes.POINTER(PointsDesc)
@@ -77,6 +89,10 @@ SIGNATURES = {
     "tkbn_fft_filter": [_GP, _P, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P],
     "tkbn_toep_apply": [_GP, _P, _P, _P, _I64, _P, _I64, _I64, _I64, _INT, _P, _P, _P],
     "tkbn_interp_fwd_noalloc": [_GP, _PP, _P, _I64, _P, _I64, _I64, _P, _P],
+    "tkbn_ragged_plan_create": [ctypes.POINTER(RaggedProblem), _I64, ctypes.POINTER(ctypes.c_void_p)],
+    "tkbn_ragged_plan_destroy": [_P],
+    "tkbn_ragged_interp_fwd": [_P, _P],
+    "tkbn_ragged_interp_adj": [_P, _P],
 }
 
 _lock = threading.Lock()

@@ -189,7 +189,7 @@ class PointsLayout:
 
 
 _layout_cache: "collections.OrderedDict" = collections.OrderedDict()
-_LAYOUT_CACHE_MAX = 8
+_LAYOUT_CACHE_MAX = 128
 
 
 def points_layout(geom: GeomKey, omega: torch.Tensor, tile=None, chunk: int = 0) -> PointsLayout:
@@ -234,7 +234,7 @@ class FFTPlan:
 
 
 _fft_cache: "collections.OrderedDict" = collections.OrderedDict()
-_FFT_CACHE_MAX = 16
+_FFT_CACHE_MAX = 128
 
 
 def fft_plan(geom: GeomKey, batch: int, coils: int, device: torch.device) -> FFTPlan:

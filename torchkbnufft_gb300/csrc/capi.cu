@@ -26,6 +26,10 @@ int ifft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, void* grid, const
 int toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, const void* kernel, int64_t kbatch,
                int by_channel, const void* smaps, int64_t smaps_batch, int64_t B, int64_t C, int norm, void* grid,
                void* out, cudaStream_t st);
+int ragged_plan_create(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan* out);
+int ragged_plan_destroy(tkbn_ragged_plan p);
+int ragged_interp_fwd(tkbn_ragged_plan p, cudaStream_t s);
+int ragged_interp_adj(tkbn_ragged_plan p, cudaStream_t s);
 }  // namespace tkbn_host
 
 using namespace tkbn_host;
@@ -180,3 +184,18 @@ int tkbn_toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* imag
 }
 
 }  // extern "C"
+
+int tkbn_ragged_plan_create(const tkbn_ragged_problem* problems, int64_t nproblems, tkbn_ragged_plan* plan) {
+  if (!problems || !plan) return set_error(TKBN_ERR_INVALID, "null argument");
+  TKBN_GUARD(ragged_plan_create(problems, nproblems, plan));
+}
+
+int tkbn_ragged_plan_destroy(tkbn_ragged_plan plan) { TKBN_GUARD(ragged_plan_destroy(plan)); }
+
+int tkbn_ragged_interp_fwd(tkbn_ragged_plan plan, void* stream) {
+  TKBN_GUARD(ragged_interp_fwd(plan, (cudaStream_t)stream));
+}
+
+int tkbn_ragged_interp_adj(tkbn_ragged_plan plan, void* stream) {
+  TKBN_GUARD(ragged_interp_adj(plan, (cudaStream_t)stream));
+}

@@ -681,16 +681,9 @@ int fft1_twiddles(int n, bool dbl, void** dev) {
 // CTA count (SMs x CTAs per SM), capped at the number of work units.
 template <typename K>
 static int fft_launch_shape(K kernel, int threads, size_t smem, int64_t units, int* blocks) {
-  int rc = check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                      "fft smem attribute");
+  int64_t b = 0;
+  const int rc = resident_grid((const void*)kernel, threads, smem, &b);
   if (rc) return rc;
-  int dev = 0, sms = 0, per_sm = 0;
-  if ((rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice"))) return rc;
-  if ((rc = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"))) return rc;
-  if ((rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem), "occupancy")))
-    return rc;
-  if (per_sm < 1) return set_error(TKBN_ERR_UNSUPPORTED, "fft pass cannot be resident with %zu B smem", smem);
-  int64_t b = (int64_t)per_sm * sms;
   if (units < b) b = units;
   *blocks = (int)(b < 1 ? 1 : b);
   return TKBN_OK;

@@ -18,7 +18,11 @@
 // The separable sums group the products per dimension; the table bins, cell
 // indices and phase argument are computed exactly as the reference does.
 
+#include <algorithm>
+#include <cstring>
+#include <new>
 #include <type_traits>
+#include <vector>
 
 #include "geo_host.cuh"
 #include "tkbn_common.cuh"
@@ -370,24 +374,22 @@ __device__ __forceinline__ bool next_job(const Geo<R>& geo, const Launch& a, int
   return true;
 }
 
+// One gather job (a work item of one batch item and coil chunk). All
+// threads of the CTA call it; `patch` is the dynamic shared memory.
 template <typename R, int D, int JC>
-__global__ void __launch_bounds__(kThreads) k_interp_fwd(Geo<R> geo, Launch a, const R* __restrict__ tm,
-                                                         const cplx<R>* __restrict__ ph,
-                                                         const cplx<R>* __restrict__ grid, cplx<R>* __restrict__ kdata) {
+__device__ __forceinline__ void fwd_job(const Geo<R>& geo, const Launch& a, const R* __restrict__ tm,
+                                        const cplx<R>* __restrict__ ph, const cplx<R>* __restrict__ grid,
+                                        cplx<R>* __restrict__ kdata, int64_t job, int64_t nitems, cplx<R>* patch) {
   constexpr int NJ = NJOf<JC>::N;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  cplx<R>* patch = reinterpret_cast<cplx<R>*>(smem_raw);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   cplx<R>* scr_warp = patch + a.Cc * a.ps + warp * a.scratch;
-  const int64_t nitems = a.hdr[0];
-  const int64_t njobs = nitems * a.nbpt * a.ncc;
   const int ppw = 32 / a.Cc;
   const int ppb = ppw * kWarps;
   const int c = lane % a.Cc;
   const int pslot = lane / a.Cc;
   const bool coop = a.Cc >= 4;
   cplx<R>* scr = scr_warp + pslot * (D * NJ);
-  for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x) {
+  {
     Item it;
     JobCtx jc;
     next_job<R>(geo, a, job, nitems, &it, &jc);
@@ -434,6 +436,18 @@ __global__ void __launch_bounds__(kThreads) k_interp_fwd(Geo<R> geo, Launch a, c
       if (active && !ok && c == 0) atomicOr(&g_status, kStatusNonFinite | kStatusOutsidePatch);
     }
   }
+}
+
+template <typename R, int D, int JC>
+__global__ void __launch_bounds__(kThreads) k_interp_fwd(Geo<R> geo, Launch a, const R* __restrict__ tm,
+                                                         const cplx<R>* __restrict__ ph,
+                                                         const cplx<R>* __restrict__ grid, cplx<R>* __restrict__ kdata) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* patch = reinterpret_cast<cplx<R>*>(smem_raw);
+  const int64_t nitems = a.hdr[0];
+  const int64_t njobs = nitems * a.nbpt * a.ncc;
+  for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
+    fwd_job<R, D, JC>(geo, a, tm, ph, grid, kdata, job, nitems, patch);
 }
 
 template <typename R, int D, int JC>
@@ -536,6 +550,34 @@ __device__ __forceinline__ void own_tile_geometry(const Geo<R>& geo, int key, in
 
 // Zero the output tiles that are split over several sub-jobs (they are
 // accumulated with atomics); every plane of the batch items the tile serves.
+// Zero output tile it.key in every plane of the batch items it serves; the
+// warps of CTA (x, y) take rows y*8 + warp, strided by 8*gridDim.y.
+template <typename R, int D>
+__device__ __forceinline__ void zero_tile(const Geo<R>& geo, const OwnLaunch& a, const Item& it,
+                                          cplx<R>* __restrict__ grid) {
+  int64_t t;
+  int td[kMaxDim], origin[kMaxDim], ext[kMaxDim];
+  own_tile_geometry<R, D>(geo, it.key, &t, td, origin, ext);
+  const int64_t b0 = a.ntraj == 1 ? 0 : t, b1 = a.ntraj == 1 ? a.B : t + 1;
+  int rows = 1;
+#pragma unroll
+  for (int d = 0; d < D - 1; ++d) rows *= ext[d];
+  const int64_t nrow = (b1 - b0) * a.C * rows;
+  const int64_t wstride = (int64_t)gridDim.y * (blockDim.x / 32);
+  for (int64_t r = (int64_t)blockIdx.y * (blockDim.x / 32) + threadIdx.x / 32; r < nrow; r += wstride) {
+    const int64_t plane = b0 * a.C + r / rows;
+    int rr = (int)(r % rows);
+    int64_t off = 0;
+    if (D == 2) off = (int64_t)(origin[0] + rr) * geo.K[1];
+    if (D == 3) {
+      const int y = rr % ext[1 % D], z = rr / ext[1 % D];
+      off = ((int64_t)(origin[0] + z) * geo.K[1 % D] + origin[1 % D] + y) * geo.K[2 % D];
+    }
+    cplx<R>* dst = grid + plane * a.gtot + off + origin[D - 1];
+    for (int x = threadIdx.x & 31; x < ext[D - 1]; x += 32) dst[x] = mk<R>(0, 0);
+  }
+}
+
 template <typename R, int D>
 __global__ void k_zero_split_tiles(Geo<R> geo, OwnLaunch a, int W, cplx<R>* __restrict__ grid) {
   const int64_t nsj = a.hdr[1];
@@ -545,40 +587,20 @@ __global__ void k_zero_split_tiles(Geo<R> geo, OwnLaunch a, int W, cplx<R>* __re
     // has the full length W: nothing after the first shorter job is one
     if (it.len < W) break;
     if (!(it.pad && it.start == 0)) continue;
-    int64_t t;
-    int td[kMaxDim], origin[kMaxDim], ext[kMaxDim];
-    own_tile_geometry<R, D>(geo, it.key, &t, td, origin, ext);
-    const int64_t b0 = a.ntraj == 1 ? 0 : t, b1 = a.ntraj == 1 ? a.B : t + 1;
-    int rows = 1;
-#pragma unroll
-    for (int d = 0; d < D - 1; ++d) rows *= ext[d];
-    const int64_t nrow = (b1 - b0) * a.C * rows;
-    const int64_t wstride = (int64_t)gridDim.y * (blockDim.x / 32);
-    for (int64_t r = (int64_t)blockIdx.y * (blockDim.x / 32) + threadIdx.x / 32; r < nrow; r += wstride) {
-      const int64_t plane = b0 * a.C + r / rows;
-      int rr = (int)(r % rows);
-      int64_t off = 0;
-      if (D == 2) off = (int64_t)(origin[0] + rr) * geo.K[1];
-      if (D == 3) {
-        const int y = rr % ext[1 % D], z = rr / ext[1 % D];
-        off = ((int64_t)(origin[0] + z) * geo.K[1 % D] + origin[1 % D] + y) * geo.K[2 % D];
-      }
-      cplx<R>* dst = grid + plane * a.gtot + off + origin[D - 1];
-      for (int x = threadIdx.x & 31; x < ext[D - 1]; x += 32) dst[x] = mk<R>(0, 0);
-    }
+    zero_tile<R, D>(geo, a, it, grid);
   }
 }
 
 // FAST: D == 2, J == 6, Cc == 16 and 16-row tiles — each warp owns two rows,
 // lanes are (coil, row) and the six footprint columns are unrolled.
+// One owned-tile adjoint job (a sub-job of one batch item and coil chunk).
+// All threads of the CTA call it; smem_raw is the dynamic shared memory.
 template <typename R, int D, int JC, bool FAST>
-__global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaunch a, const R* __restrict__ tm,
-                                                             const cplx<R>* __restrict__ ph,
-                                                             const cplx<R>* __restrict__ kdata,
-                                                             cplx<R>* __restrict__ grid) {
+__device__ __forceinline__ void own_job(const Geo<R>& geo, const OwnLaunch& a, const R* __restrict__ tm,
+                                        const cplx<R>* __restrict__ ph, const cplx<R>* __restrict__ kdata,
+                                        cplx<R>* __restrict__ grid, int64_t job, unsigned char* smem_raw) {
   constexpr int NJ = NJOf<JC>::N;
   constexpr int MAXCOMBO = D == 1 ? 8 : (D == 2 ? 16 : 27);
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* acc = reinterpret_cast<cplx<R>*>(smem_raw);  // [Cc][aps]
   cplx<R>* sfac = acc + a.Cc * a.aps;                    // [kNB][D*NJ], conjugated
   cplx<R>* sv = sfac + kNB * D * NJ;                     // [kNB][Cc]
@@ -590,7 +612,6 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t per_sj = a.nbpt * a.ncc;
-  const int64_t njobs = a.hdr[1] * per_sj;
   const int G = 32 / a.Cc;                       // lane groups per coil
   const int c = lane % a.Cc, grp = lane / a.Cc;  // this lane's coil and group
   const int JX = JC > 0 ? JC : geo.J[D - 1];
@@ -602,7 +623,7 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
   const int r_hi = FAST ? 2 * warp + 2 : ((warp + 1) * trows) / kWarps;
   const int TX = geo.T[D - 1];
 
-  for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x) {
+  {
     const Item it = a.jobs[job / per_sj];
     const int64_t rest = job % per_sj;
     const int cc = (int)(rest % a.ncc);
@@ -847,6 +868,17 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
   }
 }
 
+template <typename R, int D, int JC, bool FAST>
+__global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaunch a, const R* __restrict__ tm,
+                                                             const cplx<R>* __restrict__ ph,
+                                                             const cplx<R>* __restrict__ kdata,
+                                                             cplx<R>* __restrict__ grid) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t njobs = a.hdr[1] * a.nbpt * a.ncc;
+  for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
+    own_job<R, D, JC, FAST>(geo, a, tm, ph, kdata, grid, job, smem_raw);
+}
+
 // Smooth table lookup for the gradient: linear interpolation of value and
 // derivative tables at the exact (unrounded) position.
 // K4 (owned tiles, registers): the common 2D case — J = 6 in both dims,
@@ -887,13 +919,10 @@ __device__ __forceinline__ void reg_add_point(int lx, float2 (&racc)[kRegTileX],
 
 // vec_ok: the grid pointer is 16-byte aligned and K1 is even, so every
 // tile row starts 16-byte aligned and pairs of cells go out as one float4.
-__global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg(Geo<float> geo, OwnLaunch a,
-                                                                const float* __restrict__ tm,
-                                                                const float2* __restrict__ ph,
-                                                                const float2* __restrict__ kdata,
-                                                                float2* __restrict__ grid, int vec_ok) {
+__device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& a, const float* __restrict__ tm,
+                                        const float2* __restrict__ ph, const float2* __restrict__ kdata,
+                                        float2* __restrict__ grid, int vec_ok, int64_t job, unsigned char* smem_raw) {
   constexpr int D = 2, NJ = 6;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* sfac = reinterpret_cast<float2*>(smem_raw);  // [kNBR][12]: conj y factors, conj x factors
   float2* sv = sfac + kNBR * D * NJ;                   // [kNBR][16] conj(phase) * kdata per coil
   int2* sloc = reinterpret_cast<int2*>(sv + kNBR * kRegCoils);  // [kNBR] footprint start (y, x) in the tile
@@ -901,9 +930,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg(Geo<float> geo, 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int c = lane & 15, myrow = 2 * warp + (lane >> 4);
   const int64_t per_sj = a.nbpt * a.ncc;
-  const int64_t njobs = a.hdr[1] * per_sj;
 
-  for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x) {
+  {
     const Item it = a.jobs[job / per_sj];
     const int64_t rest = job % per_sj;
     const int cc = (int)(rest % a.ncc);
@@ -1005,6 +1033,17 @@ __global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg(Geo<float> geo, 
       }
     }
   }
+}
+
+__global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg(Geo<float> geo, OwnLaunch a,
+                                                                const float* __restrict__ tm,
+                                                                const float2* __restrict__ ph,
+                                                                const float2* __restrict__ kdata,
+                                                                float2* __restrict__ grid, int vec_ok) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t njobs = a.hdr[1] * a.nbpt * a.ncc;
+  for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
+    reg_job(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw);
 }
 
 template <typename R>
@@ -1176,6 +1215,97 @@ __global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, 
   }
 }
 
+// ---------------------------------------------------------------- K8 ragged
+// Many independent problems (each its own grid and image size, trajectory
+// and coil count; one dtype, ndim and numpoints) in one launch per stage.
+// Every entry of the merged, longest-first job list names its problem; a CTA
+// copies that problem's descriptor into shared memory when the problem
+// changes and runs the same per-job code as the single-problem kernels.
+template <typename R>
+struct RaggedProb {
+  Geo<R> geo;
+  Launch a;
+  OwnLaunch o;
+  const R* tm;
+  const cplx<R>* ph;
+  cplx<R>* grid;
+  cplx<R>* kdata;
+  int64_t nitems;
+  int vec_ok;
+  int pad_;
+};
+
+template <typename T>
+__device__ __forceinline__ void load_desc(T* dst, const T* __restrict__ src) {
+  static_assert(sizeof(T) % 4 == 0, "descriptor size");
+  const int* s = reinterpret_cast<const int*>(src);
+  int* d = reinterpret_cast<int*>(dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(T) / 4); i += blockDim.x) d[i] = s[i];
+}
+
+template <typename R, int D, int JC>
+__global__ void __launch_bounds__(kThreads) k_ragged_fwd(const RaggedProb<R>* __restrict__ probs,
+                                                         const int2* __restrict__ jobs, int64_t njobs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) RaggedProb<R> sp;
+  cplx<R>* patch = reinterpret_cast<cplx<R>*>(smem_raw);
+  int cur = -1;
+  for (int64_t g = blockIdx.x; g < njobs; g += gridDim.x) {
+    const int2 pj = jobs[g];
+    if (pj.x != cur) {
+      __syncthreads();
+      load_desc(&sp, probs + pj.x);
+      __syncthreads();
+      cur = pj.x;
+    }
+    fwd_job<R, D, JC>(sp.geo, sp.a, sp.tm, sp.ph, sp.grid, sp.kdata, pj.y, sp.nitems, patch);
+  }
+}
+
+template <typename R, int D>
+__global__ void k_ragged_zero(const RaggedProb<R>* __restrict__ probs, const int2* __restrict__ jobs, int64_t njobs) {
+  for (int64_t g = blockIdx.x; g < njobs; g += gridDim.x) {
+    const int2 pj = jobs[g];
+    const RaggedProb<R>& P = probs[pj.x];
+    zero_tile<R, D>(P.geo, P.o, P.o.jobs[pj.y], P.grid);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 3) k_ragged_adj_reg(const RaggedProb<float>* __restrict__ probs,
+                                                                const int2* __restrict__ jobs, int64_t njobs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) RaggedProb<float> sp;
+  int cur = -1;
+  for (int64_t g = blockIdx.x; g < njobs; g += gridDim.x) {
+    const int2 pj = jobs[g];
+    if (pj.x != cur) {
+      __syncthreads();
+      load_desc(&sp, probs + pj.x);
+      __syncthreads();
+      cur = pj.x;
+    }
+    reg_job(sp.geo, sp.o, sp.tm, sp.ph, sp.kdata, sp.grid, sp.vec_ok, pj.y, smem_raw);
+  }
+}
+
+template <typename R, int D, int JC>
+__global__ void __launch_bounds__(kThreads) k_ragged_adj_own(const RaggedProb<R>* __restrict__ probs,
+                                                             const int2* __restrict__ jobs, int64_t njobs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) RaggedProb<R> sp;
+  int cur = -1;
+  for (int64_t g = blockIdx.x; g < njobs; g += gridDim.x) {
+    const int2 pj = jobs[g];
+    if (pj.x != cur) {
+      __syncthreads();
+      load_desc(&sp, probs + pj.x);
+      __syncthreads();
+      cur = pj.x;
+    }
+    own_job<R, D, JC, false>(sp.geo, sp.o, sp.tm, sp.ph, sp.kdata, sp.grid, pj.y, smem_raw);
+  }
+}
+
 }  // namespace tkbn
 
 namespace tkbn_host {
@@ -1250,16 +1380,9 @@ static int prepare(const tkbn_geometry* g, const tkbn_points_desc* p, const void
 // most one per job.
 template <typename K>
 static int resident_blocks(K kernel, size_t smem, int64_t max_jobs, int* blocks) {
-  int rc = check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                      "smem attribute");
+  int64_t b = 0;
+  const int rc = resident_grid((const void*)kernel, kThreads, smem, &b);
   if (rc) return rc;
-  int dev = 0, sms = 0, per_sm = 0;
-  if ((rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice"))) return rc;
-  if ((rc = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"))) return rc;
-  if ((rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem), "occupancy")))
-    return rc;
-  if (per_sm < 1) return set_error(TKBN_ERR_UNSUPPORTED, "interpolation kernel cannot be resident with %zu B smem", smem);
-  int64_t b = (int64_t)per_sm * sms;
   if (max_jobs < b) b = max_jobs;
   *blocks = (int)(b < 1 ? 1 : b);
   return TKBN_OK;
@@ -1333,10 +1456,7 @@ constexpr int max_combo() {
   return D == 1 ? 8 : (D == 2 ? 16 : 27);
 }
 
-template <typename R, int D, int JC>
-static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* kdata, void* grid,
-                            cudaStream_t s) {
-  constexpr int NJ = NJOf<JC>::N;
+static OwnLaunch make_own(const InterpPlan& ip, const char* ws, int D) {
   OwnLaunch o;
   o.jobs = (const Item*)(ws + ip.L.off_adj_jobs);
   o.hdr = ip.a.hdr;
@@ -1358,9 +1478,35 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
   o.span = ip.L.span;
   o.vlist = ip.L.vlist ? (const int4*)(ws + ip.L.off_vlist) : nullptr;
   o.voff = ip.L.vlist ? (const int32_t*)(ws + ip.L.off_voff) : nullptr;
-  const size_t smem = (size_t)o.Cc * o.aps * sizeof(cplx<R>) + (size_t)kNB * D * NJ * sizeof(cplx<R>) +
-                      (size_t)kNB * o.Cc * sizeof(cplx<R>) +
-                      sizeof(int) * ((size_t)kNB * D + kNB + 2 * max_combo<D>() + 1 + kNB / 32);
+  return o;
+}
+
+// Shared memory of the generic owned-tile adjoint for Cc coils per job.
+template <typename R, int D, int JC>
+static size_t own_smem(const OwnLaunch& o) {
+  constexpr int NJ = NJOf<JC>::N;
+  return (size_t)o.Cc * o.aps * sizeof(cplx<R>) + (size_t)kNB * D * NJ * sizeof(cplx<R>) +
+         (size_t)kNB * o.Cc * sizeof(cplx<R>) +
+         sizeof(int) * ((size_t)kNB * D + kNB + 2 * max_combo<D>() + 1 + kNB / 32);
+}
+
+// The register adjoint applies: 2D complex64, J = 6, 16-coil jobs, 16 x 14
+// tiles with per-tile point lists.
+template <typename R, int D, int JC>
+static bool reg_eligible(const InterpPlan& ip, const OwnLaunch& o) {
+  return std::is_same<R, float>::value && D == 2 && JC == 6 && o.vlist && o.Cc == kRegCoils &&
+         ip.L.tile[0] == kRegTileY && ip.L.tile[1] == kRegTileX;
+}
+
+static size_t reg_smem() {
+  return (size_t)kNBR * (2 * 6 + kRegCoils) * sizeof(float2) + (size_t)kNBR * sizeof(int2);
+}
+
+template <typename R, int D, int JC>
+static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* kdata, void* grid,
+                            cudaStream_t s) {
+  const OwnLaunch o = make_own(ip, ws, D);
+  const size_t smem = own_smem<R, D, JC>(o);
   if (smem > 220 * 1024) return set_error(TKBN_ERR_UNSUPPORTED, "adjoint tile needs %zu bytes of shared memory", smem);
   const int64_t max_jobs = ip.L.max_subjobs * o.nbpt * o.ncc;
   // split tiles are accumulated atomically: zero them first. Blocks
@@ -1374,8 +1520,8 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
     if (rc) return rc;
   }
   if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
-    if (o.vlist && o.Cc == kRegCoils && ip.L.tile[0] == kRegTileY && ip.L.tile[1] == kRegTileX) {
-      const size_t rsmem = (size_t)kNBR * (D * 6 + kRegCoils) * sizeof(float2) + (size_t)kNBR * sizeof(int2);
+    if (reg_eligible<R, D, JC>(ip, o)) {
+      const size_t rsmem = reg_smem();
       int blocks;
       int rc = resident_blocks(k_interp_adj_reg, rsmem, max_jobs, &blocks);
       if (rc) return rc;
@@ -1493,6 +1639,241 @@ int interp_grad(const tkbn_geometry* g, const tkbn_points_desc* p, const void* w
   if (g->dtype == TKBN_C64) return interp_grad_r<float>(g, p, ws, tables, dtables, grid, v, B, C, grad, s);
   if (g->dtype == TKBN_C128) return interp_grad_r<double>(g, p, ws, tables, dtables, grid, v, B, C, grad, s);
   return set_error(TKBN_ERR_UNSUPPORTED, "unsupported dtype %d", g->dtype);
+}
+
+// ---------------------------------------------------------------- K8 ragged plan
+
+}  // namespace tkbn_host
+
+struct tkbn_ragged_plan_s {
+  int dtype, ndim, j6;
+  int64_t nprob;
+  void* probs;  // RaggedProb<R>[nprob] on the device
+  int2 *fwd_jobs, *reg_jobs, *own_jobs, *zero_jobs;
+  int64_t n_fwd, n_reg, n_own, n_zero;
+  size_t smem_fwd, smem_own;
+};
+
+namespace tkbn_host {
+
+namespace {
+
+struct JobRec {
+  int len;
+  int p;
+  int j;
+};
+
+// Longest first, then problem and job index (a fixed order).
+void lpt_sort(std::vector<JobRec>& v) {
+  std::stable_sort(v.begin(), v.end(), [](const JobRec& x, const JobRec& y) { return x.len > y.len; });
+}
+
+int upload_jobs(const std::vector<JobRec>& v, int2** dev) {
+  *dev = nullptr;
+  if (v.empty()) return TKBN_OK;
+  std::vector<int2> h(v.size());
+  for (size_t i = 0; i < v.size(); ++i) h[i] = make_int2(v[i].p, v[i].j);
+  int rc = check_cuda(cudaMalloc((void**)dev, h.size() * sizeof(int2)), "ragged job list");
+  if (rc) return rc;
+  return check_cuda(cudaMemcpy(*dev, h.data(), h.size() * sizeof(int2), cudaMemcpyHostToDevice), "ragged job upload");
+}
+
+template <typename R, int D, int JC>
+int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P) {
+  std::vector<RaggedProb<R>> desc((size_t)n);
+  std::vector<JobRec> fwd, reg, own, zero;
+  P->smem_fwd = 0;
+  P->smem_own = 0;
+  for (int64_t q = 0; q < n; ++q) {
+    const tkbn_ragged_problem& r = pr[q];
+    InterpPlan ip;
+    int rc = prepare<R>(&r.geom, &r.points, r.workspace, 1, r.ncoil, Op::kFwd, &ip);
+    if (rc) return rc;
+    if (!r.grid || !r.kdata) return set_error(TKBN_ERR_INVALID, "problem %lld: null grid or kdata", (long long)q);
+    const char* ws = (const char*)r.workspace;
+    int64_t hdr[2] = {0, 0};
+    if ((rc = check_cuda(cudaMemcpy(hdr, ip.a.hdr, sizeof(hdr), cudaMemcpyDeviceToHost), "read layout header")))
+      return rc;
+    RaggedProb<R>& d = desc[(size_t)q];
+    memset(&d, 0, sizeof(d));
+    d.geo = make_geo<R>(&r.geom, &ip.L, r.tables, nullptr);
+    d.a = ip.a;
+    d.o = make_own(ip, ws, D);
+    d.tm = (const R*)(ws + ip.L.off_coords);
+    d.ph = (const cplx<R>*)(ws + ip.L.off_phase);
+    d.grid = (cplx<R>*)r.grid;
+    d.kdata = (cplx<R>*)r.kdata;
+    d.nitems = hdr[0];
+    d.vec_ok = ((uintptr_t)r.grid % 16 == 0) && (r.geom.grid_size[D - 1] % 2 == 0);
+    if (ip.smem > P->smem_fwd) P->smem_fwd = ip.smem;
+    // forward jobs: item i % nitems of coil chunk i / nitems
+    if (r.points.npts > 0 && hdr[0] > 0) {
+      std::vector<Item> items((size_t)hdr[0]);
+      if ((rc = check_cuda(cudaMemcpy(items.data(), ip.a.items, items.size() * sizeof(Item), cudaMemcpyDeviceToHost),
+                           "read work items")))
+        return rc;
+      for (int64_t j = 0; j < hdr[0] * ip.a.ncc; ++j) fwd.push_back({items[(size_t)(j % hdr[0])].len, (int)q, (int)j});
+    }
+    // adjoint jobs: sub-job j / ncc of coil chunk j % ncc
+    if (!ip.L.owned_ok || ip.L.span.ncombo > max_combo<D>())
+      return set_error(TKBN_ERR_UNSUPPORTED, "problem %lld: grid too small for the owned-tile adjoint", (long long)q);
+    std::vector<Item> sj((size_t)hdr[1]);
+    if (hdr[1] > 0 &&
+        (rc = check_cuda(cudaMemcpy(sj.data(), d.o.jobs, sj.size() * sizeof(Item), cudaMemcpyDeviceToHost),
+                         "read adjoint sub-jobs")))
+      return rc;
+    const bool use_reg = reg_eligible<R, D, JC>(ip, d.o);
+    if (!use_reg) {
+      const size_t sm = own_smem<R, D, JC>(d.o);
+      if (sm > 220 * 1024) return set_error(TKBN_ERR_UNSUPPORTED, "adjoint tile needs %zu bytes of shared memory", sm);
+      if (sm > P->smem_own) P->smem_own = sm;
+    }
+    for (int64_t j = 0; j < hdr[1] * ip.a.ncc; ++j) {
+      const Item& it = sj[(size_t)(j / ip.a.ncc)];
+      (use_reg ? reg : own).push_back({it.len, (int)q, (int)j});
+    }
+    for (int64_t j = 0; j < hdr[1]; ++j)
+      if (sj[(size_t)j].pad && sj[(size_t)j].start == 0) zero.push_back({sj[(size_t)j].len, (int)q, (int)j});
+  }
+  lpt_sort(fwd);
+  lpt_sort(reg);
+  lpt_sort(own);
+  int rc = check_cuda(cudaMalloc(&P->probs, desc.size() * sizeof(RaggedProb<R>)), "ragged descriptors");
+  if (rc) return rc;
+  if ((rc = check_cuda(cudaMemcpy(P->probs, desc.data(), desc.size() * sizeof(RaggedProb<R>), cudaMemcpyHostToDevice),
+                       "ragged descriptor upload")))
+    return rc;
+  if ((rc = upload_jobs(fwd, &P->fwd_jobs)) || (rc = upload_jobs(reg, &P->reg_jobs)) ||
+      (rc = upload_jobs(own, &P->own_jobs)) || (rc = upload_jobs(zero, &P->zero_jobs)))
+    return rc;
+  P->n_fwd = (int64_t)fwd.size();
+  P->n_reg = (int64_t)reg.size();
+  P->n_own = (int64_t)own.size();
+  P->n_zero = (int64_t)zero.size();
+  return TKBN_OK;
+}
+
+template <typename R, int D, int JC>
+int ragged_fwd_t(const tkbn_ragged_plan_s* P, cudaStream_t s) {
+  if (P->n_fwd == 0) return TKBN_OK;
+  int blocks;
+  int rc = resident_blocks(k_ragged_fwd<R, D, JC>, P->smem_fwd, P->n_fwd, &blocks);
+  if (rc) return rc;
+  k_ragged_fwd<R, D, JC><<<blocks, kThreads, P->smem_fwd, s>>>((const RaggedProb<R>*)P->probs, P->fwd_jobs, P->n_fwd);
+  return check_cuda(cudaGetLastError(), "ragged interp_fwd launch");
+}
+
+template <typename R, int D, int JC>
+int ragged_adj_t(const tkbn_ragged_plan_s* P, cudaStream_t s) {
+  int rc;
+  const RaggedProb<R>* probs = (const RaggedProb<R>*)P->probs;
+  if (P->n_zero > 0) {
+    const int64_t zx = P->n_zero < 152 ? P->n_zero : 152;
+    k_ragged_zero<R, D><<<dim3((unsigned)zx, 16), 256, 0, s>>>(probs, P->zero_jobs, P->n_zero);
+    if ((rc = check_cuda(cudaGetLastError(), "ragged zero launch"))) return rc;
+  }
+  if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
+    if (P->n_reg > 0) {
+      int blocks;
+      if ((rc = resident_blocks(k_ragged_adj_reg, reg_smem(), P->n_reg, &blocks))) return rc;
+      k_ragged_adj_reg<<<blocks, kThreads, reg_smem(), s>>>(probs, P->reg_jobs, P->n_reg);
+      if ((rc = check_cuda(cudaGetLastError(), "ragged interp_adj launch"))) return rc;
+    }
+  }
+  if (P->n_own > 0) {
+    int blocks;
+    if ((rc = resident_blocks(k_ragged_adj_own<R, D, JC>, P->smem_own, P->n_own, &blocks))) return rc;
+    k_ragged_adj_own<R, D, JC><<<blocks, kThreads, P->smem_own, s>>>(probs, P->own_jobs, P->n_own);
+    if ((rc = check_cuda(cudaGetLastError(), "ragged interp_adj launch"))) return rc;
+  }
+  return TKBN_OK;
+}
+
+// Calls fn.template operator()<R, D, JC>() for the plan's dtype, ndim and numpoints.
+template <typename Fn>
+int ragged_dispatch(int dtype, int ndim, int j6, Fn&& fn) {
+  auto by_d = [&](auto r) -> int {
+    using R = decltype(r);
+    switch (ndim) {
+      case 1: return j6 ? fn.template run<R, 1, 6>() : fn.template run<R, 1, 0>();
+      case 2: return j6 ? fn.template run<R, 2, 6>() : fn.template run<R, 2, 0>();
+      default: return j6 ? fn.template run<R, 3, 6>() : fn.template run<R, 3, 0>();
+    }
+  };
+  return dtype == TKBN_C64 ? by_d(float{}) : by_d(double{});
+}
+
+struct BuildFn {
+  const tkbn_ragged_problem* pr;
+  int64_t n;
+  tkbn_ragged_plan_s* P;
+  template <typename R, int D, int JC>
+  int run() const { return ragged_build<R, D, JC>(pr, n, P); }
+};
+struct FwdFn {
+  const tkbn_ragged_plan_s* P;
+  cudaStream_t s;
+  template <typename R, int D, int JC>
+  int run() const { return ragged_fwd_t<R, D, JC>(P, s); }
+};
+struct AdjFn {
+  const tkbn_ragged_plan_s* P;
+  cudaStream_t s;
+  template <typename R, int D, int JC>
+  int run() const { return ragged_adj_t<R, D, JC>(P, s); }
+};
+
+}  // namespace
+
+int ragged_plan_destroy(tkbn_ragged_plan p) {
+  if (!p) return TKBN_OK;
+  cudaFree(p->probs);
+  cudaFree(p->fwd_jobs);
+  cudaFree(p->reg_jobs);
+  cudaFree(p->own_jobs);
+  cudaFree(p->zero_jobs);
+  delete p;
+  return check_cuda(cudaGetLastError(), "ragged plan free");
+}
+
+int ragged_plan_create(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan* out) {
+  if (!pr || !out || n < 1) return set_error(TKBN_ERR_INVALID, "need at least one problem");
+  const tkbn_geometry& g0 = pr[0].geom;
+  if (g0.dtype != TKBN_C64 && g0.dtype != TKBN_C128) return set_error(TKBN_ERR_UNSUPPORTED, "unsupported dtype");
+  if (g0.ndim < 1 || g0.ndim > 3) return set_error(TKBN_ERR_UNSUPPORTED, "ndim must be 1, 2 or 3");
+  const int j6 = all_j(&g0, 6) ? 1 : 0;
+  for (int64_t q = 0; q < n; ++q) {
+    const tkbn_geometry& g = pr[q].geom;
+    if (g.dtype != g0.dtype || g.ndim != g0.ndim || (all_j(&g, 6) ? 1 : 0) != j6)
+      return set_error(TKBN_ERR_INVALID, "problem %lld: all problems need the same dtype, ndim and numpoints",
+                       (long long)q);
+    if (pr[q].points.ntraj != 1) return set_error(TKBN_ERR_INVALID, "problem %lld: ntraj must be 1", (long long)q);
+    if (pr[q].ncoil < 1) return set_error(TKBN_ERR_INVALID, "problem %lld: ncoil must be >= 1", (long long)q);
+  }
+  tkbn_ragged_plan_s* P = new (std::nothrow) tkbn_ragged_plan_s();
+  if (!P) return set_error(TKBN_ERR_INVALID, "out of host memory");
+  P->dtype = g0.dtype;
+  P->ndim = g0.ndim;
+  P->j6 = j6;
+  P->nprob = n;
+  const int rc = ragged_dispatch(P->dtype, P->ndim, j6, BuildFn{pr, n, P});
+  if (rc) {
+    ragged_plan_destroy(P);
+    return rc;
+  }
+  *out = P;
+  return TKBN_OK;
+}
+
+int ragged_interp_fwd(tkbn_ragged_plan p, cudaStream_t s) {
+  if (!p) return set_error(TKBN_ERR_INVALID, "ragged plan is null");
+  return ragged_dispatch(p->dtype, p->ndim, p->j6, FwdFn{p, s});
+}
+
+int ragged_interp_adj(tkbn_ragged_plan p, cudaStream_t s) {
+  if (!p) return set_error(TKBN_ERR_INVALID, "ragged plan is null");
+  return ragged_dispatch(p->dtype, p->ndim, p->j6, AdjFn{p, s});
 }
 
 }  // namespace tkbn_host

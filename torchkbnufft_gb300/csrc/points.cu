@@ -13,6 +13,9 @@
 
 #include <cstdarg>
 #include <cstdio>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "tkbn_common.cuh"
 #include "geo_host.cuh"
@@ -119,21 +122,25 @@ __global__ void k_tile_work(Geo<R> geo, const int32_t* __restrict__ counts, cons
   }
 }
 
-// 2D owned tiles: one warp per output tile walks the points of its source
+// 2D owned tiles: one CTA per output tile walks the points of its source
 // tiles (in source-tile order, then sorted order — the order the adjoint
-// accumulates them in) and keeps those whose footprint reaches the tile,
-// with the footprint's first row and column relative to the tile origin
-// (negative when the footprint starts in an earlier tile; periodic). The
-// first pass (voff == nullptr) counts, the second writes at voff[key].
+// accumulates them in), 1024 candidates at a time, 4 consecutive ones per
+// thread, and keeps those whose footprint reaches the tile, with the
+// footprint's first row and column relative to the tile origin (negative
+// when the footprint starts in an earlier tile; periodic). A block-wide
+// exclusive scan of the per-thread counts keeps the order. The first pass
+// (voff == nullptr) counts, the second writes at voff[key].
+constexpr int kValidThreads = 256;
 template <typename R>
-__global__ void k_tile_valid(Geo<R> geo, const int32_t* __restrict__ counts, const int32_t* __restrict__ tile_off,
-                             const R* __restrict__ tm, const int32_t* __restrict__ vals, int64_t n, int64_t M,
-                             int64_t nkeys, SrcSpan span, const int32_t* __restrict__ voff,
-                             int32_t* __restrict__ vcount, int4* __restrict__ vlist) {
-  const int lane = threadIdx.x & 31;
-  const unsigned lt_mask = (1u << lane) - 1;
-  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x / 32);
-  for (int64_t key = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; key < nkeys; key += nwarps) {
+__global__ void __launch_bounds__(kValidThreads) k_tile_valid(Geo<R> geo, const int32_t* __restrict__ counts,
+                                                              const int32_t* __restrict__ tile_off,
+                                                              const R* __restrict__ tm, const int32_t* __restrict__ vals,
+                                                              int64_t n, int64_t M, int64_t nkeys, SrcSpan span,
+                                                              const int32_t* __restrict__ voff,
+                                                              int32_t* __restrict__ vcount, int4* __restrict__ vlist) {
+  __shared__ int s_start[16], s_pre[17], s_warp[kValidThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t key = blockIdx.x; key < nkeys; key += gridDim.x) {
     const int64_t t = key / geo.ntiles;
     const int rem = (int)(key - t * geo.ntiles);
     int td[kMaxDim] = {rem / geo.ntile[1], rem % geo.ntile[1], 0};
@@ -143,19 +150,34 @@ __global__ void k_tile_valid(Geo<R> geo, const int32_t* __restrict__ counts, con
       origin[d] = td[d] * geo.T[d];
       ext[d] = min(geo.T[d], geo.K[d] - origin[d]);
     }
+    __syncthreads();  // the previous key is done with the shared lists
+    if ((int)threadIdx.x < span.ncombo) {
+      const int64_t skey = t * geo.ntiles + source_tile(geo, span, td, threadIdx.x);
+      s_start[threadIdx.x] = tile_off[skey];
+      s_pre[threadIdx.x + 1] = counts[skey];
+    }
+    if (threadIdx.x == 0) s_pre[0] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int l = 0; l < span.ncombo; ++l) s_pre[l + 1] += s_pre[l];
+    __syncthreads();
+    const int total = s_pre[span.ncombo];
     const int64_t out0 = voff ? voff[key] : 0;
     int cnt = 0;
-    for (int combo = 0; combo < span.ncombo; ++combo) {
-      const int64_t skey = t * geo.ntiles + source_tile(geo, span, td, combo);
-      const int start = tile_off[skey], num = counts[skey];
-      for (int q0 = 0; q0 < num; q0 += 32) {
-        const int q = q0 + lane;
-        bool valid = false;
-        int r[2] = {0, 0};
-        int i = 0;
-        if (q < num) {
-          i = start + q;
-          valid = true;
+    for (int q0 = 0; q0 < total; q0 += 4 * kValidThreads) {
+      bool valid[4];
+      int idx[4], ry[4], rx[4];
+      int mine = 0, l = 0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int q = q0 + 4 * (int)threadIdx.x + k;
+        valid[k] = false;
+        idx[k] = ry[k] = rx[k] = 0;
+        if (q < total) {
+          while (s_pre[l + 1] <= q) ++l;
+          const int i = s_start[l] + (q - s_pre[l]);
+          bool v = true;
+          int r[2];
 #pragma unroll
           for (int d = 0; d < 2; ++d) {
             const R f = floor(sub_rn(tm[d * n + i], geo.halfJ[d]));
@@ -163,17 +185,42 @@ __global__ void k_tile_valid(Geo<R> geo, const int32_t* __restrict__ counts, con
             const int w = fin ? wrap_cell(1 + (int)f, geo.K[d]) : 0;
             int rr = w - origin[d];
             if (rr >= geo.T[d]) rr -= geo.K[d];
-            valid = valid && fin && (rr > -geo.J[d]) && (rr < ext[d]);
+            v = v && fin && (rr > -geo.J[d]) && (rr < ext[d]);
             r[d] = rr;
           }
+          valid[k] = v;
+          idx[k] = i;
+          ry[k] = r[0];
+          rx[k] = r[1];
+          mine += v ? 1 : 0;
         }
-        const unsigned bal = __ballot_sync(0xffffffffu, valid);
-        if (voff && valid)
-          vlist[out0 + cnt + __popc(bal & lt_mask)] = make_int4(i, (int)(vals[i] - t * M), r[0], r[1]);
-        cnt += __popc(bal);
       }
+      // block-wide exclusive scan of the per-thread counts
+      int incl = mine;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (lane == 31) s_warp[warp] = incl;
+      __syncthreads();
+      int before = 0, chunk = 0;
+#pragma unroll
+      for (int w = 0; w < kValidThreads / 32; ++w) {
+        const int c = s_warp[w];
+        before += w < warp ? c : 0;
+        chunk += c;
+      }
+      if (voff) {
+        int pos = cnt + before + incl - mine;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (valid[k]) vlist[out0 + pos++] = make_int4(idx[k], (int)(vals[idx[k]] - t * M), ry[k], rx[k]);
+      }
+      cnt += chunk;
+      __syncthreads();  // s_warp is rewritten by the next chunk
     }
-    if (!voff && lane == 0) vcount[key] = cnt;
+    if (!voff && threadIdx.x == 0) vcount[key] = cnt;
   }
 }
 
@@ -248,6 +295,39 @@ int set_error(int code, const char* fmt, ...) {
 int check_cuda(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return TKBN_OK;
   return set_error(TKBN_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int resident_grid(const void* kernel, int threads, size_t smem, int64_t* blocks) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, const void*, int, size_t>, int64_t> cache;
+  // the kernel's shared-memory limit only ever grows (a launch may use any
+  // size up to it), so a cached launch shape stays valid
+  static std::map<std::pair<int, const void*>, size_t> limit;
+  int dev = 0;
+  int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc) return rc;
+  const auto key = std::make_tuple(dev, kernel, threads, smem);
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    *blocks = it->second;
+    return TKBN_OK;
+  }
+  size_t& lim = limit[std::make_pair(dev, kernel)];
+  if (smem > lim) {
+    if ((rc = check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                         "smem attribute")))
+      return rc;
+    lim = smem;
+  }
+  int sms = 0, per_sm = 0;
+  if ((rc = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"))) return rc;
+  if ((rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem), "occupancy")))
+    return rc;
+  if (per_sm < 1) return set_error(TKBN_ERR_UNSUPPORTED, "kernel cannot be resident with %zu B of shared memory", smem);
+  *blocks = (int64_t)per_sm * sms;
+  cache[key] = *blocks;
+  return TKBN_OK;
 }
 
 void default_tiles(const tkbn_geometry* g, int tile[3], int* chunk) {
@@ -334,7 +414,7 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   }
   // adjoint sub-jobs: at most adj_chunk candidates (list entries in 2D) each
   L->adj_chunk = 1024;
-  L->vlist = g->ndim == 2 && L->owned_ok;
+  L->vlist = g->ndim == 2 && L->owned_ok && L->span.ncombo <= 16;  // the 2D owned-tile kernels' source limit
   L->max_valid = L->vlist ? L->span.ncombo * L->npts_total : 0;
   L->max_subjobs = 2 * L->nkeys + (L->span.ncombo * L->npts_total + L->adj_chunk - 1) / L->adj_chunk;
   int sbits = 1;
@@ -476,14 +556,14 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
     vcount = (int32_t*)(ws + L.off_vcount);
     int32_t* voff = (int32_t*)(ws + L.off_voff);
     int4* vlist = (int4*)(ws + L.off_vlist);
-    const int wblocks = blocks_for(L.nkeys * 32);
-    k_tile_valid<R><<<wblocks, threads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys, L.span,
-                                                nullptr, vcount, vlist);
+    const int wblocks = (int)(L.nkeys < 152 * 8 ? L.nkeys : 152 * 8);
+    k_tile_valid<R><<<wblocks, kValidThreads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys,
+                                                      L.span, nullptr, vcount, vlist);
     tb = L.cub_bytes;
     if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, vcount, voff, (int)L.nkeys, s) != cudaSuccess)
       return set_error(TKBN_ERR_CUDA, "scan failed");
-    k_tile_valid<R><<<wblocks, threads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys, L.span,
-                                                voff, vcount, vlist);
+    k_tile_valid<R><<<wblocks, kValidThreads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys,
+                                                      L.span, voff, vcount, vlist);
   }
   // adjoint sub-jobs (output tiles, heavy ones split), longest first
   {

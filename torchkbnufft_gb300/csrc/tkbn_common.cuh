@@ -221,6 +221,12 @@ namespace tkbn_host {
 
 int set_error(int code, const char* fmt, ...);
 int check_cuda(cudaError_t e, const char* what);
+// CTAs of `kernel` that fit on the whole GPU at once (per-SM occupancy times
+// the SM count) with `threads` threads and `smem` bytes of dynamic shared
+// memory, raising the kernel's shared-memory limit first. Cached per
+// (device, kernel, threads, smem): after the first call it makes no CUDA
+// call, so it is cheap on every launch and safe inside stream capture.
+int resident_grid(const void* kernel, int threads, size_t smem, int64_t* blocks);
 
 // Byte layout of the sorted-point workspace.
 struct PointsLayout {
