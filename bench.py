@@ -502,6 +502,125 @@ def run_ragged(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- other configurations (reported beside the metric)
+
+
+def radial_traj(spokes: int, readout: int) -> np.ndarray:
+    """(2, spokes*readout): angles k*pi/spokes, readout linspace(-pi, pi, readout+1)[:-1]."""
+    r = np.linspace(-np.pi, np.pi, readout + 1)[:-1]
+    th = np.arange(spokes) * np.pi / spokes
+    return np.stack([(np.sin(th)[:, None] * r).reshape(-1), (np.cos(th)[:, None] * r).reshape(-1)]).astype(np.float32)
+
+
+def kooshball_traj(spokes: int, readout: int) -> np.ndarray:
+    """(3, spokes*readout): Fibonacci-sphere directions times linspace(-pi, pi, readout+1)[:-1]."""
+    i = np.arange(spokes)
+    z = 1 - 2 * (i + 0.5) / spokes
+    phi = i * np.pi * (3 - np.sqrt(5))
+    rxy = np.sqrt(1 - z * z)
+    d = np.stack([z, rxy * np.sin(phi), rxy * np.cos(phi)])
+    r = np.linspace(-np.pi, np.pi, readout + 1)[:-1]
+    return (d[:, :, None] * r[None, None, :]).reshape(3, -1).astype(np.float32)
+
+
+def spiral_traj(interleaves: int, samples: int) -> np.ndarray:
+    """(2, interleaves*samples): k_j(t) = pi t^1.5 exp(i (2 pi 16 t + 2 pi j / interleaves))."""
+    t = np.arange(samples) / samples
+    k = np.concatenate([np.pi * t ** 1.5 * np.exp(1j * (2 * np.pi * 16 * t + 2 * np.pi * j / interleaves))
+                        for j in range(interleaves)])
+    return np.stack([k.imag, k.real]).astype(np.float32)
+
+
+def smooth_maps_3d(ncoil: int, n: int, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    g = np.arange(n) - n / 2
+    z, y, x = np.meshgrid(g, g, g, indexing="ij")
+    maps = []
+    for c in range(ncoil):
+        ang = 2 * np.pi * c / ncoil + rng.uniform(0, 0.3)
+        cz, cy, cx = 0.2 * n * np.cos(2 * ang), 0.35 * n * np.sin(ang), 0.35 * n * np.cos(ang)
+        mag = np.exp(-((x - cx) ** 2 + (y - cy) ** 2 + (z - cz) ** 2) / (2 * (0.4 * n) ** 2))
+        maps.append(mag * np.exp(1j * ang))
+    maps = np.stack(maps)
+    maps /= np.sqrt(np.sum(np.abs(maps) ** 2, axis=0, keepdims=True))
+    return maps[None].astype(np.complex64)
+
+
+def run_config(args):
+    """Forward+adjoint (or, for spiral-grad, loss + backward) throughput at the
+    other configurations; one JSON line each, not the headline metric."""
+    import torch
+
+    import torchkbnufft_gb300 as tkbn
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(1000)
+    w = args.workload
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    if w == "single":
+        n, om, Bc, Cc, smaps = 256, radial_traj(402, 512), 1, 1, None
+        desc = "2D single-coil radial, image 256^2, grid 512^2, 402x512 (205824 points), batch 1"
+    elif w == "kooshball":
+        n, om, Bc, Cc = 128, kooshball_traj(20000, 256), 1, 8
+        smaps = torch.tensor(smooth_maps_3d(8, 128, 3), device=dev)
+        desc = "3D kooshball, image 128^3, grid 256^3, 8 coils, 20000x256 (5.12M points), batch 1"
+    else:
+        n, om, Bc, Cc = 256, spiral_traj(32, 2048), 8, 16
+        smaps = torch.tensor(ring_smaps(16, 256, 1, 4)[:1], device=dev)
+        desc = ("2D spiral 32x2048 (65536 points), image 256^2, grid 512^2, 16 coils, batch 8; loss "
+                "||A^H A x - x||^2, gradients w.r.t. x and ktraj")
+    nd = om.shape[0]
+    im = (n,) * nd
+    M = om.shape[1]
+    x = torch.tensor((rng.standard_normal((Bc, 1 if smaps is not None else Cc) + im)
+                      + 1j * rng.standard_normal((Bc, 1 if smaps is not None else Cc) + im)).astype(np.complex64),
+                     device=dev)
+    omega = torch.tensor(om, device=dev)
+    fwd = tkbn.KbNufft(im_size=im, device=dev)
+    adj = tkbn.KbNufftAdjoint(im_size=im, device=dev)
+    work = Bc * Cc * M
+    extra = {}
+    if w == "spiral-grad":
+        xr = x.clone().requires_grad_(True)
+        om_r = omega.clone().requires_grad_(True)
+
+        def grad_step():
+            xr.grad = None
+            om_r.grad = None
+            y = adj(fwd(xr, om_r, smaps=smaps), om_r, smaps=smaps)
+            loss = (y - xr).abs().pow(2).sum()
+            loss.backward()
+
+        with torch.no_grad():
+            fwd_ms = timed(lambda: adj(fwd(x, omega, smaps=smaps), omega, smaps=smaps), args.steps, args.warmup)
+        ms = timed(grad_step, args.steps, args.warmup)
+        extra = {"forward_AHA_ms": fwd_ms, "backward_over_forward": ms / fwd_ms,
+                 "note": "the trajectory requires grad: its layout is rebuilt every step"}
+    else:
+        with torch.no_grad():
+            ms = timed(lambda: adj(fwd(x, omega, smaps=smaps), omega, smaps=smaps), args.steps, args.warmup)
+    line = {
+        "metric": f"NU points*coils/s ({w})", "value": work / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {"workload": desc, "work_per_step": work, **extra},
+    }
+    print(json.dumps(line))
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -510,8 +629,8 @@ def main():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--ref-coils", type=int, default=4)
-    p.add_argument("--workload", default="sense", choices=["sense", "ragged"],
-                   help="sense: the metric's workload (default); ragged: 64 independent problems")
+    p.add_argument("--workload", default="sense", choices=["sense", "ragged", "single", "kooshball", "spiral-grad"],
+                   help="sense: the metric's workload (default); the others are reported beside it")
     args = p.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -519,6 +638,8 @@ def main():
         run_reference(args)
     elif args.workload == "ragged":
         run_ragged(args)
+    elif args.workload != "sense":
+        run_config(args)
     else:
         run_gpu(args)
 

@@ -74,6 +74,11 @@ extern "C" {
 #define TKBN_TABLES_CONJ_SYMMETRIC 1 /* table[J*L/2 + k] == conj(table[J*L/2 - k]) exactly, for
                                         every dim with J*L even (true for KB tables); the
                                         kernels then read only the first half of each table */
+#define TKBN_ADJ_DETERMINISTIC 2     /* layout without split output tiles: every grid cell is
+                                        accumulated by one CTA in a fixed order, so the adjoint
+                                        is bitwise repeatable (heavy tiles are not spread over
+                                        several CTAs). Must be the same in tkbn_points_build
+                                        and every call that uses the layout. */
 
 /* Operator geometry (one per KbModule). Unused dims (>= ndim) are ignored. */
 typedef struct tkbn_geometry {

@@ -205,12 +205,15 @@ def test_repeated_calls_reuse_layout():
     assert rel_l2(_np(c), op.interp(_np(x), _np(om))) < TOL64
 
 
-def test_adjoint_owned_tiles_deterministic():
+@pytest.mark.parametrize("C", [16, 5, 3, 1])
+def test_adjoint_owned_tiles_deterministic(C):
     """Grids with K >= T + J - 1 use the owned-tile adjoint; tiles that are not split
-    over several sub-jobs are accumulated without atomics, so the result is bitwise repeatable."""
+    over several sub-jobs are accumulated without atomics (with fewer than 16 coils,
+    warp groups' partial tiles are summed in a fixed order), so the result is bitwise
+    repeatable."""
     gen = torch.Generator().manual_seed(21)
     K = (160, 144)
-    y = _rand(gen, (2, 16, 30000), torch.complex64)
+    y = _rand(gen, (2, C, 30000), torch.complex64)
     om = _traj(gen, (2, 30000)).float()
     adj = tkbn().KbInterpAdjoint(im_size=K, grid_size=K, dtype=torch.complex64, device=DEV)
     a = adj(y.to(DEV), om.to(DEV))
@@ -236,3 +239,30 @@ def test_adjoint_split_heavy_tiles_match_oracle(batched):
     assert rel_l2(_np(adj(y.to(DEV), om.to(DEV))), op.interp_adj(y.numpy(), om.numpy())) < TOL64
     g = _rand(gen, (B, C) + K, torch.complex64)
     assert rel_l2(_np(fwd(g.to(DEV), om.to(DEV))), op.interp(g.numpy(), om.numpy())) < TOL64
+
+
+def test_adjoint_deterministic_layout_is_bitwise_repeatable():
+    """With torch's deterministic-algorithms setting (or deterministic=True), the layout
+    has no split output tiles, so even k-space-centre-heavy trajectories give bitwise
+    repeatable adjoints."""
+    from torchkbnufft_gb300 import _runtime
+
+    gen = torch.Generator().manual_seed(23)
+    K = (160, 144)
+    y = _rand(gen, (2, 16, 30000), torch.complex64).to(DEV)
+    om = _traj(gen, (2, 30000)).float()
+    om[..., :8000] *= 0.03
+    om = om.to(DEV)
+    adj = tkbn().KbInterpAdjoint(im_size=K, grid_size=K, dtype=torch.complex64, device=DEV)
+    torch.use_deterministic_algorithms(True)
+    try:
+        a = adj(y, om)
+        b = adj(y, om)
+    finally:
+        torch.use_deterministic_algorithms(False)
+    assert torch.equal(a, b)
+    op = O.Operator(K, K, cdtype=np.complex64)
+    assert rel_l2(_np(a), op.interp_adj(_np(y), _np(om))) < TOL64
+    lay = _runtime.points_layout(_runtime.make_geom(torch.complex64, K, K, (6, 6), (1024, 1024), (0.0, 0.0)), om,
+                                 deterministic=True)
+    assert lay.flags == 2

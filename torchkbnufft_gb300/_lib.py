@@ -40,6 +40,7 @@ class Geometry(ctypes.Structure):
 
 
 TKBN_TABLES_CONJ_SYMMETRIC = 1
+TKBN_ADJ_DETERMINISTIC = 2
 
 
 class PointsDesc(ctypes.Structure):

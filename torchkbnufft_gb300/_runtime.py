@@ -162,9 +162,14 @@ def make_geom(dtype, im_size, grid_size, numpoints, table_oversamp, n_shift) -> 
 class PointsLayout:
     """Bin-sorted trajectory (K1) in a torch-owned workspace."""
 
-    def __init__(self, geom: GeomKey, omega: torch.Tensor, tile=None, chunk: int = 0):
+    def __init__(self, geom: GeomKey, omega: torch.Tensor, tile=None, chunk: int = 0,
+                 deterministic: Optional[bool] = None):
         require_cuda(omega)
         self.geom = geom
+        if deterministic is None:
+            deterministic = torch.are_deterministic_algorithms_enabled()
+        # geometry flags every call with this layout must carry
+        self.flags = L.TKBN_ADJ_DETERMINISTIC if deterministic else 0
         self.device = omega.device
         self.ntraj = 1 if omega.ndim == 2 else omega.shape[0]
         self.npts = omega.shape[-1]
@@ -175,7 +180,7 @@ class PointsLayout:
             for d, t in enumerate(tile):
                 self.desc.tile[d] = int(t)
         self.desc.chunk = int(chunk)
-        g = geom_struct(geom)
+        g = geom_struct(geom, self.flags)
         nbytes = ctypes.c_size_t(0)
         L.check(L.lib().tkbn_points_workspace_size(ctypes.byref(g), ctypes.byref(self.desc), ctypes.byref(nbytes)))
         self.nbytes = int(nbytes.value)
@@ -192,16 +197,21 @@ _layout_cache: "collections.OrderedDict" = collections.OrderedDict()
 _LAYOUT_CACHE_MAX = 128
 
 
-def points_layout(geom: GeomKey, omega: torch.Tensor, tile=None, chunk: int = 0) -> PointsLayout:
+def points_layout(geom: GeomKey, omega: torch.Tensor, tile=None, chunk: int = 0,
+                  deterministic: Optional[bool] = None) -> PointsLayout:
+    """Cached layout of omega. ``deterministic`` (default: torch's deterministic-algorithms
+    setting) builds it without split adjoint tiles, so adjoints are bitwise repeatable."""
+    if deterministic is None:
+        deterministic = torch.are_deterministic_algorithms_enabled()
     base = omega._base if omega._base is not None else omega
     key = (id(base), omega.data_ptr(), omega._version, tuple(omega.shape), tuple(omega.stride()), omega.dtype,
-           geom, tuple(tile) if tile else None, chunk, omega.device)
+           geom, tuple(tile) if tile else None, chunk, omega.device, bool(deterministic))
     with _lock:
         hit = _layout_cache.get(key)
         if hit is not None and hit[0]() is base:
             _layout_cache.move_to_end(key)
             return hit[1]
-        lay = PointsLayout(geom, omega, tile, chunk)
+        lay = PointsLayout(geom, omega, tile, chunk, deterministic)
         _layout_cache[key] = (weakref.ref(base), lay)
         while len(_layout_cache) > _LAYOUT_CACHE_MAX:
             _layout_cache.popitem(last=False)
@@ -356,7 +366,7 @@ def interp_fwd(geom: GeomKey, lay: PointsLayout, tables, grid: torch.Tensor) -> 
     B, C = grid.shape[:2]
     kdata = torch.empty((B, C, lay.npts), dtype=grid.dtype, device=dev)
     tp, keep, fl = table_ptrs(tables, grid.dtype)
-    L.check(L.lib().tkbn_interp_fwd(ctypes.byref(geom_struct(geom, fl)), ctypes.byref(lay.desc),
+    L.check(L.lib().tkbn_interp_fwd(ctypes.byref(geom_struct(geom, fl | lay.flags)), ctypes.byref(lay.desc),
                                     lay.workspace.data_ptr(), tp, grid.data_ptr(), B, C, kdata.data_ptr(),
                                     stream_handle(dev)))
     return kdata
@@ -369,7 +379,7 @@ def interp_adj(geom: GeomKey, lay: PointsLayout, tables, kdata: torch.Tensor) ->
     B, C = kdata.shape[:2]
     grid = torch.empty((B, C) + geom.grid_size, dtype=kdata.dtype, device=dev)
     tp, keep, fl = table_ptrs(tables, kdata.dtype)
-    L.check(L.lib().tkbn_interp_adj(ctypes.byref(geom_struct(geom, fl)), ctypes.byref(lay.desc),
+    L.check(L.lib().tkbn_interp_adj(ctypes.byref(geom_struct(geom, fl | lay.flags)), ctypes.byref(lay.desc),
                                     lay.workspace.data_ptr(), tp, kdata.data_ptr(), B, C, grid.data_ptr(),
                                     stream_handle(dev)))
     return grid
@@ -387,7 +397,7 @@ def interp_grad_omega(geom: GeomKey, lay: PointsLayout, tables, grid: torch.Tens
     dtabs = derivative_tables(tabs, geom.table_oversamp)
     tp, keep, fl = table_ptrs(tabs, grid.dtype)
     dp, keep2, _ = table_ptrs(dtabs, grid.dtype)
-    L.check(L.lib().tkbn_interp_grad_omega(ctypes.byref(geom_struct(geom)), ctypes.byref(lay.desc),
+    L.check(L.lib().tkbn_interp_grad_omega(ctypes.byref(geom_struct(geom, lay.flags)), ctypes.byref(lay.desc),
                                            lay.workspace.data_ptr(), tp, dp, grid.data_ptr(), v.data_ptr(), B, C,
                                            grad.data_ptr(), stream_handle(dev)))
     return grad
@@ -451,7 +461,8 @@ def nufft_fwd(geom: GeomKey, lay: PointsLayout, tables, scaling, image, smaps, n
     grid = torch.empty((B, C) + geom.grid_size, dtype=image.dtype, device=dev)
     kdata = torch.empty((B, C, lay.npts), dtype=image.dtype, device=dev)
     tp, keep, fl = table_ptrs(tables, image.dtype)
-    L.check(L.lib().tkbn_nufft_fwd(ctypes.byref(geom_struct(geom, fl)), ctypes.byref(lay.desc), lay.workspace.data_ptr(),
+    L.check(L.lib().tkbn_nufft_fwd(ctypes.byref(geom_struct(geom, fl | lay.flags)), ctypes.byref(lay.desc),
+                                   lay.workspace.data_ptr(),
                                    plan.handle, tp, _c(scaling), image.data_ptr(), _c(smaps), sb, B, C,
                                    norm_code(norm), grid.data_ptr(), kdata.data_ptr(), stream_handle(dev)))
     return kdata
@@ -473,7 +484,8 @@ def nufft_adj(geom: GeomKey, lay: PointsLayout, tables, scaling, kdata, smaps, n
     co = 1 if smaps is not None else C
     image = torch.empty((B, co) + geom.im_size, dtype=kdata.dtype, device=dev)
     tp, keep, fl = table_ptrs(tables, kdata.dtype)
-    L.check(L.lib().tkbn_nufft_adj(ctypes.byref(geom_struct(geom, fl)), ctypes.byref(lay.desc), lay.workspace.data_ptr(),
+    L.check(L.lib().tkbn_nufft_adj(ctypes.byref(geom_struct(geom, fl | lay.flags)), ctypes.byref(lay.desc),
+                                   lay.workspace.data_ptr(),
                                    plan.handle, tp, _c(scaling), kdata.data_ptr(), _c(smaps), sb, B, C,
                                    norm_code(norm), grid.data_ptr(), image.data_ptr(), stream_handle(dev)))
     return image

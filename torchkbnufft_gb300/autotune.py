@@ -21,10 +21,12 @@ import torch
 
 from . import _runtime as R
 
-# candidate (tile, chunk) per dimension count; the first entry is the library default
+# candidate (tile, chunk) per dimension count; the first entry is the library default.
+# 2D keeps the 16 x 14 tile of the register-accumulator adjoint (any other tile
+# falls back to the shared-memory adjoint) and tunes the gather's work-item size.
 CANDIDATES = {
     1: [((128,), 1024), ((64,), 1024), ((256,), 1024), ((128,), 2048)],
-    2: [((16, 14), 1024), ((16, 14), 512), ((16, 14), 2048), ((16, 16), 1024), ((8, 14), 1024), ((32, 14), 1024)],
+    2: [((16, 14), 1024), ((16, 14), 512), ((16, 14), 2048), ((16, 14), 256)],
     3: [((4, 4, 4), 1024), ((4, 4, 8), 1024), ((4, 8, 8), 1024), ((8, 8, 8), 1024), ((4, 4, 4), 2048)],
 }
 

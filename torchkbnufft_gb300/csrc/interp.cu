@@ -919,16 +919,27 @@ __device__ __forceinline__ void reg_add_point(int lx, float2 (&racc)[kRegTileX],
 
 // vec_ok: the grid pointer is 16-byte aligned and K1 is even, so every
 // tile row starts 16-byte aligned and pairs of cells go out as one float4.
+// CC coils per job (2, 4, 8 or 16; one coil runs as CC = 2 with the second
+// masked). A warp covers RPW = 32 / CC tile rows with lanes (coil, row); WPT =
+// 16 / RPW warps cover the tile, and the kWarps / WPT groups of warps take
+// the staged points in turn (point p goes to group p mod NG). With more than
+// one group, the groups' partial tiles are summed in a fixed order through
+// shared memory before the write-out, so results stay deterministic.
+template <int CC>
 __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& a, const float* __restrict__ tm,
                                         const float2* __restrict__ ph, const float2* __restrict__ kdata,
                                         float2* __restrict__ grid, int vec_ok, int64_t job, unsigned char* smem_raw) {
   constexpr int D = 2, NJ = 6;
+  constexpr int RPW = 32 / CC, WPT = kRegTileY / RPW, NG = kWarps / WPT;
+  static_assert(CC >= 2 && CC <= 16 && (CC & (CC - 1)) == 0, "coils per job");
   float2* sfac = reinterpret_cast<float2*>(smem_raw);  // [kNBR][12]: conj y factors, conj x factors
-  float2* sv = sfac + kNBR * D * NJ;                   // [kNBR][16] conj(phase) * kdata per coil
-  int2* sloc = reinterpret_cast<int2*>(sv + kNBR * kRegCoils);  // [kNBR] footprint start (y, x) in the tile
+  float2* sv = sfac + kNBR * D * NJ;                   // [kNBR][CC] conj(phase) * kdata per coil
+  int2* sloc = reinterpret_cast<int2*>(sv + kNBR * CC);  // [kNBR] footprint start (y, x) in the tile
+  float2* part = reinterpret_cast<float2*>(smem_raw);    // [NG][16][14][CC] partial tiles (after the batches)
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int c = lane & 15, myrow = 2 * warp + (lane >> 4);
+  const int c = lane % CC, grp = warp / WPT;
+  const int myrow = (warp % WPT) * RPW + lane / CC;
   const int64_t per_sj = a.nbpt * a.ncc;
 
   {
@@ -940,8 +951,8 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
     int td[kMaxDim], origin[kMaxDim], ext[kMaxDim];
     own_tile_geometry<float, D>(geo, it.key, &t, td, origin, ext);
     const int64_t b = a.ntraj == 1 ? bb : t;
-    const int c0 = cc * kRegCoils;
-    const int ncl = (int)min((int64_t)kRegCoils, a.C - c0);
+    const int c0 = cc * a.Cc;
+    const int ncl = (int)min((int64_t)min(CC, a.Cc), a.C - c0);
     const bool rowok = myrow < ext[0];
     const int64_t vbase = a.voff[it.key];
     float2 racc[kRegTileX];
@@ -970,8 +981,8 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
           out[j] = cconj<float>(table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half));
       }
 #pragma unroll 4
-      for (int e = threadIdx.x; e < nv * kRegCoils; e += kThreads) {
-        const int pt = e >> 4, cl = e & 15;
+      for (int e = threadIdx.x; e < nv * CC; e += kThreads) {
+        const int pt = e / CC, cl = e % CC;
         float2 v = make_float2(0.f, 0.f);
         if (cl < ncl) {
           const int4 ent = ents[pt];
@@ -980,13 +991,13 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
         sv[e] = v;
       }
       __syncthreads();
-      // B: each warp applies the staged points that touch its two rows
-      const int r_lo = 2 * warp, r_hi = min(2 * warp + 2, ext[0]);
+      // B: each warp applies the staged points of its group that touch its rows
+      const int r_lo = (warp % WPT) * RPW, r_hi = min(r_lo + RPW, ext[0]);
 #pragma unroll 1
       for (int h = 0; h < kNBR / 32; ++h) {
         const int p = h * 32 + lane;
         bool tch = false;
-        if (p < nv) {
+        if (p < nv && (NG == 1 || p % NG == grp)) {
           const int ly = sloc[p].x;
           tch = max(r_lo, ly) < min(r_hi, ly + NJ);
         }
@@ -996,7 +1007,7 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
           const int jy = myrow - loc.x;
           if (rowok && (unsigned)jy < (unsigned)NJ) {
             const float2* fp = sfac + pt * (D * NJ);
-            const float2 vy = cmul<float>(sv[pt * kRegCoils + c], fp[jy]);
+            const float2 vy = cmul<float>(sv[pt * CC + c], fp[jy]);
             const float4* fx4 = reinterpret_cast<const float4*>(fp + NJ);
             const float4 f01 = fx4[0], f23 = fx4[1], f45 = fx4[2];
             const float2 fx[6] = {make_float2(f01.x, f01.y), make_float2(f01.z, f01.w), make_float2(f23.x, f23.y),
@@ -1008,33 +1019,62 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
       }
       __syncthreads();
     }
-    // C: write this lane's row of its coil plane; split tiles add atomically
-    if (rowok && c < ncl) {
-      float2* dst = grid + (b * a.C + c0 + c) * a.gtot + (int64_t)(origin[0] + myrow) * geo.K[1] + origin[1];
-      const int ex = ext[1];
-      if (it.pad == 0) {
-        if (vec_ok) {
+    const int ex = ext[1];
+    if (NG == 1) {
+      // C: write this lane's row of its coil plane; split tiles add atomically
+      if (rowok && c < ncl) {
+        float2* dst = grid + (b * a.C + c0 + c) * a.gtot + (int64_t)(origin[0] + myrow) * geo.K[1] + origin[1];
+        if (it.pad == 0) {
+          if (vec_ok) {
 #pragma unroll
-          for (int x = 0; x < kRegTileX; x += 2) {
-            if (x + 1 < ex)
-              *reinterpret_cast<float4*>(dst + x) = make_float4(racc[x].x, racc[x].y, racc[x + 1].x, racc[x + 1].y);
-            else if (x < ex)
-              dst[x] = racc[x];
+            for (int x = 0; x < kRegTileX; x += 2) {
+              if (x + 1 < ex)
+                *reinterpret_cast<float4*>(dst + x) = make_float4(racc[x].x, racc[x].y, racc[x + 1].x, racc[x + 1].y);
+              else if (x < ex)
+                dst[x] = racc[x];
+            }
+          } else {
+#pragma unroll
+            for (int x = 0; x < kRegTileX; ++x)
+              if (x < ex) dst[x] = racc[x];
           }
         } else {
 #pragma unroll
           for (int x = 0; x < kRegTileX; ++x)
-            if (x < ex) dst[x] = racc[x];
+            if (x < ex) atomic_add_global(dst + x, racc[x]);
         }
-      } else {
-#pragma unroll
-        for (int x = 0; x < kRegTileX; ++x)
-          if (x < ex) atomic_add_global(dst + x, racc[x]);
       }
+    } else {
+      // C: the groups' partial tiles meet in shared memory (the staging
+      // buffers are free after the last batch's barrier); thread e sums
+      // element e (coil-major, then row, then column) over the groups in order
+      constexpr int TE = kRegTileY * kRegTileX * CC;
+#pragma unroll
+      for (int x = 0; x < kRegTileX; ++x) part[grp * TE + (c * kRegTileY + myrow) * kRegTileX + x] = racc[x];
+      __syncthreads();
+      for (int e = threadIdx.x; e < TE; e += kThreads) {
+        const int cl = e / (kRegTileY * kRegTileX);
+        const int rr = (e / kRegTileX) % kRegTileY, x = e % kRegTileX;
+        if (cl >= ncl || rr >= ext[0] || x >= ex) continue;
+        float2 v = part[e];
+#pragma unroll
+        for (int q = 1; q < NG; ++q) {
+          const float2 w = part[q * TE + e];
+          v.x += w.x;
+          v.y += w.y;
+        }
+        float2* dst = grid + (b * a.C + c0 + cl) * a.gtot + (int64_t)(origin[0] + rr) * geo.K[1] + origin[1] + x;
+        if (it.pad == 0)
+          *dst = v;
+        else
+          atomic_add_global(dst, v);
+      }
+      __syncthreads();  // the next job's staging reuses the buffer
     }
   }
 }
 
+template <int CC>
 __global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg(Geo<float> geo, OwnLaunch a,
                                                                 const float* __restrict__ tm,
                                                                 const float2* __restrict__ ph,
@@ -1043,7 +1083,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg(Geo<float> geo, 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int64_t njobs = a.hdr[1] * a.nbpt * a.ncc;
   for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
-    reg_job(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw);
+    reg_job<CC>(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw);
 }
 
 template <typename R>
@@ -1271,6 +1311,7 @@ __global__ void k_ragged_zero(const RaggedProb<R>* __restrict__ probs, const int
   }
 }
 
+template <int CC>
 __global__ void __launch_bounds__(kThreads, 3) k_ragged_adj_reg(const RaggedProb<float>* __restrict__ probs,
                                                                 const int2* __restrict__ jobs, int64_t njobs) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1284,7 +1325,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ragged_adj_reg(const RaggedProb
       __syncthreads();
       cur = pj.x;
     }
-    reg_job(sp.geo, sp.o, sp.tm, sp.ph, sp.kdata, sp.grid, sp.vec_ok, pj.y, smem_raw);
+    reg_job<CC>(sp.geo, sp.o, sp.tm, sp.ph, sp.kdata, sp.grid, sp.vec_ok, pj.y, smem_raw);
   }
 }
 
@@ -1490,16 +1531,33 @@ static size_t own_smem(const OwnLaunch& o) {
          sizeof(int) * ((size_t)kNB * D + kNB + 2 * max_combo<D>() + 1 + kNB / 32);
 }
 
-// The register adjoint applies: 2D complex64, J = 6, 16-coil jobs, 16 x 14
-// tiles with per-tile point lists.
+// The register adjoint applies: 2D complex64, J = 6, 16 x 14 tiles with
+// per-tile point lists (any coil count; CC = max(2, coils per job)).
 template <typename R, int D, int JC>
 static bool reg_eligible(const InterpPlan& ip, const OwnLaunch& o) {
-  return std::is_same<R, float>::value && D == 2 && JC == 6 && o.vlist && o.Cc == kRegCoils &&
+  return std::is_same<R, float>::value && D == 2 && JC == 6 && o.vlist && o.Cc <= kRegCoils &&
          ip.L.tile[0] == kRegTileY && ip.L.tile[1] == kRegTileX;
 }
 
-static size_t reg_smem() {
-  return (size_t)kNBR * (2 * 6 + kRegCoils) * sizeof(float2) + (size_t)kNBR * sizeof(int2);
+static int reg_cc(int Cc) { return Cc < 2 ? 2 : Cc; }
+
+// Staging of a batch, or (more than one point group) the groups' partial tiles.
+static size_t reg_smem(int CC) {
+  const size_t staging = (size_t)kNBR * (2 * 6 + CC) * sizeof(float2) + (size_t)kNBR * sizeof(int2);
+  const int ng = kWarps / (kRegTileY / (32 / CC));
+  const size_t partials = ng > 1 ? (size_t)ng * kRegTileY * kRegTileX * CC * sizeof(float2) : 0;
+  return staging > partials ? staging : partials;
+}
+
+// Calls fn(std::integral_constant<int, CC>) for CC in {2, 4, 8, 16}.
+template <typename Fn>
+static int with_cc(int CC, Fn&& fn) {
+  switch (CC) {
+    case 2: return fn(std::integral_constant<int, 2>{});
+    case 4: return fn(std::integral_constant<int, 4>{});
+    case 8: return fn(std::integral_constant<int, 8>{});
+    default: return fn(std::integral_constant<int, 16>{});
+  }
 }
 
 template <typename R, int D, int JC>
@@ -1521,15 +1579,18 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
   }
   if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
     if (reg_eligible<R, D, JC>(ip, o)) {
-      const size_t rsmem = reg_smem();
-      int blocks;
-      int rc = resident_blocks(k_interp_adj_reg, rsmem, max_jobs, &blocks);
-      if (rc) return rc;
-      const int vec_ok = ((uintptr_t)grid % 16 == 0) && (geo.K[1] % 2 == 0);
-      k_interp_adj_reg<<<blocks, kThreads, rsmem, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
-                                                       (const float2*)(ws + ip.L.off_phase), (const float2*)kdata,
-                                                       (float2*)grid, vec_ok);
-      return check_cuda(cudaGetLastError(), "interp_adj launch");
+      return with_cc(reg_cc(o.Cc), [&](auto ccv) {
+        constexpr int CC = decltype(ccv)::value;
+        const size_t rsmem = reg_smem(CC);
+        int blocks;
+        int rc = resident_blocks(k_interp_adj_reg<CC>, rsmem, max_jobs, &blocks);
+        if (rc) return rc;
+        const int vec_ok = ((uintptr_t)grid % 16 == 0) && (geo.K[1] % 2 == 0);
+        k_interp_adj_reg<CC><<<blocks, kThreads, rsmem, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
+                                                             (const float2*)(ws + ip.L.off_phase),
+                                                             (const float2*)kdata, (float2*)grid, vec_ok);
+        return check_cuda(cudaGetLastError(), "interp_adj launch");
+      });
     }
   }
   const bool fast = D == 2 && JC == 6 && o.Cc == 16 && ip.L.tile[0] == 2 * kWarps;
@@ -1649,8 +1710,8 @@ struct tkbn_ragged_plan_s {
   int dtype, ndim, j6;
   int64_t nprob;
   void* probs;  // RaggedProb<R>[nprob] on the device
-  int2 *fwd_jobs, *reg_jobs, *own_jobs, *zero_jobs;
-  int64_t n_fwd, n_reg, n_own, n_zero;
+  int2 *fwd_jobs, *reg_jobs[4], *own_jobs, *zero_jobs;  // reg_jobs[k]: jobs of 2 << k coils per job
+  int64_t n_fwd, n_reg[4], n_own, n_zero;
   size_t smem_fwd, smem_own;
 };
 
@@ -1682,7 +1743,7 @@ int upload_jobs(const std::vector<JobRec>& v, int2** dev) {
 template <typename R, int D, int JC>
 int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P) {
   std::vector<RaggedProb<R>> desc((size_t)n);
-  std::vector<JobRec> fwd, reg, own, zero;
+  std::vector<JobRec> fwd, reg[4], own, zero;
   P->smem_fwd = 0;
   P->smem_own = 0;
   for (int64_t q = 0; q < n; ++q) {
@@ -1729,26 +1790,30 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
       if (sm > 220 * 1024) return set_error(TKBN_ERR_UNSUPPORTED, "adjoint tile needs %zu bytes of shared memory", sm);
       if (sm > P->smem_own) P->smem_own = sm;
     }
+    const int rk = reg_cc(d.o.Cc) == 2 ? 0 : (reg_cc(d.o.Cc) == 4 ? 1 : (reg_cc(d.o.Cc) == 8 ? 2 : 3));
     for (int64_t j = 0; j < hdr[1] * ip.a.ncc; ++j) {
       const Item& it = sj[(size_t)(j / ip.a.ncc)];
-      (use_reg ? reg : own).push_back({it.len, (int)q, (int)j});
+      (use_reg ? reg[rk] : own).push_back({it.len, (int)q, (int)j});
     }
     for (int64_t j = 0; j < hdr[1]; ++j)
       if (sj[(size_t)j].pad && sj[(size_t)j].start == 0) zero.push_back({sj[(size_t)j].len, (int)q, (int)j});
   }
   lpt_sort(fwd);
-  lpt_sort(reg);
+  for (auto& v : reg) lpt_sort(v);
   lpt_sort(own);
   int rc = check_cuda(cudaMalloc(&P->probs, desc.size() * sizeof(RaggedProb<R>)), "ragged descriptors");
   if (rc) return rc;
   if ((rc = check_cuda(cudaMemcpy(P->probs, desc.data(), desc.size() * sizeof(RaggedProb<R>), cudaMemcpyHostToDevice),
                        "ragged descriptor upload")))
     return rc;
-  if ((rc = upload_jobs(fwd, &P->fwd_jobs)) || (rc = upload_jobs(reg, &P->reg_jobs)) ||
-      (rc = upload_jobs(own, &P->own_jobs)) || (rc = upload_jobs(zero, &P->zero_jobs)))
+  if ((rc = upload_jobs(fwd, &P->fwd_jobs)) || (rc = upload_jobs(own, &P->own_jobs)) ||
+      (rc = upload_jobs(zero, &P->zero_jobs)))
     return rc;
+  for (int k = 0; k < 4; ++k) {
+    if ((rc = upload_jobs(reg[k], &P->reg_jobs[k]))) return rc;
+    P->n_reg[k] = (int64_t)reg[k].size();
+  }
   P->n_fwd = (int64_t)fwd.size();
-  P->n_reg = (int64_t)reg.size();
   P->n_own = (int64_t)own.size();
   P->n_zero = (int64_t)zero.size();
   return TKBN_OK;
@@ -1774,11 +1839,17 @@ int ragged_adj_t(const tkbn_ragged_plan_s* P, cudaStream_t s) {
     if ((rc = check_cuda(cudaGetLastError(), "ragged zero launch"))) return rc;
   }
   if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
-    if (P->n_reg > 0) {
-      int blocks;
-      if ((rc = resident_blocks(k_ragged_adj_reg, reg_smem(), P->n_reg, &blocks))) return rc;
-      k_ragged_adj_reg<<<blocks, kThreads, reg_smem(), s>>>(probs, P->reg_jobs, P->n_reg);
-      if ((rc = check_cuda(cudaGetLastError(), "ragged interp_adj launch"))) return rc;
+    for (int k = 0; k < 4; ++k) {
+      if (P->n_reg[k] == 0) continue;
+      rc = with_cc(2 << k, [&](auto ccv) {
+        constexpr int CC = decltype(ccv)::value;
+        int blocks;
+        int r = resident_blocks(k_ragged_adj_reg<CC>, reg_smem(CC), P->n_reg[k], &blocks);
+        if (r) return r;
+        k_ragged_adj_reg<CC><<<blocks, kThreads, reg_smem(CC), s>>>(probs, P->reg_jobs[k], P->n_reg[k]);
+        return check_cuda(cudaGetLastError(), "ragged interp_adj launch");
+      });
+      if (rc) return rc;
     }
   }
   if (P->n_own > 0) {
@@ -1830,7 +1901,7 @@ int ragged_plan_destroy(tkbn_ragged_plan p) {
   if (!p) return TKBN_OK;
   cudaFree(p->probs);
   cudaFree(p->fwd_jobs);
-  cudaFree(p->reg_jobs);
+  for (int k = 0; k < 4; ++k) cudaFree(p->reg_jobs[k]);
   cudaFree(p->own_jobs);
   cudaFree(p->zero_jobs);
   delete p;

@@ -413,7 +413,7 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
     if (g->grid_size[d] < (int64_t)T + g->numpoints[d] - 1) L->owned_ok = false;
   }
   // adjoint sub-jobs: at most adj_chunk candidates (list entries in 2D) each
-  L->adj_chunk = 1024;
+  L->adj_chunk = (g->flags & TKBN_ADJ_DETERMINISTIC) ? (1 << 30) : 1024;
   L->vlist = g->ndim == 2 && L->owned_ok && L->span.ncombo <= 16;  // the 2D owned-tile kernels' source limit
   L->max_valid = L->vlist ? L->span.ncombo * L->npts_total : 0;
   L->max_subjobs = 2 * L->nkeys + (L->span.ncombo * L->npts_total + L->adj_chunk - 1) / L->adj_chunk;

@@ -118,7 +118,7 @@ class RaggedNufft:
         for p in range(n):
             k = self.class_of[p]
             g = L.Geometry.from_buffer_copy(k.gstruct)
-            g.flags = k.flags
+            g.flags = k.flags | self.layouts[p].flags
             arr[p].geom = g
             arr[p].points = self.layouts[p].desc
             arr[p].workspace = self.layouts[p].workspace.data_ptr()
