@@ -81,8 +81,12 @@ def tune_layout(geom: R.GeomKey, omega: torch.Tensor, tables: Sequence[torch.Ten
         times = []
         for tile, chunk in cands:
             tile = tuple(min(int(t), int(k)) for t, k in zip(tile, geom.grid_size))
-            times.append((_time_candidate(geom, omega, tables, ncoil, tile, chunk, reps), (tile, chunk)))
-        best = min(times, key=lambda x: x[0])[1]
+            try:
+                times.append((_time_candidate(geom, omega, tables, ncoil, tile, chunk, reps), (tile, chunk)))
+            except (TypeError, ValueError):  # e.g. a patch that does not fit shared memory
+                continue
+        if times:
+            best = min(times, key=lambda x: x[0])[1]
     with _lock:
         _best[key] = best
     return best
