@@ -438,6 +438,137 @@ __device__ __forceinline__ void fwd_job(const Geo<R>& geo, const Launch& a, cons
   }
 }
 
+// ---------------------------------------------------------------- K3, coil pairs
+// Gather for 2D complex64, J = 6, CC coils per job (2, 4, 8 or 16): the tile
+// patch is stored coil-fastest ([cell][CC]), so a lane reads two coils of a
+// cell with one 16-byte load and the point's per-lane work (coordinates,
+// table factors, addressing) is shared by two coils. Lanes are (point slot,
+// coil pair): 64 / CC points per warp.
+template <int CC>
+__device__ __forceinline__ void load_patch_pairs(const Geo<float>& geo, const float2* __restrict__ grid,
+                                                 int64_t plane0, int64_t gtot, int ncl, const int* origin,
+                                                 float2* patch) {
+  const int PX = geo.P[1], PY = geo.P[0], KX = geo.K[1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int rr = warp; rr < PY; rr += kWarps) {
+    const int64_t rbase = patch_row_base<float, 2>(geo, rr, origin);
+    float2* dst = patch + rr * PX * CC;
+    for (int idx = lane; idx < PX * CC; idx += 32) {
+      const int x = idx / CC, c = idx % CC;
+      if (c < ncl)
+        cp_async_elem(dst + idx, grid + (plane0 + c) * gtot + rbase + wrap_cell(origin[1] + x, KX));
+      else
+        dst[idx] = make_float2(0.f, 0.f);
+    }
+  }
+  cp_async_wait_all();
+}
+
+template <int CC>
+__device__ __forceinline__ void fwd_job_pairs(const Geo<float>& geo, const Launch& a, const float* __restrict__ tm,
+                                              const float2* __restrict__ ph, const float2* __restrict__ grid,
+                                              float2* __restrict__ kdata, int64_t job, int64_t nitems,
+                                              float2* patch) {
+  constexpr int D = 2, NJ = 6, LPP = CC / 2, PPW = 32 / LPP;  // lanes per point, points per warp
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int PX = geo.P[1];
+  const int cells = geo.P[0] * PX;
+  float2* scr = patch + cells * CC + warp * (PPW * D * NJ);
+  const int k = lane % LPP;       // coil pair: coils 2k, 2k+1 of the chunk
+  const int pslot = lane / LPP;   // point slot in the warp
+  float2* pscr = scr + pslot * (D * NJ);
+  Item it;
+  JobCtx jc;
+  next_job<float>(geo, a, job, nitems, &it, &jc);
+  __syncthreads();
+  load_patch_pairs<CC>(geo, grid, jc.b * a.C + jc.c0, a.gtot, jc.ncl, jc.origin, patch);
+  __syncthreads();
+  constexpr int PPB = PPW * kWarps;
+  const int nrounds = (it.len + PPB - 1) / PPB;
+  int64_t i_next = it.start + min(warp * PPW + pslot, it.len - 1);
+  float tm_next[D];
+  int32_t val_next = a.vals[i_next];
+  float2 ph_next = ph[i_next];
+#pragma unroll
+  for (int d = 0; d < D; ++d) tm_next[d] = tm[d * a.n + i_next];
+  for (int r = 0; r < nrounds; ++r) {
+    const int s = r * PPB + warp * PPW + pslot;
+    const bool active = s < it.len;
+    float tmv[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) tmv[d] = tm_next[d];
+    const int32_t val = val_next;
+    const float2 phv = ph_next;
+    if (r + 1 < nrounds) {
+      i_next = it.start + min(s + PPB, it.len - 1);
+      val_next = a.vals[i_next];
+      ph_next = ph[i_next];
+#pragma unroll
+      for (int d = 0; d < D; ++d) tm_next[d] = tm[d * a.n + i_next];
+    }
+    int base[D], local[D];
+    const bool ok = point_base_at<float, D>(geo, tmv, jc.origin, base, local);
+    // the point's D*NJ table factors, split over its LPP lanes, exchanged in scratch
+#pragma unroll
+    for (int f = k; f < D * NJ; f += LPP) {
+      const int d = f / NJ, j = f % NJ;
+      const int kb = table_bin<float>(d == 0 ? tmv[0] : tmv[1], (d == 0 ? base[0] : base[1]) + j,
+                                      sel<float, D>(geo.Lr, d), sel<int, D>(geo.center, d), sel<int, D>(geo.tmax, d));
+      pscr[f] = table_entry<float>(sel<const float2*, D>(geo.tab, d), kb, sel<int, D>(geo.center, d),
+                                   sel<bool, D>(geo.half, d));
+    }
+    __syncwarp();
+    float2 hy[NJ], hx[NJ];
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      hy[j] = pscr[j];
+      hx[j] = pscr[NJ + j];
+    }
+    __syncwarp();
+    if (active && 2 * k < jc.ncl) {
+      const int64_t m = val - jc.t * a.M;
+      float2 y0, y1;
+      if (ok) {
+        float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
+        const float4* prow = reinterpret_cast<const float4*>(patch + (local[0] * PX + local[1]) * CC) + k;
+#pragma unroll
+        for (int jy = 0; jy < NJ; ++jy) {
+          float2 r0 = make_float2(0.f, 0.f), r1 = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int jx = 0; jx < NJ; ++jx) {
+            const float4 q = prow[(jy * PX + jx) * LPP];
+            r0 = cfma<float>(hx[jx], make_float2(q.x, q.y), r0);
+            r1 = cfma<float>(hx[jx], make_float2(q.z, q.w), r1);
+          }
+          acc0 = cfma<float>(hy[jy], r0, acc0);
+          acc1 = cfma<float>(hy[jy], r1, acc1);
+        }
+        y0 = cmul<float>(acc0, phv);
+        y1 = cmul<float>(acc1, phv);
+      } else {
+        y0 = y1 = make_float2(NAN, NAN);
+      }
+      float2* out = kdata + (jc.b * a.C + jc.c0 + 2 * k) * a.M + m;
+      out[0] = y0;
+      if (2 * k + 1 < jc.ncl) out[a.M] = y1;
+    }
+    if (active && !ok && k == 0) atomicOr(&g_status, kStatusNonFinite | kStatusOutsidePatch);
+  }
+}
+
+template <int CC>
+__global__ void __launch_bounds__(kThreads) k_interp_fwd_pairs(Geo<float> geo, Launch a, const float* __restrict__ tm,
+                                                               const float2* __restrict__ ph,
+                                                               const float2* __restrict__ grid,
+                                                               float2* __restrict__ kdata) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* patch = reinterpret_cast<float2*>(smem_raw);
+  const int64_t nitems = a.hdr[0];
+  const int64_t njobs = nitems * a.nbpt * a.ncc;
+  for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
+    fwd_job_pairs<CC>(geo, a, tm, ph, grid, kdata, job, nitems, patch);
+}
+
 template <typename R, int D, int JC>
 __global__ void __launch_bounds__(kThreads) k_interp_fwd(Geo<R> geo, Launch a, const R* __restrict__ tm,
                                                          const cplx<R>* __restrict__ ph,
@@ -1111,11 +1242,12 @@ __device__ __forceinline__ void lerp_tables(const Geo<R>& geo, int d, R tm, int 
 // d tm_d / d omega_d = 1 / gam_d and d phase / d omega_d = i n_shift_d phase.
 // Uses the patch staging of the forward; one lane per (point, coil), coils
 // reduced with warp shuffles, batches with atomics.
-template <typename R, int D>
+template <typename R, int D, int JC>
 __global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, const R* __restrict__ tm,
                                                           const cplx<R>* __restrict__ ph,
                                                           const cplx<R>* __restrict__ grid,
                                                           const cplx<R>* __restrict__ v, R* __restrict__ grad) {
+  constexpr int NJ = NJOf<JC>::N;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* patch = reinterpret_cast<cplx<R>*>(smem_raw);
   const int64_t nitems = a.hdr[0];
@@ -1124,6 +1256,10 @@ __global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, 
   const int ppw = 32 / a.Cc;
   const int ppb = ppw * kWarps;
   const int c = lane % a.Cc;
+  // with 4 or more coil lanes per point, the lanes split the 2*D*NJ value and
+  // derivative factors of their point and exchange them through scratch
+  const bool coop = a.Cc >= 4;
+  cplx<R>* scr = patch + a.Cc * a.ps + (warp * ppw + lane / a.Cc) * (2 * D * NJ);
   for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x) {
     Item it;
     JobCtx jc;
@@ -1139,16 +1275,35 @@ __global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, 
       R tmv[D];
       int base[D], local[D];
       const bool ok = point_base<R, D>(geo, tm, a.n, i, jc.origin, tmv, base, local) && active;
-      cplx<R> hv[D][kMaxJ], hd[D][kMaxJ];
+      cplx<R> hv[D][NJ], hd[D][NJ];
+      if (coop) {
+        for (int f = c; f < D * NJ; f += a.Cc) {
+          const int d = f / NJ, j = f - (f / NJ) * NJ;
+          cplx<R> fv = mk<R>(0, 0), fd = mk<R>(0, 0);
+          if (JC > 0 || j < sel<int, 3>(geo.J, d)) lerp_tables<R>(geo, d, sel<R, D>(tmv, d), sel<int, D>(base, d) + j, &fv, &fd);
+          scr[f] = fv;
+          scr[D * NJ + f] = fd;
+        }
+        __syncwarp();
 #pragma unroll
-      for (int d = 0; d < D; ++d) {
+        for (int d = 0; d < D; ++d)
 #pragma unroll
-        for (int j = 0; j < kMaxJ; ++j) {
-          if (j < geo.J[d]) {
-            lerp_tables<R>(geo, d, tmv[d], base[d] + j, &hv[d][j], &hd[d][j]);
-          } else {
-            hv[d][j] = mk<R>(0, 0);
-            hd[d][j] = mk<R>(0, 0);
+          for (int j = 0; j < NJ; ++j) {
+            hv[d][j] = scr[d * NJ + j];
+            hd[d][j] = scr[D * NJ + d * NJ + j];
+          }
+        __syncwarp();
+      } else {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+#pragma unroll
+          for (int j = 0; j < NJ; ++j) {
+            if (JC > 0 || j < geo.J[d]) {
+              lerp_tables<R>(geo, d, tmv[d], base[d] + j, &hv[d][j], &hd[d][j]);
+            } else {
+              hv[d][j] = mk<R>(0, 0);
+              hd[d][j] = mk<R>(0, 0);
+            }
           }
         }
       }
@@ -1165,8 +1320,8 @@ __global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, 
         for (int d = 0; d < D; ++d) der[d] = mk<R>(0, 0);
         if (D == 1) {
 #pragma unroll
-          for (int j = 0; j < kMaxJ; ++j) {
-            if (j < geo.J[0]) {
+          for (int j = 0; j < NJ; ++j) {
+            if (JC > 0 || j < geo.J[0]) {
               const cplx<R> x = plane[local[0] + j];
               val = cfma<R>(hv[0][j], x, val);
               der[0] = cfma<R>(hd[0][j], x, der[0]);
@@ -1174,13 +1329,13 @@ __global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, 
           }
         } else if (D == 2) {
 #pragma unroll
-          for (int jy = 0; jy < kMaxJ; ++jy) {
-            if (jy < geo.J[0]) {
+          for (int jy = 0; jy < NJ; ++jy) {
+            if (JC > 0 || jy < geo.J[0]) {
               cplx<R> rv = mk<R>(0, 0), rd = mk<R>(0, 0);
               const cplx<R>* row = plane + (local[0] + jy) * geo.P[1 % D] + local[1 % D];
 #pragma unroll
-              for (int jx = 0; jx < kMaxJ; ++jx) {
-                if (jx < geo.J[1 % D]) {
+              for (int jx = 0; jx < NJ; ++jx) {
+                if (JC > 0 || jx < geo.J[1 % D]) {
                   const cplx<R> x = row[jx];
                   rv = cfma<R>(hv[1 % D][jx], x, rv);
                   rd = cfma<R>(hd[1 % D][jx], x, rd);
@@ -1193,18 +1348,18 @@ __global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, 
           }
         } else {
 #pragma unroll 1
-          for (int jz = 0; jz < kMaxJ; ++jz) {
-            if (jz < geo.J[0]) {
+          for (int jz = 0; jz < NJ; ++jz) {
+            if (JC > 0 || jz < geo.J[0]) {
               cplx<R> zv = mk<R>(0, 0), zdy = mk<R>(0, 0), zdx = mk<R>(0, 0);
 #pragma unroll
-              for (int jy = 0; jy < kMaxJ; ++jy) {
-                if (jy < geo.J[1 % D]) {
+              for (int jy = 0; jy < NJ; ++jy) {
+                if (JC > 0 || jy < geo.J[1 % D]) {
                   cplx<R> rv = mk<R>(0, 0), rd = mk<R>(0, 0);
                   const cplx<R>* row =
                       plane + ((local[0] + jz) * geo.P[1 % D] + local[1 % D] + jy) * geo.P[2 % D] + local[2 % D];
 #pragma unroll
-                  for (int jx = 0; jx < kMaxJ; ++jx) {
-                    if (jx < geo.J[2 % D]) {
+                  for (int jx = 0; jx < NJ; ++jx) {
+                    if (JC > 0 || jx < geo.J[2 % D]) {
                       const cplx<R> x = row[jx];
                       rv = cfma<R>(hv[2 % D][jx], x, rv);
                       rd = cfma<R>(hd[2 % D][jx], x, rd);
@@ -1218,7 +1373,7 @@ __global__ void __launch_bounds__(kThreads) k_interp_grad(Geo<R> geo, Launch a, 
               // jz is a runtime index, so hv[0][jz] is read through a select chain
               cplx<R> hz = hv[0][0], dz = hd[0][0];
 #pragma unroll
-              for (int q = 1; q < kMaxJ; ++q)
+              for (int q = 1; q < NJ; ++q)
                 if (q == jz) {
                   hz = hv[0][q];
                   dz = hd[0][q];
@@ -1299,6 +1454,25 @@ __global__ void __launch_bounds__(kThreads) k_ragged_fwd(const RaggedProb<R>* __
       cur = pj.x;
     }
     fwd_job<R, D, JC>(sp.geo, sp.a, sp.tm, sp.ph, sp.grid, sp.kdata, pj.y, sp.nitems, patch);
+  }
+}
+
+template <int CC>
+__global__ void __launch_bounds__(kThreads) k_ragged_fwd_pairs(const RaggedProb<float>* __restrict__ probs,
+                                                               const int2* __restrict__ jobs, int64_t njobs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) RaggedProb<float> sp;
+  float2* patch = reinterpret_cast<float2*>(smem_raw);
+  int cur = -1;
+  for (int64_t g = blockIdx.x; g < njobs; g += gridDim.x) {
+    const int2 pj = jobs[g];
+    if (pj.x != cur) {
+      __syncthreads();
+      load_desc(&sp, probs + pj.x);
+      __syncthreads();
+      cur = pj.x;
+    }
+    fwd_job_pairs<CC>(sp.geo, sp.a, sp.tm, sp.ph, sp.grid, sp.kdata, pj.y, sp.nitems, patch);
   }
 }
 
@@ -1410,7 +1584,8 @@ static int prepare(const tkbn_geometry* g, const tkbn_points_desc* p, const void
   const int nj = j6 ? 6 : kMaxJ;
   a.scratch = (32 / a.Cc) * g->ndim * nj;
   const size_t patch = op == Op::kAdj ? (size_t)2 * a.Cc * a.ps * sizeof(R) : (size_t)a.Cc * a.ps * sizeof(cplx<R>);
-  ip->smem = patch + (op == Op::kGrad ? 0 : (size_t)kWarps * a.scratch * sizeof(cplx<R>));
+  // per-warp factor scratch: the table factors (the gradient keeps values and derivatives)
+  ip->smem = patch + (size_t)kWarps * a.scratch * (op == Op::kGrad ? 2 : 1) * sizeof(cplx<R>);
   if (ip->smem > 220 * 1024)
     return set_error(TKBN_ERR_UNSUPPORTED, "tile patch needs %zu bytes of shared memory", ip->smem);
   ip->max_jobs = ip->L.max_items * a.nbpt * a.ncc;
@@ -1429,9 +1604,36 @@ static int resident_blocks(K kernel, size_t smem, int64_t max_jobs, int* blocks)
   return TKBN_OK;
 }
 
+// Calls fn(std::integral_constant<int, CC>) for CC in {2, 4, 8, 16}.
+template <typename Fn>
+static int with_cc(int CC, Fn&& fn) {
+  switch (CC) {
+    case 2: return fn(std::integral_constant<int, 2>{});
+    case 4: return fn(std::integral_constant<int, 4>{});
+    case 8: return fn(std::integral_constant<int, 8>{});
+    default: return fn(std::integral_constant<int, 16>{});
+  }
+}
+
 template <typename R, int D, int JC>
 static int launch_fwd_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* grid, void* kdata,
                         cudaStream_t s) {
+  if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
+    if (ip.a.Cc >= 2) {
+      return with_cc(ip.a.Cc, [&](auto ccv) {
+        constexpr int CC = decltype(ccv)::value;
+        constexpr int PPW = 64 / CC;
+        const size_t smem = (size_t)ip.a.cells * CC * sizeof(float2) + (size_t)kWarps * PPW * 2 * 6 * sizeof(float2);
+        int blocks;
+        int rc = resident_blocks(k_interp_fwd_pairs<CC>, smem, ip.max_jobs, &blocks);
+        if (rc) return rc;
+        k_interp_fwd_pairs<CC><<<blocks, kThreads, smem, s>>>(geo, ip.a, (const float*)(ws + ip.L.off_coords),
+                                                              (const float2*)(ws + ip.L.off_phase),
+                                                              (const float2*)grid, (float2*)kdata);
+        return check_cuda(cudaGetLastError(), "interp_fwd launch");
+      });
+    }
+  }
   auto k = k_interp_fwd<R, D, JC>;
   int blocks;
   int rc = resident_blocks(k, ip.smem, ip.max_jobs, &blocks);
@@ -1453,10 +1655,10 @@ static int launch_adj_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws,
   return check_cuda(cudaGetLastError(), "interp_adj launch");
 }
 
-template <typename R, int D>
+template <typename R, int D, int JC>
 static int launch_grad_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* grid, const void* v,
                          void* grad, cudaStream_t s) {
-  auto k = k_interp_grad<R, D>;
+  auto k = k_interp_grad<R, D, JC>;
   int blocks;
   int rc = resident_blocks(k, ip.smem, ip.max_jobs, &blocks);
   if (rc) return rc;
@@ -1547,17 +1749,6 @@ static size_t reg_smem(int CC) {
   const int ng = kWarps / (kRegTileY / (32 / CC));
   const size_t partials = ng > 1 ? (size_t)ng * kRegTileY * kRegTileX * CC * sizeof(float2) : 0;
   return staging > partials ? staging : partials;
-}
-
-// Calls fn(std::integral_constant<int, CC>) for CC in {2, 4, 8, 16}.
-template <typename Fn>
-static int with_cc(int CC, Fn&& fn) {
-  switch (CC) {
-    case 2: return fn(std::integral_constant<int, 2>{});
-    case 4: return fn(std::integral_constant<int, 4>{});
-    case 8: return fn(std::integral_constant<int, 8>{});
-    default: return fn(std::integral_constant<int, 16>{});
-  }
 }
 
 template <typename R, int D, int JC>
@@ -1670,13 +1861,14 @@ static int interp_grad_r(const tkbn_geometry* g, const tkbn_points_desc* p, cons
   if (rc || p->npts == 0) return rc;
   Geo<R> geo = make_geo<R>(g, &ip.L, tables, dtables);
   const char* w = (const char*)ws;
+  const bool j6 = all_j(g, 6);
   switch (g->ndim) {
     case 1:
-      return launch_grad_t<R, 1>(geo, ip, w, grid, v, grad, s);
+      return j6 ? launch_grad_t<R, 1, 6>(geo, ip, w, grid, v, grad, s) : launch_grad_t<R, 1, 0>(geo, ip, w, grid, v, grad, s);
     case 2:
-      return launch_grad_t<R, 2>(geo, ip, w, grid, v, grad, s);
+      return j6 ? launch_grad_t<R, 2, 6>(geo, ip, w, grid, v, grad, s) : launch_grad_t<R, 2, 0>(geo, ip, w, grid, v, grad, s);
     default:
-      return launch_grad_t<R, 3>(geo, ip, w, grid, v, grad, s);
+      return j6 ? launch_grad_t<R, 3, 6>(geo, ip, w, grid, v, grad, s) : launch_grad_t<R, 3, 0>(geo, ip, w, grid, v, grad, s);
   }
 }
 
@@ -1710,9 +1902,10 @@ struct tkbn_ragged_plan_s {
   int dtype, ndim, j6;
   int64_t nprob;
   void* probs;  // RaggedProb<R>[nprob] on the device
-  int2 *fwd_jobs, *reg_jobs[4], *own_jobs, *zero_jobs;  // reg_jobs[k]: jobs of 2 << k coils per job
-  int64_t n_fwd, n_reg[4], n_own, n_zero;
-  size_t smem_fwd, smem_own;
+  // fwd_pairs[k], reg_jobs[k]: jobs of problems with 2 << k coils per job
+  int2 *fwd_jobs, *fwd_pairs[4], *reg_jobs[4], *own_jobs, *zero_jobs;
+  int64_t n_fwd, n_fwd_pairs[4], n_reg[4], n_own, n_zero;
+  size_t smem_fwd, smem_fwd_pairs[4], smem_own;
 };
 
 namespace tkbn_host {
@@ -1743,9 +1936,10 @@ int upload_jobs(const std::vector<JobRec>& v, int2** dev) {
 template <typename R, int D, int JC>
 int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P) {
   std::vector<RaggedProb<R>> desc((size_t)n);
-  std::vector<JobRec> fwd, reg[4], own, zero;
+  std::vector<JobRec> fwd, fwdp[4], reg[4], own, zero;
   P->smem_fwd = 0;
   P->smem_own = 0;
+  for (int k = 0; k < 4; ++k) P->smem_fwd_pairs[k] = 0;
   for (int64_t q = 0; q < n; ++q) {
     const tkbn_ragged_problem& r = pr[q];
     InterpPlan ip;
@@ -1767,14 +1961,23 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
     d.kdata = (cplx<R>*)r.kdata;
     d.nitems = hdr[0];
     d.vec_ok = ((uintptr_t)r.grid % 16 == 0) && (r.geom.grid_size[D - 1] % 2 == 0);
-    if (ip.smem > P->smem_fwd) P->smem_fwd = ip.smem;
-    // forward jobs: item i % nitems of coil chunk i / nitems
+    // forward jobs: item i % nitems of coil chunk i / nitems; 2D complex64
+    // J = 6 problems with 2 or more coils per job take the coil-pair gather
+    const bool pairs = std::is_same<R, float>::value && D == 2 && JC == 6 && ip.a.Cc >= 2;
+    const int pk = ip.a.Cc == 2 ? 0 : (ip.a.Cc == 4 ? 1 : (ip.a.Cc == 8 ? 2 : 3));
+    if (pairs) {
+      const size_t sm = (size_t)ip.a.cells * ip.a.Cc * sizeof(float2) + (size_t)kWarps * (64 / ip.a.Cc) * 12 * sizeof(float2);
+      if (sm > P->smem_fwd_pairs[pk]) P->smem_fwd_pairs[pk] = sm;
+    } else if (ip.smem > P->smem_fwd) {
+      P->smem_fwd = ip.smem;
+    }
     if (r.points.npts > 0 && hdr[0] > 0) {
       std::vector<Item> items((size_t)hdr[0]);
       if ((rc = check_cuda(cudaMemcpy(items.data(), ip.a.items, items.size() * sizeof(Item), cudaMemcpyDeviceToHost),
                            "read work items")))
         return rc;
-      for (int64_t j = 0; j < hdr[0] * ip.a.ncc; ++j) fwd.push_back({items[(size_t)(j % hdr[0])].len, (int)q, (int)j});
+      for (int64_t j = 0; j < hdr[0] * ip.a.ncc; ++j)
+        (pairs ? fwdp[pk] : fwd).push_back({items[(size_t)(j % hdr[0])].len, (int)q, (int)j});
     }
     // adjoint jobs: sub-job j / ncc of coil chunk j % ncc
     if (!ip.L.owned_ok || ip.L.span.ncombo > max_combo<D>())
@@ -1799,6 +2002,7 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
       if (sj[(size_t)j].pad && sj[(size_t)j].start == 0) zero.push_back({sj[(size_t)j].len, (int)q, (int)j});
   }
   lpt_sort(fwd);
+  for (auto& v : fwdp) lpt_sort(v);
   for (auto& v : reg) lpt_sort(v);
   lpt_sort(own);
   int rc = check_cuda(cudaMalloc(&P->probs, desc.size() * sizeof(RaggedProb<R>)), "ragged descriptors");
@@ -1811,7 +2015,9 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
     return rc;
   for (int k = 0; k < 4; ++k) {
     if ((rc = upload_jobs(reg[k], &P->reg_jobs[k]))) return rc;
+    if ((rc = upload_jobs(fwdp[k], &P->fwd_pairs[k]))) return rc;
     P->n_reg[k] = (int64_t)reg[k].size();
+    P->n_fwd_pairs[k] = (int64_t)fwdp[k].size();
   }
   P->n_fwd = (int64_t)fwd.size();
   P->n_own = (int64_t)own.size();
@@ -1821,9 +2027,25 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
 
 template <typename R, int D, int JC>
 int ragged_fwd_t(const tkbn_ragged_plan_s* P, cudaStream_t s) {
+  int rc;
+  if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
+    for (int k = 0; k < 4; ++k) {
+      if (P->n_fwd_pairs[k] == 0) continue;
+      rc = with_cc(2 << k, [&](auto ccv) {
+        constexpr int CC = decltype(ccv)::value;
+        int blocks;
+        int r = resident_blocks(k_ragged_fwd_pairs<CC>, P->smem_fwd_pairs[k], P->n_fwd_pairs[k], &blocks);
+        if (r) return r;
+        k_ragged_fwd_pairs<CC><<<blocks, kThreads, P->smem_fwd_pairs[k], s>>>(
+            (const RaggedProb<float>*)P->probs, P->fwd_pairs[k], P->n_fwd_pairs[k]);
+        return check_cuda(cudaGetLastError(), "ragged interp_fwd launch");
+      });
+      if (rc) return rc;
+    }
+  }
   if (P->n_fwd == 0) return TKBN_OK;
   int blocks;
-  int rc = resident_blocks(k_ragged_fwd<R, D, JC>, P->smem_fwd, P->n_fwd, &blocks);
+  rc = resident_blocks(k_ragged_fwd<R, D, JC>, P->smem_fwd, P->n_fwd, &blocks);
   if (rc) return rc;
   k_ragged_fwd<R, D, JC><<<blocks, kThreads, P->smem_fwd, s>>>((const RaggedProb<R>*)P->probs, P->fwd_jobs, P->n_fwd);
   return check_cuda(cudaGetLastError(), "ragged interp_fwd launch");
@@ -1901,7 +2123,10 @@ int ragged_plan_destroy(tkbn_ragged_plan p) {
   if (!p) return TKBN_OK;
   cudaFree(p->probs);
   cudaFree(p->fwd_jobs);
-  for (int k = 0; k < 4; ++k) cudaFree(p->reg_jobs[k]);
+  for (int k = 0; k < 4; ++k) {
+    cudaFree(p->reg_jobs[k]);
+    cudaFree(p->fwd_pairs[k]);
+  }
   cudaFree(p->own_jobs);
   cudaFree(p->zero_jobs);
   delete p;
