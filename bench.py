@@ -607,8 +607,8 @@ def run_config(args):
         with torch.no_grad():
             fwd_ms = timed(lambda: adj(fwd(x, omega, smaps=smaps), omega, smaps=smaps), args.steps, args.warmup)
         ms = timed(grad_step, args.steps, args.warmup)
-        extra = {"forward_AHA_ms": fwd_ms, "backward_over_forward": ms / fwd_ms,
-                 "note": "the trajectory requires grad: its layout is rebuilt every step"}
+        extra = {"forward_AHA_ms": fwd_ms, "grad_step_ms": ms, "backward_over_forward": (ms - fwd_ms) / fwd_ms,
+                 "note": "a step is the forward A^H A x, the loss and its backward (x and ktraj gradients)"}
     else:
         with torch.no_grad():
             ms = timed(lambda: adj(fwd(x, omega, smaps=smaps), omega, smaps=smaps), args.steps, args.warmup)

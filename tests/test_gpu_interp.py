@@ -77,6 +77,8 @@ CASES = [
     ((200,), 2, 4, 3000, False, 6, 1024, 1.0),
     ((24, 20, 28), 1, 3, 4000, False, 6, 1024, 1.0),
     ((16, 18, 14), 2, 2, 1500, True, (4, 5, 6), 1024, 1.0),
+    ((32, 24, 40), 1, 8, 30000, False, 6, 1024, 1.0),  # 3D register adjoint, 8 coils per job
+    ((26, 21, 30), 2, 11, 9000, True, 6, 1024, 1.0),  # 3D, two coil chunks, edge tiles
 ]
 
 
@@ -266,3 +268,27 @@ def test_adjoint_deterministic_layout_is_bitwise_repeatable():
     lay = _runtime.points_layout(_runtime.make_geom(torch.complex64, K, K, (6, 6), (1024, 1024), (0.0, 0.0)), om,
                                  deterministic=True)
     assert lay.flags == 2
+
+
+@pytest.mark.parametrize("C", [8, 3, 1])
+def test_adjoint_3d_owned_tiles_deterministic(C):
+    """3D owned tiles (4 x 8 x 8, register accumulators): bitwise repeatable, and
+    equal to the oracle, with points concentrated at the k-space centre."""
+    gen = torch.Generator().manual_seed(31)
+    K = (40, 32, 48)
+    M = 20000
+    y = _rand(gen, (1, C, M), torch.complex64)
+    om = _traj(gen, (3, M)).float()
+    om[..., :5000] *= 0.1
+    adj = tkbn().KbInterpAdjoint(im_size=K, grid_size=K, dtype=torch.complex64, device=DEV)
+    torch.use_deterministic_algorithms(True)
+    try:
+        a = adj(y.to(DEV), om.to(DEV))
+        b = adj(y.to(DEV), om.to(DEV))
+    finally:
+        torch.use_deterministic_algorithms(False)
+    assert torch.equal(a, b)
+    op = O.Operator(K, K, cdtype=np.complex64)
+    assert rel_l2(_np(a), op.interp_adj(y.numpy(), om.numpy())) < TOL64
+    c = adj(y.to(DEV), om.to(DEV))  # split heavy tiles (default layout)
+    assert rel_l2(_np(c), op.interp_adj(y.numpy(), om.numpy())) < TOL64

@@ -782,14 +782,19 @@ __device__ __forceinline__ void own_job(const Geo<R>& geo, const OwnLaunch& a, c
     const int64_t vbase = a.vlist ? (int64_t)a.voff[it.key] : 0;
     for (int q0 = it.start; q0 < qend; q0 += kNB) {
       int nv = 0;
-      if (D == 2 && a.vlist) {
-        // A1 (2D): the tile's list holds only points that reach it
+      if (D > 1 && a.vlist) {
+        // A1 (2D, 3D): the tile's list holds only points that reach it
         nv = min(kNB, qend - q0);
         for (int e = threadIdx.x; e < nv; e += kThreads) {
           const int4 ent = a.vlist[vbase + q0 + e];
           spt[e] = ent.x;
           sloc[e * D] = ent.z;
-          sloc[e * D + (D - 1)] = ent.w;
+          if (D == 2) {
+            sloc[e * D + (D - 1)] = ent.w;
+          } else {
+            sloc[e * D + 1 % D] = (int)(short)(ent.w & 0xffff);
+            sloc[e * D + 2 % D] = ent.w >> 16;
+          }
         }
         __syncthreads();
       } else {
@@ -1025,18 +1030,22 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
 constexpr int kNBR = 256;  // staged points per batch (== kThreads)
 constexpr int kRegTileY = 16, kRegTileX = 14, kRegCoils = 16;
 
-template <int LX>
-__device__ __forceinline__ void reg_add_cols(float2 (&racc)[kRegTileX], float2 vy, const float2 (&fx)[6]) {
+// racc[LX + jx] += vy * fx[jx] for the columns inside the row (TXR cells).
+template <int TXR, int LX>
+__device__ __forceinline__ void reg_add_cols(float2 (&racc)[TXR], float2 vy, const float2 (&fx)[6]) {
 #pragma unroll
   for (int jx = 0; jx < 6; ++jx)
-    if (LX + jx >= 0 && LX + jx < kRegTileX) racc[LX + jx] = cfma<float>(vy, fx[jx], racc[LX + jx]);
+    if (LX + jx >= 0 && LX + jx < TXR) racc[LX + jx] = cfma<float>(vy, fx[jx], racc[LX + jx]);
 }
 
-__device__ __forceinline__ void reg_add_point(int lx, float2 (&racc)[kRegTileX], float2 vy, const float2 (&fx)[6]) {
+// A point's column offset lx is uniform over the warp: the switch selects
+// code with static register indices (lx in [-5, TXR - 1], TXR <= 14).
+template <int TXR>
+__device__ __forceinline__ void reg_add_point(int lx, float2 (&racc)[TXR], float2 vy, const float2 (&fx)[6]) {
   switch (lx) {
-#define TKBN_REG_CASE(L) \
-  case L:                \
-    reg_add_cols<L>(racc, vy, fx); \
+#define TKBN_REG_CASE(L)                                   \
+  case L:                                                  \
+    if constexpr (L < TXR) reg_add_cols<TXR, L>(racc, vy, fx); \
     break;
     TKBN_REG_CASE(-5) TKBN_REG_CASE(-4) TKBN_REG_CASE(-3) TKBN_REG_CASE(-2) TKBN_REG_CASE(-1)
     TKBN_REG_CASE(0) TKBN_REG_CASE(1) TKBN_REG_CASE(2) TKBN_REG_CASE(3) TKBN_REG_CASE(4) TKBN_REG_CASE(5)
@@ -1143,7 +1152,7 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
             const float4 f01 = fx4[0], f23 = fx4[1], f45 = fx4[2];
             const float2 fx[6] = {make_float2(f01.x, f01.y), make_float2(f01.z, f01.w), make_float2(f23.x, f23.y),
                                   make_float2(f23.z, f23.w), make_float2(f45.x, f45.y), make_float2(f45.z, f45.w)};
-            reg_add_point(loc.y, racc, vy, fx);
+            reg_add_point<kRegTileX>(loc.y, racc, vy, fx);
           }
         }
         if ((h + 1) * 32 >= nv) break;
@@ -1203,6 +1212,173 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
       __syncthreads();  // the next job's staging reuses the buffer
     }
   }
+}
+
+// K4 (owned tiles, registers), 3D: complex64, J = 6, 4 x 8 x 8 tiles, CC
+// coils per job (2, 4 or 8; one coil runs as CC = 2). Lane (coil, row) keeps
+// the 8 x-cells of one (z, y) row of the tile in registers; a warp covers
+// RPW = 32 / CC of the tile's 32 rows, and the groups of warps that cover
+// the tile take the staged points in turn, as in the 2D kernel.
+constexpr int kReg3Z = 4, kReg3Y = 8, kReg3X = 8, kReg3Rows = kReg3Z * kReg3Y;
+
+template <int CC>
+__device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch& a, const float* __restrict__ tm,
+                                         const float2* __restrict__ ph, const float2* __restrict__ kdata,
+                                         float2* __restrict__ grid, int vec_ok, int64_t job, unsigned char* smem_raw) {
+  constexpr int D = 3, NJ = 6;
+  constexpr int RPW = 32 / CC, WPT = kReg3Rows / RPW, NG = kWarps / WPT;
+  static_assert(CC >= 2 && CC <= 8 && (CC & (CC - 1)) == 0, "coils per job");
+  float2* sfac = reinterpret_cast<float2*>(smem_raw);  // [kNBR][18]: conj z, y, x factors
+  float2* sv = sfac + kNBR * D * NJ;                   // [kNBR][CC] conj(phase) * kdata per coil
+  int4* sloc = reinterpret_cast<int4*>(sv + kNBR * CC);  // [kNBR] footprint start (z, y, x) in the tile
+  float2* part = reinterpret_cast<float2*>(smem_raw);    // [NG][CC][32][8] partial tiles (after the batches)
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int c = lane % CC, grp = warp / WPT;
+  const int r_lo = (warp % WPT) * RPW;
+  const int myrow = r_lo + lane / CC;
+  const int mz = myrow / kReg3Y, my = myrow % kReg3Y;
+  const int64_t per_sj = a.nbpt * a.ncc;
+  {
+    const Item it = a.jobs[job / per_sj];
+    const int64_t rest = job % per_sj;
+    const int cc = (int)(rest % a.ncc);
+    const int64_t bb = rest / a.ncc;
+    int64_t t;
+    int td[kMaxDim], origin[kMaxDim], ext[kMaxDim];
+    own_tile_geometry<float, D>(geo, it.key, &t, td, origin, ext);
+    const int64_t b = a.ntraj == 1 ? bb : t;
+    const int c0 = cc * a.Cc;
+    const int ncl = (int)min((int64_t)min(CC, a.Cc), a.C - c0);
+    const bool rowok = mz < ext[0] && my < ext[1];
+    const int64_t vbase = a.voff[it.key];
+    // the warp's rows: z in [zlo, zhi], y in [ylo, yhi] (clipped to the tile)
+    const int zlo = r_lo / kReg3Y, zhi = min((r_lo + RPW - 1) / kReg3Y, ext[0] - 1);
+    const int ylo = RPW >= kReg3Y ? 0 : r_lo % kReg3Y;
+    const int yhi = min(RPW >= kReg3Y ? kReg3Y - 1 : ylo + RPW - 1, ext[1] - 1);
+    float2 racc[kReg3X];
+#pragma unroll
+    for (int x = 0; x < kReg3X; ++x) racc[x] = make_float2(0.f, 0.f);
+    const int qend = it.start + it.len;
+    for (int q0 = it.start; q0 < qend; q0 += kNBR) {
+      const int nv = min(kNBR, qend - q0);
+      const int4* ents = a.vlist + vbase + q0;
+      for (int e = threadIdx.x; e < nv * D; e += kThreads) {
+        const int pt = e / D, d = e - (e / D) * D;
+        const int4 ent = ents[pt];
+        if (d == 0) sloc[pt] = make_int4(ent.z, (int)(short)(ent.w & 0xffff), ent.w >> 16, 0);
+        const float tv = tm[d * a.n + ent.x];
+        const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
+        const float Lr = sel<float, D>(geo.Lr, d);
+        const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
+        const float2* tab = sel<const float2*, D>(geo.tab, d);
+        const bool half = sel<bool, D>(geo.half, d);
+        float2* out = sfac + e * NJ;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j)
+          out[j] = cconj<float>(table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half));
+      }
+#pragma unroll 4
+      for (int e = threadIdx.x; e < nv * CC; e += kThreads) {
+        const int pt = e / CC, cl = e % CC;
+        float2 v = make_float2(0.f, 0.f);
+        if (cl < ncl) {
+          const int4 ent = ents[pt];
+          v = cmulc<float>(kdata[(b * a.C + c0 + cl) * a.M + ent.y], ph[ent.x]);
+        }
+        sv[e] = v;
+      }
+      __syncthreads();
+#pragma unroll 1
+      for (int h = 0; h < kNBR / 32; ++h) {
+        const int p = h * 32 + lane;
+        bool tch = false;
+        if (p < nv && (NG == 1 || p % NG == grp)) {
+          const int4 loc = sloc[p];
+          tch = max(zlo, loc.x) <= min(zhi, loc.x + NJ - 1) && max(ylo, loc.y) <= min(yhi, loc.y + NJ - 1);
+        }
+        for (unsigned msk = __ballot_sync(0xffffffffu, tch); msk; msk &= msk - 1) {
+          const int pt = h * 32 + __ffs(msk) - 1;
+          const int4 loc = sloc[pt];
+          const int jz = mz - loc.x, jy = my - loc.y;
+          if (rowok && (unsigned)jz < (unsigned)NJ && (unsigned)jy < (unsigned)NJ) {
+            const float2* fp = sfac + pt * (D * NJ);
+            const float2 vzy = cmul<float>(cmul<float>(sv[pt * CC + c], fp[jz]), fp[NJ + jy]);
+            const float4* fx4 = reinterpret_cast<const float4*>(fp + 2 * NJ);
+            const float4 f01 = fx4[0], f23 = fx4[1], f45 = fx4[2];
+            const float2 fx[6] = {make_float2(f01.x, f01.y), make_float2(f01.z, f01.w), make_float2(f23.x, f23.y),
+                                  make_float2(f23.z, f23.w), make_float2(f45.x, f45.y), make_float2(f45.z, f45.w)};
+            reg_add_point<kReg3X>(loc.z, racc, vzy, fx);
+          }
+        }
+        if ((h + 1) * 32 >= nv) break;
+      }
+      __syncthreads();
+    }
+    const int ex = ext[2];
+    if (NG == 1) {
+      if (rowok && c < ncl) {
+        float2* dst = grid + (b * a.C + c0 + c) * a.gtot +
+                      ((int64_t)(origin[0] + mz) * geo.K[1] + origin[1] + my) * geo.K[2] + origin[2];
+        if (it.pad == 0) {
+          if (vec_ok) {
+#pragma unroll
+            for (int x = 0; x < kReg3X; x += 2) {
+              if (x + 1 < ex)
+                *reinterpret_cast<float4*>(dst + x) = make_float4(racc[x].x, racc[x].y, racc[x + 1].x, racc[x + 1].y);
+              else if (x < ex)
+                dst[x] = racc[x];
+            }
+          } else {
+#pragma unroll
+            for (int x = 0; x < kReg3X; ++x)
+              if (x < ex) dst[x] = racc[x];
+          }
+        } else {
+#pragma unroll
+          for (int x = 0; x < kReg3X; ++x)
+            if (x < ex) atomic_add_global(dst + x, racc[x]);
+        }
+      }
+    } else {
+      constexpr int TE = kReg3Rows * kReg3X * CC;
+#pragma unroll
+      for (int x = 0; x < kReg3X; ++x) part[grp * TE + (c * kReg3Rows + myrow) * kReg3X + x] = racc[x];
+      __syncthreads();
+      for (int e = threadIdx.x; e < TE; e += kThreads) {
+        const int cl = e / (kReg3Rows * kReg3X);
+        const int rr = (e / kReg3X) % kReg3Rows, x = e % kReg3X;
+        const int z = rr / kReg3Y, y = rr % kReg3Y;
+        if (cl >= ncl || z >= ext[0] || y >= ext[1] || x >= ex) continue;
+        float2 v = part[e];
+#pragma unroll
+        for (int q = 1; q < NG; ++q) {
+          const float2 w = part[q * TE + e];
+          v.x += w.x;
+          v.y += w.y;
+        }
+        float2* dst = grid + (b * a.C + c0 + cl) * a.gtot +
+                      ((int64_t)(origin[0] + z) * geo.K[1] + origin[1] + y) * geo.K[2] + origin[2] + x;
+        if (it.pad == 0)
+          *dst = v;
+        else
+          atomic_add_global(dst, v);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <int CC>
+__global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg3(Geo<float> geo, OwnLaunch a,
+                                                                 const float* __restrict__ tm,
+                                                                 const float2* __restrict__ ph,
+                                                                 const float2* __restrict__ kdata,
+                                                                 float2* __restrict__ grid, int vec_ok) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t njobs = a.hdr[1] * a.nbpt * a.ncc;
+  for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
+    reg3_job<CC>(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw);
 }
 
 template <int CC>
@@ -1567,7 +1743,8 @@ static int prepare(const tkbn_geometry* g, const tkbn_points_desc* p, const void
   a.B = B;
   a.C = C;
   // coil chunk: power of two, <= 16 (<= 8 for complex128), covering C when possible
-  const int cmax = g->dtype == TKBN_C64 ? 16 : 8;
+  // (the 3D adjoint's register path takes at most 8 coils per job)
+  const int cmax = g->dtype == TKBN_C64 ? ((op == Op::kAdj && g->ndim == 3) ? 8 : 16) : 8;
   a.Cc = next_pow2((int)(C < cmax ? C : cmax));
   a.ncc = (int)((C + a.Cc - 1) / a.Cc);
   a.nbpt = p->ntraj == 1 ? B : 1;
@@ -1744,6 +1921,20 @@ static bool reg_eligible(const InterpPlan& ip, const OwnLaunch& o) {
 static int reg_cc(int Cc) { return Cc < 2 ? 2 : Cc; }
 
 // Staging of a batch, or (more than one point group) the groups' partial tiles.
+// 3D: 4 x 8 x 8 tiles, at most 8 coils per job.
+template <typename R, int D, int JC>
+static bool reg3_eligible(const InterpPlan& ip, const OwnLaunch& o) {
+  return std::is_same<R, float>::value && D == 3 && JC == 6 && o.vlist && o.Cc <= 8 && ip.L.tile[0] == kReg3Z &&
+         ip.L.tile[1] == kReg3Y && ip.L.tile[2] == kReg3X;
+}
+
+static size_t reg3_smem(int CC) {
+  const size_t staging = (size_t)kNBR * (3 * 6 + CC) * sizeof(float2) + (size_t)kNBR * sizeof(int4);
+  const int ng = kWarps / (kReg3Rows / (32 / CC));
+  const size_t partials = ng > 1 ? (size_t)ng * kReg3Rows * kReg3X * CC * sizeof(float2) : 0;
+  return staging > partials ? staging : partials;
+}
+
 static size_t reg_smem(int CC) {
   const size_t staging = (size_t)kNBR * (2 * 6 + CC) * sizeof(float2) + (size_t)kNBR * sizeof(int2);
   const int ng = kWarps / (kRegTileY / (32 / CC));
@@ -1780,6 +1971,22 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
         k_interp_adj_reg<CC><<<blocks, kThreads, rsmem, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
                                                              (const float2*)(ws + ip.L.off_phase),
                                                              (const float2*)kdata, (float2*)grid, vec_ok);
+        return check_cuda(cudaGetLastError(), "interp_adj launch");
+      });
+    }
+  }
+  if constexpr (std::is_same<R, float>::value && D == 3 && JC == 6) {
+    if (reg3_eligible<R, D, JC>(ip, o)) {
+      return with_cc(reg_cc(o.Cc), [&](auto ccv) {
+        constexpr int CC = decltype(ccv)::value < 8 ? decltype(ccv)::value : 8;
+        const size_t rsmem = reg3_smem(CC);
+        int blocks;
+        int rc = resident_blocks(k_interp_adj_reg3<CC>, rsmem, max_jobs, &blocks);
+        if (rc) return rc;
+        const int vec_ok = ((uintptr_t)grid % 16 == 0) && (geo.K[2] % 2 == 0);
+        k_interp_adj_reg3<CC><<<blocks, kThreads, rsmem, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
+                                                              (const float2*)(ws + ip.L.off_phase),
+                                                              (const float2*)kdata, (float2*)grid, vec_ok);
         return check_cuda(cudaGetLastError(), "interp_adj launch");
       });
     }

@@ -130,23 +130,30 @@ __global__ void k_tile_work(Geo<R> geo, const int32_t* __restrict__ counts, cons
 // when the footprint starts in an earlier tile; periodic). A block-wide
 // exclusive scan of the per-thread counts keeps the order. The first pass
 // (voff == nullptr) counts, the second writes at voff[key].
+// In 3D the entry packs the row and column offsets: {i, m, rz, (ry & 0xffff) | (rx << 16)}.
 constexpr int kValidThreads = 256;
-template <typename R>
+template <typename R, int D>
 __global__ void __launch_bounds__(kValidThreads) k_tile_valid(Geo<R> geo, const int32_t* __restrict__ counts,
                                                               const int32_t* __restrict__ tile_off,
                                                               const R* __restrict__ tm, const int32_t* __restrict__ vals,
                                                               int64_t n, int64_t M, int64_t nkeys, SrcSpan span,
                                                               const int32_t* __restrict__ voff,
                                                               int32_t* __restrict__ vcount, int4* __restrict__ vlist) {
-  __shared__ int s_start[16], s_pre[17], s_warp[kValidThreads / 32];
+  constexpr int MAXCOMBO = D == 2 ? 16 : 27;
+  __shared__ int s_start[MAXCOMBO], s_pre[MAXCOMBO + 1], s_warp[kValidThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int64_t key = blockIdx.x; key < nkeys; key += gridDim.x) {
     const int64_t t = key / geo.ntiles;
-    const int rem = (int)(key - t * geo.ntiles);
-    int td[kMaxDim] = {rem / geo.ntile[1], rem % geo.ntile[1], 0};
-    int origin[2], ext[2];
+    int rem = (int)(key - t * geo.ntiles);
+    int td[kMaxDim] = {0, 0, 0};
 #pragma unroll
-    for (int d = 0; d < 2; ++d) {
+    for (int d = D - 1; d >= 0; --d) {
+      td[d] = rem % geo.ntile[d];
+      rem /= geo.ntile[d];
+    }
+    int origin[D], ext[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
       origin[d] = td[d] * geo.T[d];
       ext[d] = min(geo.T[d], geo.K[d] - origin[d]);
     }
@@ -177,9 +184,9 @@ __global__ void __launch_bounds__(kValidThreads) k_tile_valid(Geo<R> geo, const 
           while (s_pre[l + 1] <= q) ++l;
           const int i = s_start[l] + (q - s_pre[l]);
           bool v = true;
-          int r[2];
+          int r[D];
 #pragma unroll
-          for (int d = 0; d < 2; ++d) {
+          for (int d = 0; d < D; ++d) {
             const R f = floor(sub_rn(tm[d * n + i], geo.halfJ[d]));
             const bool fin = fabs(f) < R(1 << 30);
             const int w = fin ? wrap_cell(1 + (int)f, geo.K[d]) : 0;
@@ -191,7 +198,7 @@ __global__ void __launch_bounds__(kValidThreads) k_tile_valid(Geo<R> geo, const 
           valid[k] = v;
           idx[k] = i;
           ry[k] = r[0];
-          rx[k] = r[1];
+          rx[k] = D == 2 ? r[1] : ((r[1 % D] & 0xffff) | (r[2 % D] << 16));
           mine += v ? 1 : 0;
         }
       }
@@ -341,7 +348,9 @@ void default_tiles(const tkbn_geometry* g, int tile[3], int* chunk) {
     tile[0] = 16;
     tile[1] = 14;
   } else {
-    tile[0] = tile[1] = tile[2] = 4;
+    // 4 x 8 x 8: 32 (z, y) rows of 8 cells for the register adjoint
+    tile[0] = 4;
+    tile[1] = tile[2] = 8;
   }
   *chunk = 1024;
 }
@@ -414,7 +423,8 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   }
   // adjoint sub-jobs: at most adj_chunk candidates (list entries in 2D) each
   L->adj_chunk = (g->flags & TKBN_ADJ_DETERMINISTIC) ? (1 << 30) : 1024;
-  L->vlist = g->ndim == 2 && L->owned_ok && L->span.ncombo <= 16;  // the 2D owned-tile kernels' source limit
+  // the owned-tile kernels' source limits: 16 source tiles in 2D, 27 in 3D
+  L->vlist = L->owned_ok && ((g->ndim == 2 && L->span.ncombo <= 16) || (g->ndim == 3 && L->span.ncombo <= 27));
   L->max_valid = L->vlist ? L->span.ncombo * L->npts_total : 0;
   L->max_subjobs = 2 * L->nkeys + (L->span.ncombo * L->npts_total + L->adj_chunk - 1) / L->adj_chunk;
   int sbits = 1;
@@ -557,13 +567,14 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
     int32_t* voff = (int32_t*)(ws + L.off_voff);
     int4* vlist = (int4*)(ws + L.off_vlist);
     const int wblocks = (int)(L.nkeys < 152 * 8 ? L.nkeys : 152 * 8);
-    k_tile_valid<R><<<wblocks, kValidThreads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys,
-                                                      L.span, nullptr, vcount, vlist);
+    auto kv = g->ndim == 2 ? k_tile_valid<R, 2> : k_tile_valid<R, 3>;
+    kv<<<wblocks, kValidThreads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys, L.span, nullptr,
+                                         vcount, vlist);
     tb = L.cub_bytes;
     if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, vcount, voff, (int)L.nkeys, s) != cudaSuccess)
       return set_error(TKBN_ERR_CUDA, "scan failed");
-    k_tile_valid<R><<<wblocks, kValidThreads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys,
-                                                      L.span, voff, vcount, vlist);
+    kv<<<wblocks, kValidThreads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys, L.span, voff,
+                                         vcount, vlist);
   }
   // adjoint sub-jobs (output tiles, heavy ones split), longest first
   {
