@@ -39,6 +39,8 @@
  *   tkbn_fft_filter        fft_filter                   torchkbnufft/_nufft/fft.py:121-173
  *   tkbn_toep_apply        ToepNufft.forward / toep_batch_loop
  *                          torchkbnufft/modules/kbnufft.py:441-547
+ *   tkbn_spmat_interp(_adjoint) spmat_interp / spmat_interp_adjoint
+ *                          torchkbnufft/_nufft/interp.py:13-85
  *   tkbn_ragged_*          a loop of table_interp / table_interp_adjoint calls
  *                          over independent problems (no single counterpart)
  */
@@ -141,6 +143,20 @@ int tkbn_interp_grad_omega(const tkbn_geometry* g, const tkbn_points_desc* p, co
 #define TKBN_NOALLOC_SCRATCH_BYTES ((size_t)8 << 20)
 int tkbn_interp_fwd_noalloc(const tkbn_geometry* g, const void* const* tables, const void* omega, int64_t npts,
                             const void* grid, int64_t nbatch, int64_t ncoil, void* kdata, void* stream);
+
+/* ---- sparse-matrix interpolation ----------------------------------------
+ * The interpolation matrix A (nrows k-space points x ncols grid cells,
+ * complex of the working type) as CSR (crow[nrows + 1], col[nnz], val[nnz])
+ * for the forward and as COO rows (row[nnz]) with the same col/val for the
+ * adjoint. x and y hold nplanes (batch x coil) planes of ncols / nrows.
+ * Replaces spmat_interp / spmat_interp_adjoint,
+ * torchkbnufft/_nufft/interp.py:13-85. */
+int tkbn_spmat_interp(int dtype, int64_t nrows, int64_t ncols, const int64_t* crow, const int32_t* col,
+                      const void* val, const void* x, int64_t nplanes, void* y, void* stream);
+/* x = A^H y; x is fully overwritten. */
+int tkbn_spmat_interp_adjoint(int dtype, int64_t nrows, int64_t ncols, int64_t nnz, const int32_t* row,
+                              const int32_t* col, const void* val, const void* y, int64_t nplanes, void* x,
+                              void* stream);
 
 /* ---- ragged batch (K8): many independent problems per launch ------------
  * No single counterpart in the reference, where each problem is one call of

@@ -14,6 +14,7 @@ Two kinds of fixtures are written:
   CUDA path to the reference's table mode at the working precision.
 
 The tests only read the ``.npz`` files; nothing at test time needs the reference.
+``TKBN_GOLDEN_ONLY=<prefix>`` rewrites only the live fixtures with that prefix.
 """
 
 from __future__ import annotations
@@ -135,12 +136,30 @@ def live_cases():
         cases[name] = dict(omega=_np(om), dcomp=_np(tkbn.calc_density_compensation_function(om, im_size)),
                            im_size=np.array(im_size))
 
+    # sparse-matrix interpolation: the matrices (dense) and a NUFFT pair through them
+    for name, im_size, M, seed in (("spmat_2d", (12, 10), 150, 40), ("spmat_3d", (6, 8, 6), 120, 41)):
+        gen = torch.Generator().manual_seed(seed)
+        om = _traj(gen, (len(im_size), M), torch.float32)
+        real, imag = tkbn.calc_tensor_spmatrix(om, im_size)
+        image = _cplx(gen, (2, 3) + im_size, torch.complex64)
+        kin = _cplx(gen, (2, 3, M), torch.complex64)
+        fwd = tkbn.KbNufft(im_size=im_size)
+        adj = tkbn.KbNufftAdjoint(im_size=im_size)
+        cases[name] = dict(omega=_np(om), mat_real=_np(real.to_dense()), mat_imag=_np(imag.to_dense()),
+                           image=_np(image), kdata_in=_np(kin),
+                           kdata=_np(fwd(image, om, interp_mats=(real, imag))),
+                           image_adj=_np(adj(kin, om, interp_mats=(real, imag))))
+
+    only = os.environ.get("TKBN_GOLDEN_ONLY")
     for name, arrs in cases.items():
+        if only and not name.startswith(only):
+            continue
         np.savez_compressed(os.path.join(HERE, f"live_{name}.npz"), **arrs)
 
 
 if __name__ == "__main__":
     sys.path.insert(0, REF)
-    convert_reference_pickles()
+    if not os.environ.get("TKBN_GOLDEN_ONLY"):
+        convert_reference_pickles()
     live_cases()
     print("wrote fixtures to", HERE)

@@ -139,8 +139,8 @@ def test_dtype_and_norm_errors():
         ob(torch.zeros((1, 1, 8, 8, 3), device=DEV), om)
     with pytest.raises(ValueError):
         ob(torch.zeros((2, 1, 8, 8), dtype=torch.complex64, device=DEV), torch.zeros((3, 2, 4), device=DEV))
-    with pytest.raises(NotImplementedError):
-        ob(x, om, interp_mats=(om, om))
+    with pytest.raises(TypeError):
+        ob(x, om, interp_mats=om)
 
 
 def test_module_to_and_state_dict():

@@ -14,16 +14,12 @@ from ._setup import init_fn
 from .dcomp import calc_density_compensation_function
 from .modules import KbInterp, KbInterpAdjoint, KbNufft, KbNufftAdjoint, ToepNufft
 from .ragged import RaggedNufft
+from .spmat import calc_tensor_spmatrix
 from .toep import calc_toeplitz_kernel
 from . import autotune
 from . import _setup as nufft_utils
 
 __version__ = "0.1.0"
-
-
-def calc_tensor_spmatrix(*args, **kwargs):
-    """Sparse-matrix interpolation is not provided; use table interpolation."""
-    raise NotImplementedError("sparse-matrix interpolation is not provided by torchkbnufft_gb300")
 
 
 __all__ = [

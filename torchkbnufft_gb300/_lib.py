@@ -90,6 +90,8 @@ SIGNATURES = {
     "tkbn_fft_filter": [_GP, _P, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P],
     "tkbn_toep_apply": [_GP, _P, _P, _P, _I64, _P, _I64, _I64, _I64, _INT, _P, _P, _P],
     "tkbn_interp_fwd_noalloc": [_GP, _PP, _P, _I64, _P, _I64, _I64, _P, _P],
+    "tkbn_spmat_interp": [_INT, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P],
+    "tkbn_spmat_interp_adjoint": [_INT, _I64, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P],
     "tkbn_ragged_plan_create": [ctypes.POINTER(RaggedProblem), _I64, ctypes.POINTER(ctypes.c_void_p)],
     "tkbn_ragged_plan_destroy": [_P],
     "tkbn_ragged_interp_fwd": [_P, _P],

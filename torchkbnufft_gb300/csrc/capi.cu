@@ -26,6 +26,10 @@ int ifft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, void* grid, const
 int toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, const void* kernel, int64_t kbatch,
                int by_channel, const void* smaps, int64_t smaps_batch, int64_t B, int64_t C, int norm, void* grid,
                void* out, cudaStream_t st);
+int spmat_interp(int dtype, int64_t nrows, int64_t ncols, const int64_t* crow, const int32_t* col, const void* val,
+                 const void* x, int64_t nplanes, void* y, cudaStream_t s);
+int spmat_interp_adjoint(int dtype, int64_t nrows, int64_t ncols, int64_t nnz, const int32_t* row, const int32_t* col,
+                         const void* val, const void* y, int64_t nplanes, void* x, cudaStream_t s);
 int ragged_plan_create(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan* out);
 int ragged_plan_destroy(tkbn_ragged_plan p);
 int ragged_interp_fwd(tkbn_ragged_plan p, cudaStream_t s);
@@ -198,4 +202,15 @@ int tkbn_ragged_interp_fwd(tkbn_ragged_plan plan, void* stream) {
 
 int tkbn_ragged_interp_adj(tkbn_ragged_plan plan, void* stream) {
   TKBN_GUARD(ragged_interp_adj(plan, (cudaStream_t)stream));
+}
+
+int tkbn_spmat_interp(int dtype, int64_t nrows, int64_t ncols, const int64_t* crow, const int32_t* col,
+                      const void* val, const void* x, int64_t nplanes, void* y, void* stream) {
+  TKBN_GUARD(spmat_interp(dtype, nrows, ncols, crow, col, val, x, nplanes, y, (cudaStream_t)stream));
+}
+
+int tkbn_spmat_interp_adjoint(int dtype, int64_t nrows, int64_t ncols, int64_t nnz, const int32_t* row,
+                              const int32_t* col, const void* val, const void* y, int64_t nplanes, void* x,
+                              void* stream) {
+  TKBN_GUARD(spmat_interp_adjoint(dtype, nrows, ncols, nnz, row, col, val, y, nplanes, x, (cudaStream_t)stream));
 }

@@ -115,14 +115,45 @@ def _check_omega(omega: Tensor, batch: int, what: str = "image") -> None:
         raise ValueError(f"If omega has batch dim, omega batch dimension must match {what}.")
 
 
-def _spmat_unsupported(*args, **kwargs):
-    raise NotImplementedError(
-        "sparse-matrix interpolation (interp_mats) is not provided by torchkbnufft_gb300; "
-        "use table interpolation (omit interp_mats)"
-    )
+def kb_spmat_interp(image: Tensor, interp_mats: Tuple[Tensor, Tensor]) -> Tensor:
+    """Sparse-matrix interpolation grid -> k-space (``functional/interp.py:11-44``)."""
+    from .spmat import SpmatInterp
+
+    image, is_complex = _to_complex(image)
+    return _back(SpmatInterp.apply(image, interp_mats, tuple(image.shape[2:])), is_complex)
 
 
-kb_spmat_interp = _spmat_unsupported
-kb_spmat_interp_adjoint = _spmat_unsupported
-kb_spmat_nufft = _spmat_unsupported
-kb_spmat_nufft_adjoint = _spmat_unsupported
+def kb_spmat_interp_adjoint(data: Tensor, interp_mats: Tuple[Tensor, Tensor], grid_size: Tensor) -> Tensor:
+    """Sparse-matrix adjoint interpolation k-space -> grid (``functional/interp.py:47-79``)."""
+    from .spmat import SpmatInterpAdjoint
+
+    data, is_complex = _to_complex(data)
+    gs = tuple(R.host_values(grid_size, int))
+    return _back(SpmatInterpAdjoint.apply(data, interp_mats, gs), is_complex)
+
+
+def _fft_geom(dtype, im_size, grid_size) -> R.GeomKey:
+    nd = len(R.host_values(grid_size, int))
+    return R.make_geom(dtype, im_size, grid_size, (1,) * nd, (1,) * nd, (0.0,) * nd)
+
+
+def kb_spmat_nufft(image: Tensor, scaling_coef: Tensor, im_size: Tensor, grid_size: Tensor,
+                   interp_mats: Tuple[Tensor, Tensor], norm: Optional[str] = None) -> Tensor:
+    """Forward NUFFT with sparse-matrix interpolation (``functional/nufft.py:16-66``)."""
+    from .spmat import SpmatNufft
+
+    image, is_complex = _to_complex(image)
+    R.norm_code(norm)
+    data = SpmatNufft.apply(image, interp_mats, _fft_geom(image.dtype, im_size, grid_size), scaling_coef, norm)
+    return _back(data, is_complex)
+
+
+def kb_spmat_nufft_adjoint(data: Tensor, scaling_coef: Tensor, im_size: Tensor, grid_size: Tensor,
+                           interp_mats: Tuple[Tensor, Tensor], norm: Optional[str] = None) -> Tensor:
+    """Adjoint NUFFT with sparse-matrix interpolation (``functional/nufft.py:69-123``)."""
+    from .spmat import SpmatNufftAdjoint
+
+    data, is_complex = _to_complex(data)
+    R.norm_code(norm)
+    image = SpmatNufftAdjoint.apply(data, interp_mats, _fft_geom(data.dtype, im_size, grid_size), scaling_coef, norm)
+    return _back(image, is_complex)

@@ -168,7 +168,10 @@ class KbNufft(KbNufftModule):
                 smaps: Optional[Tensor] = None, norm: Optional[str] = None) -> Tensor:
         image, smaps, is_complex = _complex_inputs(image, smaps, "image")
         if interp_mats is not None:
-            return F.kb_spmat_nufft(image, self.scaling_coef, self.im_size, self.grid_size, interp_mats, norm)
+            if smaps is not None:
+                image = image * smaps
+            out = F.kb_spmat_nufft(image, self.scaling_coef, self.im_size, self.grid_size, interp_mats, norm)
+            return out if is_complex else torch.view_as_real(out)
         R.norm_code(norm)
         F._check_omega(omega, image.shape[0])
         if smaps is not None and image.shape[1] != 1:
@@ -189,7 +192,10 @@ class KbNufftAdjoint(KbNufftModule):
                 smaps: Optional[Tensor] = None, norm: Optional[str] = None) -> Tensor:
         data, smaps, is_complex = _complex_inputs(data, smaps, "data")
         if interp_mats is not None:
-            return F.kb_spmat_nufft_adjoint(data, self.scaling_coef, self.im_size, self.grid_size, interp_mats, norm)
+            out = F.kb_spmat_nufft_adjoint(data, self.scaling_coef, self.im_size, self.grid_size, interp_mats, norm)
+            if smaps is not None:
+                out = torch.sum(out * smaps.conj(), dim=1, keepdim=True)
+            return out if is_complex else torch.view_as_real(out)
         R.norm_code(norm)
         F._check_omega(omega, data.shape[0], "data")
         out = NufftAdjoint.apply(data, smaps, omega, self._geom(data.dtype), self._tables(), self.scaling_coef, norm)
