@@ -364,6 +364,166 @@ __host__ __device__ constexpr int ct_min_blocks() {
 //             inverse FFT, rows < N0 written.
 enum ColMode { kColFwd = 0, kColInv = 1, kColToep = 2 };
 
+// Column transforms that read their first stage straight from the grid and
+// write their last stage straight back (compile-time plans): four passes over
+// shared memory per transform instead of eight, so the column pass is bound
+// by HBM rather than by shared memory. The F columns of a unit are adjacent,
+// so every global access is a run of F complex values.
+//   first stage : butterfly j takes rows j + r N/R0 of the column (rows >= nload are zero)
+//   last stage  : outputs (j - k) R + k + r Ns go to rows < nstore, times scale
+template <typename R, int DIR, int N, int RAD, int P>
+__device__ __forceinline__ void stage_ct_gload(const cplx<R>* __restrict__ g, int64_t rstride, int nload, bool cok,
+                                               cplx<R>* __restrict__ out, int f, int tj) {
+  constexpr int F = kFftF, T = N / RAD, ITERS = (T + P - 1) / P;
+#pragma unroll
+  for (int it = 0; it < ITERS; ++it) {
+    const int j = tj + it * P;
+    if (T % P == 0 || j < T) {
+      cplx<R> v[RAD];
+#pragma unroll
+      for (int r = 0; r < RAD; ++r) {
+        const int row = j + r * T;
+        v[r] = (cok && row < nload) ? g[row * rstride] : mk<R>(0, 0);
+      }
+      Dft<R, DIR, RAD>::run(v);
+      cplx<R>* dst = out + j * RAD * F + f;
+#pragma unroll
+      for (int r = 0; r < RAD; ++r) dst[r * F] = v[r];
+    }
+  }
+}
+
+template <typename R, int DIR, int N, int RAD, int NS, int P>
+__device__ __forceinline__ void stage_ct_gstore(const cplx<R>* __restrict__ in, cplx<R>* __restrict__ g,
+                                                int64_t rstride, int nstore, bool cok, R scale, int f, int tj,
+                                                const cplx<R>* __restrict__ tw) {
+  constexpr int F = kFftF, T = N / RAD, TSTEP = N / (NS * RAD), ITERS = (T + P - 1) / P;
+#pragma unroll
+  for (int it = 0; it < ITERS; ++it) {
+    const int j = tj + it * P;
+    if (T % P == 0 || j < T) {
+      const int k = NS == 1 ? 0 : j % NS;
+      const cplx<R>* src = in + j * F + f;
+      cplx<R> v[RAD];
+#pragma unroll
+      for (int r = 0; r < RAD; ++r) v[r] = src[r * T * F];
+      if (NS > 1) {
+        const int kt = k * TSTEP;
+#pragma unroll
+        for (int r = 1; r < RAD; ++r) v[r] = cmul<R>(v[r], twiddle<R, DIR>(tw, r * kt));
+      }
+      Dft<R, DIR, RAD>::run(v);
+      const int base = (j - k) * RAD + k;
+#pragma unroll
+      for (int r = 0; r < RAD; ++r) {
+        const int row = base + r * NS;
+        if (cok && row < nstore) g[row * rstride] = cscale<R>(v[r], scale);
+      }
+    }
+  }
+}
+
+// Whole transform: global -> (stages in shared memory) -> global. With
+// TO_SMEM the last stage stays in shared memory instead (returned buffer).
+template <typename R, int DIR, int N, bool FROM_GLOBAL, bool TO_GLOBAL>
+__device__ __forceinline__ cplx<R>* fft_ct_io(const cplx<R>* gin, cplx<R>* gout, int64_t rstride, int nload,
+                                              int nstore, bool cok, R scale, cplx<R>* buf0, cplx<R>* buf1, int f,
+                                              int tj, const cplx<R>* __restrict__ tw) {
+  using Pl = CtPlan<N>;
+  constexpr int S = Pl::R3 > 1 ? 4 : 3;
+  static_assert(Pl::R2 > 1, "column plans have at least three stages");
+  constexpr int NS1 = Pl::R0, NS2 = Pl::R0 * Pl::R1, NS3 = Pl::R0 * Pl::R1 * Pl::R2;
+  // stage 0
+  if constexpr (FROM_GLOBAL) {
+    stage_ct_gload<R, DIR, N, Pl::R0, Pl::P>(gin, rstride, nload, cok, buf1, f, tj);
+  } else {
+    stage_ct<R, DIR, N, Pl::R0, 1, Pl::P>(buf0, buf1, f, tj, tw);
+  }
+  __syncthreads();
+  // stage 1 (middle for 3 and 4 stages)
+  stage_ct<R, DIR, N, Pl::R1, NS1, Pl::P>(buf1, buf0, f, tj, tw);
+  __syncthreads();
+  if constexpr (S == 4) {
+    stage_ct<R, DIR, N, Pl::R2, NS2, Pl::P>(buf0, buf1, f, tj, tw);
+    __syncthreads();
+    if constexpr (TO_GLOBAL) {
+      stage_ct_gstore<R, DIR, N, Pl::R3, NS3, Pl::P>(buf1, gout, rstride, nstore, cok, scale, f, tj, tw);
+      return nullptr;
+    } else {
+      stage_ct<R, DIR, N, Pl::R3, NS3, Pl::P>(buf1, buf0, f, tj, tw);
+      __syncthreads();
+      return buf0;
+    }
+  } else {
+    if constexpr (TO_GLOBAL) {
+      stage_ct_gstore<R, DIR, N, Pl::R2, NS2, Pl::P>(buf0, gout, rstride, nstore, cok, scale, f, tj, tw);
+      return nullptr;
+    } else {
+      stage_ct<R, DIR, N, Pl::R2, NS2, Pl::P>(buf0, buf1, f, tj, tw);
+      __syncthreads();
+      return buf1;
+    }
+  }
+}
+
+// Column pass with compile-time plan NC: F adjacent columns of one plane per
+// unit, transformed between global memory and two shared buffers.
+template <typename R, int MODE, int NC>
+__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
+    k_fft_cols_io(Fft2dShape s, const cplx<R>* __restrict__ tw, int64_t planes, int64_t C,
+                  const cplx<R>* __restrict__ kernel, int64_t kbatch, int by_channel, R scale,
+                  cplx<R>* __restrict__ grid) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int F = kFftF, P = CtPlan<NC>::P;
+  cplx<R>* buf0 = reinterpret_cast<cplx<R>*>(smem_raw);
+  cplx<R>* buf1 = buf0 + NC * F;
+  const int f = threadIdx.x % F, tj = threadIdx.x / F;
+  const int K1 = s.K1;
+  const int64_t gtot = (int64_t)NC * K1;
+  const int64_t ngrp = (K1 + F - 1) / F;
+  const int64_t units = planes * ngrp;
+  const int nload = MODE == kColInv ? NC : s.N0;
+  const int nstore = MODE == kColFwd ? NC : s.N0;
+  for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const int64_t plane = u / ngrp;
+    const int col = (int)(u - plane * ngrp) * F + f;
+    const bool cok = col < K1;
+    cplx<R>* g = grid + plane * gtot + (cok ? col : 0);
+    if (MODE == kColToep) {
+      cplx<R>* res = fft_ct_io<R, -1, NC, true, false>(g, g, K1, nload, 0, cok, R(1), buf0, buf1, f, tj, tw);
+      cplx<R>* other = res == buf0 ? buf1 : buf0;
+      const int64_t k = kbatch == 1 ? 0 : (by_channel ? plane % C : plane / C);
+      const cplx<R>* kp = kernel + k * gtot + (cok ? col : 0);
+      for (int m0 = tj; m0 < NC; m0 += 4 * P) {
+        cplx<R> kv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int m = m0 + q * P;
+          kv[q] = (cok && m < NC) ? kp[(int64_t)m * K1] : mk<R>(0, 0);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int m = m0 + q * P;
+          if (m < NC) res[m * F + f] = cscale<R>(cmul<R>(res[m * F + f], kv[q]), scale);
+        }
+      }
+      __syncthreads();
+      // second transform: from res through the stages; the unused buffer is the partner
+      if (res == buf0) {
+        fft_ct_io<R, +1, NC, false, true>(nullptr, g, K1, 0, nstore, cok, R(1), buf0, buf1, f, tj, tw);
+      } else {
+        // the result sits in buf1: run the stages with the roles swapped
+        fft_ct_io<R, +1, NC, false, true>(nullptr, g, K1, 0, nstore, cok, R(1), buf1, buf0, f, tj, tw);
+      }
+    } else if (MODE == kColInv) {
+      fft_ct_io<R, +1, NC, true, true>(g, g, K1, nload, nstore, cok, scale, buf0, buf1, f, tj, tw);
+    } else {
+      fft_ct_io<R, -1, NC, true, true>(g, g, K1, nload, nstore, cok, scale, buf0, buf1, f, tj, tw);
+    }
+    __syncthreads();
+  }
+}
+
 template <typename R, int MODE, int NC>
 __global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
     k_fft_cols(Fft2dShape s, FftPlan1 pl, const cplx<R>* __restrict__ tw, int64_t planes, int64_t C,
@@ -716,6 +876,32 @@ static int threads_for(const FftPlan1& pl) {
 template <typename R, int NC>
 static int cols_r(const Fft2dShape& s, const FftPlan1& pl, const void* tw, int mode, int64_t planes, int64_t C,
                   const void* kernel, int64_t kbatch, int by_channel, double scale, void* grid, cudaStream_t st) {
+  if constexpr (NC != 0) {
+    // compile-time plan: first and last stages straight from and to the grid
+    const size_t smem = 2 * (size_t)NC * kFftF * sizeof(cplx<R>);
+    const int threads = CtPlan<NC>::P * kFftF;
+    const int64_t units = planes * ((s.K1 + kFftF - 1) / kFftF);
+    int blocks, rc;
+    switch (mode) {
+      case kColFwd:
+        if ((rc = fft_launch_shape(k_fft_cols_io<R, kColFwd, NC>, threads, smem, units, &blocks))) return rc;
+        k_fft_cols_io<R, kColFwd, NC><<<blocks, threads, smem, st>>>(s, (const cplx<R>*)tw, planes, C, nullptr, 1, 0,
+                                                                     (R)scale, (cplx<R>*)grid);
+        break;
+      case kColInv:
+        if ((rc = fft_launch_shape(k_fft_cols_io<R, kColInv, NC>, threads, smem, units, &blocks))) return rc;
+        k_fft_cols_io<R, kColInv, NC><<<blocks, threads, smem, st>>>(s, (const cplx<R>*)tw, planes, C, nullptr, 1, 0,
+                                                                     (R)scale, (cplx<R>*)grid);
+        break;
+      default:
+        if ((rc = fft_launch_shape(k_fft_cols_io<R, kColToep, NC>, threads, smem, units, &blocks))) return rc;
+        k_fft_cols_io<R, kColToep, NC><<<blocks, threads, smem, st>>>(s, (const cplx<R>*)tw, planes, C,
+                                                                      (const cplx<R>*)kernel, kbatch, by_channel,
+                                                                      (R)scale, (cplx<R>*)grid);
+        break;
+    }
+    return check_cuda(cudaGetLastError(), "fft column pass launch");
+  }
   const size_t smem = 3 * (size_t)pl.n * kFftF * sizeof(cplx<R>);
   const int threads = threads_for<NC>(pl);
   const int64_t units = planes * ((s.K1 + kFftF - 1) / kFftF);

@@ -658,6 +658,7 @@ struct OwnLaunch {
   SrcSpan span;
   const int4* vlist;     // 2D: per-tile lists of the points that reach the tile (else null)
   const int32_t* voff;   // first list entry of each tile key
+  const int32_t* koff;   // 2D lists sorted by footprint start: first entry of each start (else null)
 };
 
 template <typename R, int D>
@@ -1019,12 +1020,13 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
 // derivative tables at the exact (unrounded) position.
 // K4 (owned tiles, registers): the common 2D case — J = 6 in both dims,
 // 16 coils per job, 16 x 14 tiles, complex64. Lane (coil c, row 2*warp + g)
-// keeps the 14 cells of its row of its coil plane in registers. A staged
-// point's column offset within the tile is the same for every lane of the
-// warp, so a switch on it selects fully unrolled code with static register
-// indices; accumulation needs no shared-memory read-modify-write. Points are
-// staged 256 at a time (every thread stages one candidate), two barriers per
-// batch. Cells outside the tile (edge tiles narrower than 14) accumulate
+// keeps the 14 cells of its row of its coil plane in registers. The tile's
+// point list is sorted by footprint start (column offset, then row offset),
+// so the points of one column offset that reach a warp's rows are one run of
+// the list: a loop per column offset, unrolled over the 19 offsets, updates
+// registers with static indices and needs no per-point branch; accumulation
+// needs no shared-memory read-modify-write. Points are staged 256 at a time,
+// two barriers per batch. Cells outside the tile (edge tiles narrower than 14) accumulate
 // contributions that are never written; those cells belong to the wrapped
 // tile, which gets the same points with its own column offsets.
 constexpr int kNBR = 256;  // staged points per batch (== kThreads)
@@ -1055,6 +1057,40 @@ __device__ __forceinline__ void reg_add_point(int lx, float2 (&racc)[TXR], float
     default:
       break;
   }
+}
+
+// Footprint starts of a 16 x 14 tile with J = 6: row offsets -5 .. 15 (21),
+// column offsets -5 .. 13 (19); start k = (rx + 5) * 21 + ry + 5.
+constexpr int kRegKeyRows = kRegTileY + 5, kRegKeys = kRegKeyRows * (kRegTileX + 5);
+
+// Points of the batch (list entries q0 .. q0 + nv - 1) with column offset
+// LX - 5 .. 13 that reach rows [r_lo, r_hi): for each LX, entries
+// ko[k(LX, r_lo - 5)] .. ko[k(LX, r_hi - 1) + 1] of the sorted list. With
+// point groups (NG > 1) group g takes the batch positions p = g mod NG.
+template <int CC, int NG, int LXI>
+__device__ __forceinline__ void reg_columns(const int32_t* __restrict__ ko, int r_lo, int r_hi, int q0, int nv,
+                                           int grp, const float2* __restrict__ sfac, const float2* __restrict__ sv,
+                                           const int2* __restrict__ sloc, int myrow, bool rowok, int c,
+                                           float2 (&racc)[kRegTileX]) {
+  constexpr int NJ = 6, LX = LXI - 5;
+  const int kb = LXI * kRegKeyRows;
+  int p = max(__ldg(ko + kb + r_lo) - q0, 0);
+  const int e = min(__ldg(ko + kb + r_hi + 5) - q0, nv);
+  if (NG > 1) p += (grp - p % NG + NG) % NG;
+  for (; p < e; p += NG) {
+    const int jy = myrow - sloc[p].x;
+    const float2* fp = sfac + p * (2 * NJ);
+    float2 fy = make_float2(0.f, 0.f);
+    if (rowok && (unsigned)jy < (unsigned)NJ) fy = fp[jy];
+    const float2 vy = cmul<float>(sv[p * CC + c], fy);
+    const float4* fx4 = reinterpret_cast<const float4*>(fp + NJ);
+    const float4 f01 = fx4[0], f23 = fx4[1], f45 = fx4[2];
+    const float2 fx[6] = {make_float2(f01.x, f01.y), make_float2(f01.z, f01.w), make_float2(f23.x, f23.y),
+                          make_float2(f23.z, f23.w), make_float2(f45.x, f45.y), make_float2(f45.z, f45.w)};
+    reg_add_cols<kRegTileX, LX>(racc, vy, fx);
+  }
+  if constexpr (LXI + 1 < kRegTileX + 5)
+    reg_columns<CC, NG, LXI + 1>(ko, r_lo, r_hi, q0, nv, grp, sfac, sv, sloc, myrow, rowok, c, racc);
 }
 
 // vec_ok: the grid pointer is 16-byte aligned and K1 is even, so every
@@ -1095,6 +1131,7 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
     const int ncl = (int)min((int64_t)min(CC, a.Cc), a.C - c0);
     const bool rowok = myrow < ext[0];
     const int64_t vbase = a.voff[it.key];
+    const int32_t* __restrict__ ko = a.koff + (int64_t)it.key * (kRegKeys + 1);
     float2 racc[kRegTileX];
 #pragma unroll
     for (int x = 0; x < kRegTileX; ++x) racc[x] = make_float2(0.f, 0.f);
@@ -1131,31 +1168,15 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
         sv[e] = v;
       }
       __syncthreads();
-      // B: each warp applies the staged points of its group that touch its rows
-      const int r_lo = (warp % WPT) * RPW, r_hi = min(r_lo + RPW, ext[0]);
-#pragma unroll 1
-      for (int h = 0; h < kNBR / 32; ++h) {
-        const int p = h * 32 + lane;
-        bool tch = false;
-        if (p < nv && (NG == 1 || p % NG == grp)) {
-          const int ly = sloc[p].x;
-          tch = max(r_lo, ly) < min(r_hi, ly + NJ);
-        }
-        for (unsigned msk = __ballot_sync(0xffffffffu, tch); msk; msk &= msk - 1) {
-          const int pt = h * 32 + __ffs(msk) - 1;
-          const int2 loc = sloc[pt];
-          const int jy = myrow - loc.x;
-          if (rowok && (unsigned)jy < (unsigned)NJ) {
-            const float2* fp = sfac + pt * (D * NJ);
-            const float2 vy = cmul<float>(sv[pt * CC + c], fp[jy]);
-            const float4* fx4 = reinterpret_cast<const float4*>(fp + NJ);
-            const float4 f01 = fx4[0], f23 = fx4[1], f45 = fx4[2];
-            const float2 fx[6] = {make_float2(f01.x, f01.y), make_float2(f01.z, f01.w), make_float2(f23.x, f23.y),
-                                  make_float2(f23.z, f23.w), make_float2(f45.x, f45.y), make_float2(f45.z, f45.w)};
-            reg_add_point<kRegTileX>(loc.y, racc, vy, fx);
-          }
-        }
-        if ((h + 1) * 32 >= nv) break;
+      // B: the list is sorted by footprint start (column offset, then row
+      // offset), so for each column offset LX the points that reach this
+      // warp's rows [r_lo, r_hi) — row offsets r_lo - 5 .. r_hi - 1 — are one
+      // run of the batch; LX is a template argument, so every update uses
+      // static register indices. Lanes whose row the footprint misses add 0.
+      {
+        const int r_lo = (warp % WPT) * RPW, r_hi = min(r_lo + RPW, ext[0]);
+        if (r_lo < r_hi)
+          reg_columns<CC, NG, 0>(ko, r_lo, r_hi, q0, nv, grp, sfac, sv, sloc, myrow, rowok, c, racc);
       }
       __syncthreads();
     }
@@ -1898,6 +1919,7 @@ static OwnLaunch make_own(const InterpPlan& ip, const char* ws, int D) {
   o.span = ip.L.span;
   o.vlist = ip.L.vlist ? (const int4*)(ws + ip.L.off_vlist) : nullptr;
   o.voff = ip.L.vlist ? (const int32_t*)(ws + ip.L.off_voff) : nullptr;
+  o.koff = ip.L.ksort ? (const int32_t*)(ws + ip.L.off_koff) : nullptr;
   return o;
 }
 
@@ -1914,8 +1936,8 @@ static size_t own_smem(const OwnLaunch& o) {
 // per-tile point lists (any coil count; CC = max(2, coils per job)).
 template <typename R, int D, int JC>
 static bool reg_eligible(const InterpPlan& ip, const OwnLaunch& o) {
-  return std::is_same<R, float>::value && D == 2 && JC == 6 && o.vlist && o.Cc <= kRegCoils &&
-         ip.L.tile[0] == kRegTileY && ip.L.tile[1] == kRegTileX;
+  return std::is_same<R, float>::value && D == 2 && JC == 6 && o.vlist && o.koff && o.Cc <= kRegCoils &&
+         ip.L.tile[0] == kRegTileY && ip.L.tile[1] == kRegTileX && ip.L.knk == kRegKeys;
 }
 
 static int reg_cc(int Cc) { return Cc < 2 ? 2 : Cc; }

@@ -231,6 +231,69 @@ __global__ void __launch_bounds__(kValidThreads) k_tile_valid(Geo<R> geo, const 
   }
 }
 
+// 2D lists sorted by footprint start, stable (equal starts keep list order):
+// one warp per tile counts the starts (k = (rx + ox) * ny + ry + oy), scans
+// the counts into koff[tile][0 .. nk] and places the entries 32 at a time in
+// list order, ranking equal starts within the 32 by lane.
+constexpr int kSortWarps = 8, kSortMaxKeys = 1024;
+__global__ void __launch_bounds__(kSortWarps * 32)
+    k_tile_keysort(int64_t nkeys, int ny, int oy, int ox, int nk, const int32_t* __restrict__ voff,
+                   const int32_t* __restrict__ vcount, const int4* __restrict__ vin, int4* __restrict__ vout,
+                   int32_t* __restrict__ koff) {
+  extern __shared__ int32_t s_cur[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int32_t* cur = s_cur + warp * (nk + 1);
+  for (int64_t key = (int64_t)blockIdx.x * kSortWarps + warp; key < nkeys; key += (int64_t)gridDim.x * kSortWarps) {
+    const int64_t base = voff[key];
+    const int cnt = vcount[key];
+    for (int k = lane; k <= nk; k += 32) cur[k] = 0;
+    __syncwarp();
+    for (int q = lane; q < cnt; q += 32) {
+      const int4 e = vin[base + q];
+      atomicAdd(&cur[(e.w + ox) * ny + e.z + oy], 1);
+    }
+    __syncwarp();
+    // exclusive scan of cur[0 .. nk]: lane l takes a run of `per` entries
+    const int per = (nk + 1 + 31) / 32, lo = lane * per, hi = min(lo + per, nk + 1);
+    int sum = 0;
+    for (int k = lo; k < hi; ++k) sum += cur[k];
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int run = incl - sum;
+    for (int k = lo; k < hi; ++k) {
+      const int c = cur[k];
+      cur[k] = run;
+      run += c;
+    }
+    __syncwarp();
+    int32_t* ko = koff + key * (nk + 1);
+    for (int k = lane; k <= nk; k += 32) ko[k] = cur[k];
+    __syncwarp();
+    for (int q0 = 0; q0 < cnt; q0 += 32) {
+      const int q = q0 + lane;
+      const bool act = q < cnt;
+      int4 e = make_int4(0, 0, 0, 0);
+      int k = nk;  // idle lanes share the end slot and write nothing
+      if (act) {
+        e = vin[base + q];
+        k = (e.w + ox) * ny + e.z + oy;
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, k);
+      const int rank = __popc(peers & ((1u << lane) - 1u));
+      const int pos = cur[k] + rank;
+      __syncwarp();
+      if (act && rank == 0) cur[k] += __popc(peers);
+      __syncwarp();
+      if (act) vout[base + pos] = e;
+    }
+    __syncwarp();
+  }
+}
+
 // Adjoint sub-jobs: candidates [start, start+len) of output tile `key`; pad = 1
 // when the tile is split over several sub-jobs (their results are added with
 // atomics into a pre-zeroed tile; unsplit tiles are written with plain stores).
@@ -426,6 +489,9 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   // the owned-tile kernels' source limits: 16 source tiles in 2D, 27 in 3D
   L->vlist = L->owned_ok && ((g->ndim == 2 && L->span.ncombo <= 16) || (g->ndim == 3 && L->span.ncombo <= 27));
   L->max_valid = L->vlist ? L->span.ncombo * L->npts_total : 0;
+  L->kny = L->tile[0] + g->numpoints[0] - 1;
+  L->knk = g->ndim == 2 ? L->kny * (L->tile[1] + g->numpoints[1] - 1) : 0;
+  L->ksort = L->vlist && g->ndim == 2 && L->knk <= tkbn::kSortMaxKeys;
   L->max_subjobs = 2 * L->nkeys + (L->span.ncombo * L->npts_total + L->adj_chunk - 1) / L->adj_chunk;
   int sbits = 1;
   while (((int64_t)1 << sbits) <= L->adj_chunk + 1) ++sbits;
@@ -490,6 +556,10 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   o = align_up(o + (L->vlist ? 4 * (L->nkeys + 1) : 0));
   L->off_vlist = o;
   o = align_up(o + sizeof(int4) * L->max_valid);
+  L->off_vtmp = o;
+  o = align_up(o + (L->ksort ? sizeof(int4) * L->max_valid : 0));
+  L->off_koff = o;
+  o = align_up(o + (L->ksort ? 4 * L->nkeys * (L->knk + 1) : 0));
   L->off_coords = o;
   o = align_up(o + rsize * g->ndim * n);
   L->off_phase = o;
@@ -573,8 +643,16 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
     tb = L.cub_bytes;
     if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, vcount, voff, (int)L.nkeys, s) != cudaSuccess)
       return set_error(TKBN_ERR_CUDA, "scan failed");
+    int4* vdst = L.ksort ? (int4*)(ws + L.off_vtmp) : vlist;
     kv<<<wblocks, kValidThreads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys, L.span, voff,
-                                         vcount, vlist);
+                                         vcount, vdst);
+    if (L.ksort) {
+      const int64_t sb = (L.nkeys + kSortWarps - 1) / kSortWarps;
+      const size_t ssmem = (size_t)kSortWarps * (L.knk + 1) * sizeof(int32_t);
+      k_tile_keysort<<<(int)(sb < 152 * 8 ? sb : 152 * 8), kSortWarps * 32, ssmem, s>>>(
+          L.nkeys, L.kny, g->numpoints[0] - 1, g->numpoints[1] - 1, L.knk, voff, vcount, vdst, vlist,
+          (int32_t*)(ws + L.off_koff));
+    }
   }
   // adjoint sub-jobs (output tiles, heavy ones split), longest first
   {

@@ -248,10 +248,15 @@ struct PointsLayout {
   // per trajectory; the adjoint's sub-jobs are ranges of these lists.
   bool vlist;
   int64_t max_valid;  // upper bound on list entries (ncombo * npts_total)
+  // 2D lists sorted by footprint start (column offset, then row offset): the
+  // entries of each start are one run; koff[tile][k] is the first entry of
+  // start k = (rx + J1 - 1) * kny + (ry + J0 - 1), k = 0 .. knk (knk = end).
+  bool ksort;
+  int kny, knk;
   size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
       off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_phase,
       off_tile_work, off_tile_nsub, off_tile_suboff, off_sj_raw, off_adj_jobs, off_sj_keys_in, off_sj_keys,
-      off_sj_vals_in, off_sj_vals, off_vcount, off_voff, off_vlist, off_cub;
+      off_sj_vals_in, off_sj_vals, off_vcount, off_voff, off_vlist, off_vtmp, off_koff, off_cub;
   size_t cub_bytes;
   size_t total;
 };
