@@ -364,16 +364,15 @@ __host__ __device__ constexpr int ct_min_blocks() {
 //             inverse FFT, rows < N0 written.
 enum ColMode { kColFwd = 0, kColInv = 1, kColToep = 2 };
 
-// Column transforms that read their first stage straight from the grid and
-// write their last stage straight back (compile-time plans): four passes over
-// shared memory per transform instead of eight, so the column pass is bound
-// by HBM rather than by shared memory. The F columns of a unit are adjacent,
-// so every global access is a run of F complex values.
-//   first stage : butterfly j takes rows j + r N/R0 of the column (rows >= nload are zero)
-//   last stage  : outputs (j - k) R + k + r Ns go to rows < nstore, times scale
-template <typename R, int DIR, int N, int RAD, int P>
-__device__ __forceinline__ void stage_ct_gload(const cplx<R>* __restrict__ g, int64_t rstride, int nload, bool cok,
-                                               cplx<R>* __restrict__ out, int f, int tj) {
+// Transforms that read their first stage straight from global memory and
+// write their last stage straight back (compile-time plans): four passes
+// over shared memory per transform instead of eight. The caller supplies the
+// element access as functors: ld(i) returns input element i (zero where the
+// input is padded), st(i, v) takes output element i.
+//   first stage : butterfly j takes inputs j + r N/R0
+//   last stage  : butterfly j gives outputs (j - k) R + k + r Ns
+template <typename R, int DIR, int N, int RAD, int P, class LD>
+__device__ __forceinline__ void stage_ct_first(LD ld, cplx<R>* __restrict__ out, int f, int tj) {
   constexpr int F = kFftF, T = N / RAD, ITERS = (T + P - 1) / P;
 #pragma unroll
   for (int it = 0; it < ITERS; ++it) {
@@ -381,10 +380,7 @@ __device__ __forceinline__ void stage_ct_gload(const cplx<R>* __restrict__ g, in
     if (T % P == 0 || j < T) {
       cplx<R> v[RAD];
 #pragma unroll
-      for (int r = 0; r < RAD; ++r) {
-        const int row = j + r * T;
-        v[r] = (cok && row < nload) ? g[row * rstride] : mk<R>(0, 0);
-      }
+      for (int r = 0; r < RAD; ++r) v[r] = ld(j + r * T);
       Dft<R, DIR, RAD>::run(v);
       cplx<R>* dst = out + j * RAD * F + f;
 #pragma unroll
@@ -393,10 +389,9 @@ __device__ __forceinline__ void stage_ct_gload(const cplx<R>* __restrict__ g, in
   }
 }
 
-template <typename R, int DIR, int N, int RAD, int NS, int P>
-__device__ __forceinline__ void stage_ct_gstore(const cplx<R>* __restrict__ in, cplx<R>* __restrict__ g,
-                                                int64_t rstride, int nstore, bool cok, R scale, int f, int tj,
-                                                const cplx<R>* __restrict__ tw) {
+template <typename R, int DIR, int N, int RAD, int NS, int P, class ST>
+__device__ __forceinline__ void stage_ct_last(const cplx<R>* __restrict__ in, ST st, int f, int tj,
+                                              const cplx<R>* __restrict__ tw) {
   constexpr int F = kFftF, T = N / RAD, TSTEP = N / (NS * RAD), ITERS = (T + P - 1) / P;
 #pragma unroll
   for (int it = 0; it < ITERS; ++it) {
@@ -415,39 +410,34 @@ __device__ __forceinline__ void stage_ct_gstore(const cplx<R>* __restrict__ in, 
       Dft<R, DIR, RAD>::run(v);
       const int base = (j - k) * RAD + k;
 #pragma unroll
-      for (int r = 0; r < RAD; ++r) {
-        const int row = base + r * NS;
-        if (cok && row < nstore) g[row * rstride] = cscale<R>(v[r], scale);
-      }
+      for (int r = 0; r < RAD; ++r) st(base + r * NS, v[r]);
     }
   }
 }
 
-// Whole transform: global -> (stages in shared memory) -> global. With
-// TO_SMEM the last stage stays in shared memory instead (returned buffer).
-template <typename R, int DIR, int N, bool FROM_GLOBAL, bool TO_GLOBAL>
-__device__ __forceinline__ cplx<R>* fft_ct_io(const cplx<R>* gin, cplx<R>* gout, int64_t rstride, int nload,
-                                              int nstore, bool cok, R scale, cplx<R>* buf0, cplx<R>* buf1, int f,
-                                              int tj, const cplx<R>* __restrict__ tw) {
+// Whole transform. FROM_GLOBAL: the first stage reads through ld, else from
+// buf0. TO_GLOBAL: the last stage writes through st (returns nullptr), else
+// it stays in shared memory (the returned buffer).
+template <typename R, int DIR, int N, bool FROM_GLOBAL, bool TO_GLOBAL, class LD, class ST>
+__device__ __forceinline__ cplx<R>* fft_ct_io(LD ld, ST st, cplx<R>* buf0, cplx<R>* buf1, int f, int tj,
+                                              const cplx<R>* __restrict__ tw) {
   using Pl = CtPlan<N>;
   constexpr int S = Pl::R3 > 1 ? 4 : 3;
-  static_assert(Pl::R2 > 1, "column plans have at least three stages");
+  static_assert(Pl::R2 > 1, "direct-IO plans have at least three stages");
   constexpr int NS1 = Pl::R0, NS2 = Pl::R0 * Pl::R1, NS3 = Pl::R0 * Pl::R1 * Pl::R2;
-  // stage 0
   if constexpr (FROM_GLOBAL) {
-    stage_ct_gload<R, DIR, N, Pl::R0, Pl::P>(gin, rstride, nload, cok, buf1, f, tj);
+    stage_ct_first<R, DIR, N, Pl::R0, Pl::P>(ld, buf1, f, tj);
   } else {
     stage_ct<R, DIR, N, Pl::R0, 1, Pl::P>(buf0, buf1, f, tj, tw);
   }
   __syncthreads();
-  // stage 1 (middle for 3 and 4 stages)
   stage_ct<R, DIR, N, Pl::R1, NS1, Pl::P>(buf1, buf0, f, tj, tw);
   __syncthreads();
   if constexpr (S == 4) {
     stage_ct<R, DIR, N, Pl::R2, NS2, Pl::P>(buf0, buf1, f, tj, tw);
     __syncthreads();
     if constexpr (TO_GLOBAL) {
-      stage_ct_gstore<R, DIR, N, Pl::R3, NS3, Pl::P>(buf1, gout, rstride, nstore, cok, scale, f, tj, tw);
+      stage_ct_last<R, DIR, N, Pl::R3, NS3, Pl::P>(buf1, st, f, tj, tw);
       return nullptr;
     } else {
       stage_ct<R, DIR, N, Pl::R3, NS3, Pl::P>(buf1, buf0, f, tj, tw);
@@ -456,7 +446,7 @@ __device__ __forceinline__ cplx<R>* fft_ct_io(const cplx<R>* gin, cplx<R>* gout,
     }
   } else {
     if constexpr (TO_GLOBAL) {
-      stage_ct_gstore<R, DIR, N, Pl::R2, NS2, Pl::P>(buf0, gout, rstride, nstore, cok, scale, f, tj, tw);
+      stage_ct_last<R, DIR, N, Pl::R2, NS2, Pl::P>(buf0, st, f, tj, tw);
       return nullptr;
     } else {
       stage_ct<R, DIR, N, Pl::R2, NS2, Pl::P>(buf0, buf1, f, tj, tw);
@@ -466,8 +456,16 @@ __device__ __forceinline__ cplx<R>* fft_ct_io(const cplx<R>* gin, cplx<R>* gout,
   }
 }
 
+struct NoIo {
+  template <typename... A>
+  __device__ __forceinline__ float2 operator()(A...) const {
+    return make_float2(0.f, 0.f);
+  }
+};
+
 // Column pass with compile-time plan NC: F adjacent columns of one plane per
-// unit, transformed between global memory and two shared buffers.
+// unit (every global access is a run of F complex values), transformed
+// between global memory and two shared buffers.
 template <typename R, int MODE, int NC>
 __global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
     k_fft_cols_io(Fft2dShape s, const cplx<R>* __restrict__ tw, int64_t planes, int64_t C,
@@ -489,9 +487,13 @@ __global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
     const int col = (int)(u - plane * ngrp) * F + f;
     const bool cok = col < K1;
     cplx<R>* g = grid + plane * gtot + (cok ? col : 0);
+    auto ld = [&](int row) { return (cok && row < nload) ? g[(int64_t)row * K1] : mk<R>(0, 0); };
+    const R osc = MODE == kColToep ? R(1) : scale;
+    auto st = [&](int row, cplx<R> v) {
+      if (cok && row < nstore) g[(int64_t)row * K1] = cscale<R>(v, osc);
+    };
     if (MODE == kColToep) {
-      cplx<R>* res = fft_ct_io<R, -1, NC, true, false>(g, g, K1, nload, 0, cok, R(1), buf0, buf1, f, tj, tw);
-      cplx<R>* other = res == buf0 ? buf1 : buf0;
+      cplx<R>* res = fft_ct_io<R, -1, NC, true, false>(ld, NoIo{}, buf0, buf1, f, tj, tw);
       const int64_t k = kbatch == 1 ? 0 : (by_channel ? plane % C : plane / C);
       const cplx<R>* kp = kernel + k * gtot + (cok ? col : 0);
       for (int m0 = tj; m0 < NC; m0 += 4 * P) {
@@ -508,17 +510,15 @@ __global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
         }
       }
       __syncthreads();
-      // second transform: from res through the stages; the unused buffer is the partner
-      if (res == buf0) {
-        fft_ct_io<R, +1, NC, false, true>(nullptr, g, K1, 0, nstore, cok, R(1), buf0, buf1, f, tj, tw);
-      } else {
-        // the result sits in buf1: run the stages with the roles swapped
-        fft_ct_io<R, +1, NC, false, true>(nullptr, g, K1, 0, nstore, cok, R(1), buf1, buf0, f, tj, tw);
-      }
+      // second transform from res; the other buffer is its partner
+      if (res == buf0)
+        fft_ct_io<R, +1, NC, false, true>(NoIo{}, st, buf0, buf1, f, tj, tw);
+      else
+        fft_ct_io<R, +1, NC, false, true>(NoIo{}, st, buf1, buf0, f, tj, tw);
     } else if (MODE == kColInv) {
-      fft_ct_io<R, +1, NC, true, true>(g, g, K1, nload, nstore, cok, scale, buf0, buf1, f, tj, tw);
+      fft_ct_io<R, +1, NC, true, true>(ld, st, buf0, buf1, f, tj, tw);
     } else {
-      fft_ct_io<R, -1, NC, true, true>(g, g, K1, nload, nstore, cok, scale, buf0, buf1, f, tj, tw);
+      fft_ct_io<R, -1, NC, true, true>(ld, st, buf0, buf1, f, tj, tw);
     }
     __syncthreads();
   }
@@ -657,6 +657,127 @@ __global__ void __launch_bounds__(ct_threads<NC>()) k_fft_rows_pad(Fft2dShape s,
       if (cok) {
         cplx<R>* g = grid + (b * C + c) * gtot + (int64_t)n0 * K1;
         for (int m = tj; m < K1; m += P) g[m] = res[m * F + f];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Forward row pass with compile-time plan NC = K1: the first stage reads
+// image [* smaps] * scaling * scale straight from global memory (zero past
+// N1), the last stage writes the grid row.
+template <typename R, int NC>
+__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
+    k_fft_rows_pad_io(Fft2dShape s, const cplx<R>* __restrict__ tw, int64_t B, int64_t C, int64_t ci,
+                      const cplx<R>* __restrict__ image, const cplx<R>* __restrict__ smaps, int64_t sb,
+                      const cplx<R>* __restrict__ scaling, R scale, cplx<R>* __restrict__ grid) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int F = kFftF;
+  cplx<R>* buf0 = reinterpret_cast<cplx<R>*>(smem_raw);
+  cplx<R>* buf1 = buf0 + NC * F;
+  const int f = threadIdx.x % F, tj = threadIdx.x / F;
+  const int N0 = s.N0, N1 = s.N1;
+  const int64_t ntot = (int64_t)N0 * N1, gtot = (int64_t)s.K0 * NC;
+  const int64_t units = B * N0;
+  for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const int64_t b = u / N0;
+    const int n0 = (int)(u - b * N0);
+    const cplx<R>* sc = scaling ? scaling + (int64_t)n0 * N1 : nullptr;
+    for (int64_t c0 = 0; c0 < C; c0 += F) {
+      const int64_t c = c0 + f;
+      const bool cok = c < C;
+      const cplx<R>* im = image + (b * ci + (ci == 1 ? 0 : (cok ? c : 0))) * ntot + (int64_t)n0 * N1;
+      const cplx<R>* sm = smaps ? smaps + ((sb == 1 ? 0 : b) * C + (cok ? c : 0)) * ntot + (int64_t)n0 * N1 : nullptr;
+      cplx<R>* g = grid + (b * C + (cok ? c : 0)) * gtot + (int64_t)n0 * NC;
+      auto ld = [&](int m) {
+        cplx<R> v = mk<R>(0, 0);
+        if (cok && m < N1) {
+          v = im[m];
+          if (sm) v = cmul<R>(v, sm[m]);
+          if (sc) v = cmul<R>(v, sc[m]);
+          v = cscale<R>(v, scale);
+        }
+        return v;
+      };
+      auto st = [&](int m, cplx<R> v) {
+        if (cok) g[m] = v;
+      };
+      fft_ct_io<R, -1, NC, true, true>(ld, st, buf0, buf1, f, tj, tw);
+      __syncthreads();
+    }
+  }
+}
+
+// Inverse row pass with compile-time plan NC = K1: the first stage reads the
+// grid row, the last stage applies conj(scaling) * scale and either writes
+// each coil's cropped row or (smaps) multiplies by conj(smaps), sums the F
+// coils of a butterfly's lanes with shuffles and adds the group to a running
+// coil sum (shared memory, one owner thread per element; the last group
+// writes the sum). The coil sum is taken in the same order as the
+// shared-memory kernel's.
+template <typename R, int NC>
+__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
+    k_ifft_rows_crop_io(Fft2dShape s, const cplx<R>* __restrict__ tw, int64_t B, int64_t C,
+                        const cplx<R>* __restrict__ grid, const cplx<R>* __restrict__ smaps, int64_t sb,
+                        const cplx<R>* __restrict__ scaling, R scale, cplx<R>* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int F = kFftF;
+  static_assert((F & (F - 1)) == 0 && F <= 32, "coil group fits a warp");
+  cplx<R>* buf0 = reinterpret_cast<cplx<R>*>(smem_raw);
+  cplx<R>* buf1 = buf0 + NC * F;
+  cplx<R>* acc = buf1 + NC * F;  // [N1] running coil sum (smaps only)
+  const int f = threadIdx.x % F, tj = threadIdx.x / F;
+  const unsigned gmask = ((1u << F) - 1u) << ((threadIdx.x & 31) & ~(F - 1));
+  const int N0 = s.N0, N1 = s.N1;
+  const int64_t ntot = (int64_t)N0 * N1, gtot = (int64_t)s.K0 * NC;
+  const int64_t units = B * N0;
+  for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const int64_t b = u / N0;
+    const int n0 = (int)(u - b * N0);
+    const cplx<R>* sc = scaling ? scaling + (int64_t)n0 * N1 : nullptr;
+    for (int64_t c0 = 0; c0 < C; c0 += F) {
+      const int64_t c = c0 + f;
+      const bool cok = c < C;
+      const cplx<R>* g = grid + (b * C + (cok ? c : 0)) * gtot + (int64_t)n0 * NC;
+      auto ld = [&](int m) { return cok ? g[m] : mk<R>(0, 0); };
+      if (smaps) {
+        const cplx<R>* sm = smaps + ((sb == 1 ? 0 : b) * C + (cok ? c : 0)) * ntot + (int64_t)n0 * N1;
+        cplx<R>* orow = out + b * ntot + (int64_t)n0 * N1;
+        const bool first = c0 == 0, last = c0 + F >= C;
+        // m is the same for the F lanes of a butterfly, so they shuffle together
+        auto st = [&](int m, cplx<R> v) {
+          if (m < N1) {
+            cplx<R> t = mk<R>(0, 0);
+            if (cok) {
+              cplx<R> w = sc ? cconj<R>(sc[m]) : mk<R>(1, 0);
+              w = cscale<R>(w, scale);
+              t = cmul<R>(cmul<R>(v, w), cconj<R>(sm[m]));
+            }
+#pragma unroll
+            for (int o = 1; o < F; o <<= 1) {
+              t.x += __shfl_xor_sync(gmask, t.x, o);
+              t.y += __shfl_xor_sync(gmask, t.y, o);
+            }
+            if (f == 0) {
+              if (!first) t = cadd<R>(acc[m], t);
+              if (last)
+                orow[m] = t;
+              else
+                acc[m] = t;
+            }
+          }
+        };
+        fft_ct_io<R, +1, NC, true, true>(ld, st, buf0, buf1, f, tj, tw);
+      } else {
+        cplx<R>* orow = out + (b * C + (cok ? c : 0)) * ntot + (int64_t)n0 * N1;
+        auto st = [&](int m, cplx<R> v) {
+          if (cok && m < N1) {
+            cplx<R> w = sc ? cconj<R>(sc[m]) : mk<R>(1, 0);
+            w = cscale<R>(w, scale);
+            orow[m] = cmul<R>(v, w);
+          }
+        };
+        fft_ct_io<R, +1, NC, true, true>(ld, st, buf0, buf1, f, tj, tw);
       }
       __syncthreads();
     }
@@ -931,6 +1052,17 @@ template <typename R, int NC>
 static int rows_pad_r(const Fft2dShape& s, const FftPlan1& pl, const void* tw, int64_t B, int64_t C, int64_t ci,
                       const void* image, const void* smaps, int64_t sb, const void* scaling, double scale, void* grid,
                       cudaStream_t st) {
+  if constexpr (NC != 0) {
+    const size_t smem = 2 * (size_t)NC * kFftF * sizeof(cplx<R>);
+    const int threads = CtPlan<NC>::P * kFftF;
+    int blocks;
+    int rc = fft_launch_shape(k_fft_rows_pad_io<R, NC>, threads, smem, B * s.N0, &blocks);
+    if (rc) return rc;
+    k_fft_rows_pad_io<R, NC><<<blocks, threads, smem, st>>>(s, (const cplx<R>*)tw, B, C, ci, (const cplx<R>*)image,
+                                                            (const cplx<R>*)smaps, sb, (const cplx<R>*)scaling,
+                                                            (R)scale, (cplx<R>*)grid);
+    return check_cuda(cudaGetLastError(), "fft row pass launch");
+  }
   const size_t smem = 2 * (size_t)pl.n * kFftF * sizeof(cplx<R>);
   const int threads = threads_for<NC>(pl);
   int blocks;
@@ -946,6 +1078,17 @@ template <typename R, int NC>
 static int rows_crop_r(const Fft2dShape& s, const FftPlan1& pl, const void* tw, int64_t B, int64_t C,
                        const void* grid, const void* smaps, int64_t sb, const void* scaling, double scale, void* out,
                        cudaStream_t st) {
+  if constexpr (NC != 0) {
+    const size_t smem = (2 * (size_t)NC * kFftF + s.N1) * sizeof(cplx<R>);
+    const int threads = CtPlan<NC>::P * kFftF;
+    int blocks;
+    int rc = fft_launch_shape(k_ifft_rows_crop_io<R, NC>, threads, smem, B * s.N0, &blocks);
+    if (rc) return rc;
+    k_ifft_rows_crop_io<R, NC><<<blocks, threads, smem, st>>>(s, (const cplx<R>*)tw, B, C, (const cplx<R>*)grid,
+                                                              (const cplx<R>*)smaps, sb, (const cplx<R>*)scaling,
+                                                              (R)scale, (cplx<R>*)out);
+    return check_cuda(cudaGetLastError(), "ifft row pass launch");
+  }
   const size_t smem = (3 * (size_t)pl.n * kFftF + s.N1) * sizeof(cplx<R>);
   const int threads = threads_for<NC>(pl);
   int blocks;

@@ -440,25 +440,37 @@ __device__ __forceinline__ void fwd_job(const Geo<R>& geo, const Launch& a, cons
 
 // ---------------------------------------------------------------- K3, coil pairs
 // Gather for 2D complex64, J = 6, CC coils per job (2, 4, 8 or 16): the tile
-// patch is stored coil-fastest ([cell][CC]), so a lane reads two coils of a
+// patch is stored coil-fastest ([cell][CC + 2]), so a lane reads two coils of a
 // cell with one 16-byte load and the point's per-lane work (coordinates,
 // table factors, addressing) is shared by two coils. Lanes are (point slot,
 // coil pair): 64 / CC points per warp.
+// Coil-pair patch cell: CC coils then 16 unused bytes, so that lanes copying
+// consecutive columns of one coil write to different banks while the lanes
+// of a point still read one cell's CC coils as contiguous 16-byte pairs.
+template <int CC>
+__host__ __device__ constexpr int pair_cell_stride() {
+  return CC + 2;
+}
+
 template <int CC>
 __device__ __forceinline__ void load_patch_pairs(const Geo<float>& geo, const float2* __restrict__ grid,
                                                  int64_t plane0, int64_t gtot, int ncl, const int* origin,
                                                  float2* patch) {
+  constexpr int CS = pair_cell_stride<CC>();
   const int PX = geo.P[1], PY = geo.P[0], KX = geo.K[1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int rr = warp; rr < PY; rr += kWarps) {
     const int64_t rbase = patch_row_base<float, 2>(geo, rr, origin);
-    float2* dst = patch + rr * PX * CC;
-    for (int idx = lane; idx < PX * CC; idx += 32) {
-      const int x = idx / CC, c = idx % CC;
-      if (c < ncl)
-        cp_async_elem(dst + idx, grid + (plane0 + c) * gtot + rbase + wrap_cell(origin[1] + x, KX));
-      else
-        dst[idx] = make_float2(0.f, 0.f);
+    for (int x = lane; x < PX; x += 32) {
+      const float2* src = grid + plane0 * gtot + rbase + wrap_cell(origin[1] + x, KX);
+      float2* dst = patch + (rr * PX + x) * CS;
+#pragma unroll 4
+      for (int c = 0; c < CC; ++c) {
+        if (c < ncl)
+          cp_async_elem(dst + c, src + c * gtot);
+        else
+          dst[c] = make_float2(0.f, 0.f);
+      }
     }
   }
   cp_async_wait_all();
@@ -473,7 +485,8 @@ __device__ __forceinline__ void fwd_job_pairs(const Geo<float>& geo, const Launc
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int PX = geo.P[1];
   const int cells = geo.P[0] * PX;
-  float2* scr = patch + cells * CC + warp * (PPW * D * NJ);
+  constexpr int CS = pair_cell_stride<CC>();
+  float2* scr = patch + cells * CS + warp * (PPW * D * NJ);
   const int k = lane % LPP;       // coil pair: coils 2k, 2k+1 of the chunk
   const int pslot = lane / LPP;   // point slot in the warp
   float2* pscr = scr + pslot * (D * NJ);
@@ -530,13 +543,13 @@ __device__ __forceinline__ void fwd_job_pairs(const Geo<float>& geo, const Launc
       float2 y0, y1;
       if (ok) {
         float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
-        const float4* prow = reinterpret_cast<const float4*>(patch + (local[0] * PX + local[1]) * CC) + k;
+        const float4* prow = reinterpret_cast<const float4*>(patch + (local[0] * PX + local[1]) * CS) + k;
 #pragma unroll
         for (int jy = 0; jy < NJ; ++jy) {
           float2 r0 = make_float2(0.f, 0.f), r1 = make_float2(0.f, 0.f);
 #pragma unroll
           for (int jx = 0; jx < NJ; ++jx) {
-            const float4 q = prow[(jy * PX + jx) * LPP];
+            const float4 q = prow[(jy * PX + jx) * (CS / 2)];
             r0 = cfma<float>(hx[jx], make_float2(q.x, q.y), r0);
             r1 = cfma<float>(hx[jx], make_float2(q.z, q.w), r1);
           }
@@ -1140,8 +1153,17 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
     for (int q0 = it.start; q0 < qend; q0 += kNBR) {
       const int nv = min(kNBR, qend - q0);
       const int4* ents = a.vlist + vbase + q0;
-      // A: conjugated table factors and footprint offsets (one thread per
-      // point and dim); conj(phase) * kdata (one thread per point and coil)
+      // A: the k-space values of each (point, coil) are copied to shared
+      // memory as they are (cp.async, all in flight at once) while each
+      // (point, dim) thread computes the conjugated table factors; the row
+      // factors carry conj(phase) as well.
+      for (int e = threadIdx.x; e < nv * CC; e += kThreads) {
+        const int pt = e / CC, cl = e % CC;
+        if (cl < ncl)
+          cp_async_elem(sv + e, kdata + (b * a.C + c0 + cl) * a.M + ents[pt].y);
+        else
+          sv[e] = make_float2(0.f, 0.f);
+      }
       for (int e = threadIdx.x; e < nv * D; e += kThreads) {
         const int pt = e >> 1, d = e & 1;
         const int4 ent = ents[pt];
@@ -1152,21 +1174,15 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
         const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
         const float2* tab = sel<const float2*, D>(geo.tab, d);
         const bool half = sel<bool, D>(geo.half, d);
+        const float2 phv = d == 0 ? ph[ent.x] : make_float2(1.f, 0.f);
         float2* out = sfac + e * NJ;
 #pragma unroll
-        for (int j = 0; j < NJ; ++j)
-          out[j] = cconj<float>(table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half));
-      }
-#pragma unroll 4
-      for (int e = threadIdx.x; e < nv * CC; e += kThreads) {
-        const int pt = e / CC, cl = e % CC;
-        float2 v = make_float2(0.f, 0.f);
-        if (cl < ncl) {
-          const int4 ent = ents[pt];
-          v = cmulc<float>(kdata[(b * a.C + c0 + cl) * a.M + ent.y], ph[ent.x]);
+        for (int j = 0; j < NJ; ++j) {
+          const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
+          out[j] = cconj<float>(d == 0 ? cmul<float>(te, phv) : te);
         }
-        sv[e] = v;
       }
+      cp_async_wait_all();
       __syncthreads();
       // B: the list is sorted by footprint start (column offset, then row
       // offset), so for each column offset LX the points that reach this
@@ -1821,7 +1837,8 @@ static int launch_fwd_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws,
       return with_cc(ip.a.Cc, [&](auto ccv) {
         constexpr int CC = decltype(ccv)::value;
         constexpr int PPW = 64 / CC;
-        const size_t smem = (size_t)ip.a.cells * CC * sizeof(float2) + (size_t)kWarps * PPW * 2 * 6 * sizeof(float2);
+        const size_t smem = (size_t)ip.a.cells * pair_cell_stride<CC>() * sizeof(float2) +
+                            (size_t)kWarps * PPW * 2 * 6 * sizeof(float2);
         int blocks;
         int rc = resident_blocks(k_interp_fwd_pairs<CC>, smem, ip.max_jobs, &blocks);
         if (rc) return rc;
@@ -2195,7 +2212,8 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
     const bool pairs = std::is_same<R, float>::value && D == 2 && JC == 6 && ip.a.Cc >= 2;
     const int pk = ip.a.Cc == 2 ? 0 : (ip.a.Cc == 4 ? 1 : (ip.a.Cc == 8 ? 2 : 3));
     if (pairs) {
-      const size_t sm = (size_t)ip.a.cells * ip.a.Cc * sizeof(float2) + (size_t)kWarps * (64 / ip.a.Cc) * 12 * sizeof(float2);
+      const int cc = 2 << pk;  // the kernel's coils per job
+      const size_t sm = (size_t)ip.a.cells * (cc + 2) * sizeof(float2) + (size_t)kWarps * (64 / cc) * 12 * sizeof(float2);
       if (sm > P->smem_fwd_pairs[pk]) P->smem_fwd_pairs[pk] = sm;
     } else if (ip.smem > P->smem_fwd) {
       P->smem_fwd = ip.smem;
