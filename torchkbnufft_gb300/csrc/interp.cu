@@ -1053,25 +1053,6 @@ __device__ __forceinline__ void reg_add_cols(float2 (&racc)[TXR], float2 vy, con
     if (LX + jx >= 0 && LX + jx < TXR) racc[LX + jx] = cfma<float>(vy, fx[jx], racc[LX + jx]);
 }
 
-// A point's column offset lx is uniform over the warp: the switch selects
-// code with static register indices (lx in [-5, TXR - 1], TXR <= 14).
-template <int TXR>
-__device__ __forceinline__ void reg_add_point(int lx, float2 (&racc)[TXR], float2 vy, const float2 (&fx)[6]) {
-  switch (lx) {
-#define TKBN_REG_CASE(L)                                   \
-  case L:                                                  \
-    if constexpr (L < TXR) reg_add_cols<TXR, L>(racc, vy, fx); \
-    break;
-    TKBN_REG_CASE(-5) TKBN_REG_CASE(-4) TKBN_REG_CASE(-3) TKBN_REG_CASE(-2) TKBN_REG_CASE(-1)
-    TKBN_REG_CASE(0) TKBN_REG_CASE(1) TKBN_REG_CASE(2) TKBN_REG_CASE(3) TKBN_REG_CASE(4) TKBN_REG_CASE(5)
-    TKBN_REG_CASE(6) TKBN_REG_CASE(7) TKBN_REG_CASE(8) TKBN_REG_CASE(9) TKBN_REG_CASE(10) TKBN_REG_CASE(11)
-    TKBN_REG_CASE(12) TKBN_REG_CASE(13)
-#undef TKBN_REG_CASE
-    default:
-      break;
-  }
-}
-
 // Footprint starts of a 16 x 14 tile with J = 6: row offsets -5 .. 15 (21),
 // column offsets -5 .. 13 (19); start k = (rx + 5) * 21 + ry + 5.
 constexpr int kRegKeyRows = kRegTileY + 5, kRegKeys = kRegKeyRows * (kRegTileX + 5);
@@ -1252,29 +1233,66 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
 }
 
 // K4 (owned tiles, registers), 3D: complex64, J = 6, 4 x 8 x 8 tiles, CC
-// coils per job (2, 4 or 8; one coil runs as CC = 2). Lane (coil, row) keeps
-// the 8 x-cells of one (z, y) row of the tile in registers; a warp covers
-// RPW = 32 / CC of the tile's 32 rows, and the groups of warps that cover
-// the tile take the staged points in turn, as in the 2D kernel.
+// coils per job (2, 4 or 8; one coil runs as CC = 2). Lane (coil, z, y) keeps
+// the 8 x-cells of one (z, y) row of the tile in registers; a warp covers all
+// 4 z planes of 32 / (4 CC) y rows, so with the tile's list sorted by
+// (x offset, y offset) the points reaching a warp's rows are one run per x
+// offset, as in the 2D kernel. The groups of warps that cover the tile take
+// the staged points in turn.
 constexpr int kReg3Z = 4, kReg3Y = 8, kReg3X = 8, kReg3Rows = kReg3Z * kReg3Y;
+// footprint starts (y, x) of a 4 x 8 x 8 tile with J = 6: 13 x 13
+constexpr int kReg3KeyRows = kReg3Y + 5, kReg3Keys = kReg3KeyRows * (kReg3X + 5);
+
+// Points of the batch with x offset LXI - 5 whose y rows reach [ylo, yhi):
+// entries ko[k(LXI, ylo - 5)] .. ko[k(LXI, yhi - 1) + 1] of the sorted list.
+template <int CC, int NG, int LXI>
+__device__ __forceinline__ void reg3_columns(const int32_t* __restrict__ ko, int ylo, int yhi, int q0, int nv, int grp,
+                                            const float2* __restrict__ sfac, const float2* __restrict__ sv,
+                                            const int4* __restrict__ sloc, int mz, int my, bool rowok, int c,
+                                            float2 (&racc)[kReg3X]) {
+  constexpr int NJ = 6, LX = LXI - 5;
+  const int kb = LXI * kReg3KeyRows;
+  int p = max(__ldg(ko + kb + ylo) - q0, 0);
+  const int e = min(__ldg(ko + kb + yhi + 5) - q0, nv);
+  if (NG > 1) p += (grp - p % NG + NG) % NG;
+  for (; p < e; p += NG) {
+    const int4 loc = sloc[p];
+    const int jz = mz - loc.x, jy = my - loc.y;
+    const float2* fp = sfac + p * (3 * NJ);
+    float2 fz = make_float2(0.f, 0.f), fy = make_float2(0.f, 0.f);
+    if (rowok && (unsigned)jz < (unsigned)NJ && (unsigned)jy < (unsigned)NJ) {
+      fz = fp[jz];
+      fy = fp[NJ + jy];
+    }
+    const float2 vzy = cmul<float>(cmul<float>(sv[p * CC + c], fz), fy);
+    const float4* fx4 = reinterpret_cast<const float4*>(fp + 2 * NJ);
+    const float4 f01 = fx4[0], f23 = fx4[1], f45 = fx4[2];
+    const float2 fx[6] = {make_float2(f01.x, f01.y), make_float2(f01.z, f01.w), make_float2(f23.x, f23.y),
+                          make_float2(f23.z, f23.w), make_float2(f45.x, f45.y), make_float2(f45.z, f45.w)};
+    reg_add_cols<kReg3X, LX>(racc, vzy, fx);
+  }
+  if constexpr (LXI + 1 < kReg3X + 5)
+    reg3_columns<CC, NG, LXI + 1>(ko, ylo, yhi, q0, nv, grp, sfac, sv, sloc, mz, my, rowok, c, racc);
+}
 
 template <int CC>
 __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch& a, const float* __restrict__ tm,
                                          const float2* __restrict__ ph, const float2* __restrict__ kdata,
                                          float2* __restrict__ grid, int vec_ok, int64_t job, unsigned char* smem_raw) {
   constexpr int D = 3, NJ = 6;
-  constexpr int RPW = 32 / CC, WPT = kReg3Rows / RPW, NG = kWarps / WPT;
+  // lane (coil, z, y): a warp covers all kReg3Z planes of YB rows y0 .. y0 + YB - 1
+  constexpr int RPW = 32 / CC, YB = RPW / kReg3Z, WPT = kReg3Y / YB, NG = kWarps / WPT;
   static_assert(CC >= 2 && CC <= 8 && (CC & (CC - 1)) == 0, "coils per job");
-  float2* sfac = reinterpret_cast<float2*>(smem_raw);  // [kNBR][18]: conj z, y, x factors
-  float2* sv = sfac + kNBR * D * NJ;                   // [kNBR][CC] conj(phase) * kdata per coil
+  float2* sfac = reinterpret_cast<float2*>(smem_raw);  // [kNBR][18]: conj z (times conj phase), y, x factors
+  float2* sv = sfac + kNBR * D * NJ;                   // [kNBR][CC] kdata per coil
   int4* sloc = reinterpret_cast<int4*>(sv + kNBR * CC);  // [kNBR] footprint start (z, y, x) in the tile
   float2* part = reinterpret_cast<float2*>(smem_raw);    // [NG][CC][32][8] partial tiles (after the batches)
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int c = lane % CC, grp = warp / WPT;
-  const int r_lo = (warp % WPT) * RPW;
-  const int myrow = r_lo + lane / CC;
-  const int mz = myrow / kReg3Y, my = myrow % kReg3Y;
+  const int y0 = (warp % WPT) * YB;
+  const int mz = (lane / CC) % kReg3Z, my = y0 + (lane / CC) / kReg3Z;
+  const int myrow = mz * kReg3Y + my;
   const int64_t per_sj = a.nbpt * a.ncc;
   {
     const Item it = a.jobs[job / per_sj];
@@ -1289,10 +1307,8 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
     const int ncl = (int)min((int64_t)min(CC, a.Cc), a.C - c0);
     const bool rowok = mz < ext[0] && my < ext[1];
     const int64_t vbase = a.voff[it.key];
-    // the warp's rows: z in [zlo, zhi], y in [ylo, yhi] (clipped to the tile)
-    const int zlo = r_lo / kReg3Y, zhi = min((r_lo + RPW - 1) / kReg3Y, ext[0] - 1);
-    const int ylo = RPW >= kReg3Y ? 0 : r_lo % kReg3Y;
-    const int yhi = min(RPW >= kReg3Y ? kReg3Y - 1 : ylo + RPW - 1, ext[1] - 1);
+    const int32_t* __restrict__ ko = a.koff + (int64_t)it.key * (kReg3Keys + 1);
+    const int y_hi = min(y0 + YB, ext[1]);
     float2 racc[kReg3X];
 #pragma unroll
     for (int x = 0; x < kReg3X; ++x) racc[x] = make_float2(0.f, 0.f);
@@ -1300,6 +1316,15 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
     for (int q0 = it.start; q0 < qend; q0 += kNBR) {
       const int nv = min(kNBR, qend - q0);
       const int4* ents = a.vlist + vbase + q0;
+      // A: k-space values copied as they are (cp.async); conjugated table
+      // factors per (point, dim), the z factors times conj(phase)
+      for (int e = threadIdx.x; e < nv * CC; e += kThreads) {
+        const int pt = e / CC, cl = e % CC;
+        if (cl < ncl)
+          cp_async_elem(sv + e, kdata + (b * a.C + c0 + cl) * a.M + ents[pt].y);
+        else
+          sv[e] = make_float2(0.f, 0.f);
+      }
       for (int e = threadIdx.x; e < nv * D; e += kThreads) {
         const int pt = e / D, d = e - (e / D) * D;
         const int4 ent = ents[pt];
@@ -1310,46 +1335,20 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
         const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
         const float2* tab = sel<const float2*, D>(geo.tab, d);
         const bool half = sel<bool, D>(geo.half, d);
+        const float2 phv = d == 0 ? ph[ent.x] : make_float2(1.f, 0.f);
         float2* out = sfac + e * NJ;
 #pragma unroll
-        for (int j = 0; j < NJ; ++j)
-          out[j] = cconj<float>(table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half));
-      }
-#pragma unroll 4
-      for (int e = threadIdx.x; e < nv * CC; e += kThreads) {
-        const int pt = e / CC, cl = e % CC;
-        float2 v = make_float2(0.f, 0.f);
-        if (cl < ncl) {
-          const int4 ent = ents[pt];
-          v = cmulc<float>(kdata[(b * a.C + c0 + cl) * a.M + ent.y], ph[ent.x]);
+        for (int j = 0; j < NJ; ++j) {
+          const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
+          out[j] = cconj<float>(d == 0 ? cmul<float>(te, phv) : te);
         }
-        sv[e] = v;
       }
+      cp_async_wait_all();
       __syncthreads();
-#pragma unroll 1
-      for (int h = 0; h < kNBR / 32; ++h) {
-        const int p = h * 32 + lane;
-        bool tch = false;
-        if (p < nv && (NG == 1 || p % NG == grp)) {
-          const int4 loc = sloc[p];
-          tch = max(zlo, loc.x) <= min(zhi, loc.x + NJ - 1) && max(ylo, loc.y) <= min(yhi, loc.y + NJ - 1);
-        }
-        for (unsigned msk = __ballot_sync(0xffffffffu, tch); msk; msk &= msk - 1) {
-          const int pt = h * 32 + __ffs(msk) - 1;
-          const int4 loc = sloc[pt];
-          const int jz = mz - loc.x, jy = my - loc.y;
-          if (rowok && (unsigned)jz < (unsigned)NJ && (unsigned)jy < (unsigned)NJ) {
-            const float2* fp = sfac + pt * (D * NJ);
-            const float2 vzy = cmul<float>(cmul<float>(sv[pt * CC + c], fp[jz]), fp[NJ + jy]);
-            const float4* fx4 = reinterpret_cast<const float4*>(fp + 2 * NJ);
-            const float4 f01 = fx4[0], f23 = fx4[1], f45 = fx4[2];
-            const float2 fx[6] = {make_float2(f01.x, f01.y), make_float2(f01.z, f01.w), make_float2(f23.x, f23.y),
-                                  make_float2(f23.z, f23.w), make_float2(f45.x, f45.y), make_float2(f45.z, f45.w)};
-            reg_add_point<kReg3X>(loc.z, racc, vzy, fx);
-          }
-        }
-        if ((h + 1) * 32 >= nv) break;
-      }
+      // B: runs of the list sorted by (column offset, row offset): for each
+      // column offset, the points whose rows reach y0 .. y_hi - 1
+      if (y0 < y_hi)
+        reg3_columns<CC, NG, 0>(ko, y0, y_hi, q0, nv, grp, sfac, sv, sloc, mz, my, rowok, c, racc);
       __syncthreads();
     }
     const int ex = ext[2];
@@ -1963,8 +1962,8 @@ static int reg_cc(int Cc) { return Cc < 2 ? 2 : Cc; }
 // 3D: 4 x 8 x 8 tiles, at most 8 coils per job.
 template <typename R, int D, int JC>
 static bool reg3_eligible(const InterpPlan& ip, const OwnLaunch& o) {
-  return std::is_same<R, float>::value && D == 3 && JC == 6 && o.vlist && o.Cc <= 8 && ip.L.tile[0] == kReg3Z &&
-         ip.L.tile[1] == kReg3Y && ip.L.tile[2] == kReg3X;
+  return std::is_same<R, float>::value && D == 3 && JC == 6 && o.vlist && o.koff && o.Cc <= 8 &&
+         ip.L.tile[0] == kReg3Z && ip.L.tile[1] == kReg3Y && ip.L.tile[2] == kReg3X && ip.L.knk == kReg3Keys;
 }
 
 static size_t reg3_smem(int CC) {

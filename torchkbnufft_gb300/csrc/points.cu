@@ -231,13 +231,15 @@ __global__ void __launch_bounds__(kValidThreads) k_tile_valid(Geo<R> geo, const 
   }
 }
 
-// 2D lists sorted by footprint start, stable (equal starts keep list order):
-// one warp per tile counts the starts (k = (rx + ox) * ny + ry + oy), scans
-// the counts into koff[tile][0 .. nk] and places the entries 32 at a time in
-// list order, ranking equal starts within the 32 by lane.
+// Lists sorted by footprint start in the last two dims, stable (equal starts
+// keep list order): one warp per tile counts the starts
+// (k = (rx + ox) * ny + ry + oy; rx, ry the column and row offsets, packed in
+// the entry's last word in 3D), scans the counts into koff[tile][0 .. nk] and
+// places the entries 32 at a time in list order, ranking equal starts within
+// the 32 by lane.
 constexpr int kSortWarps = 8, kSortMaxKeys = 1024;
 __global__ void __launch_bounds__(kSortWarps * 32)
-    k_tile_keysort(int64_t nkeys, int ny, int oy, int ox, int nk, const int32_t* __restrict__ voff,
+    k_tile_keysort(int64_t nkeys, int d3, int ny, int oy, int ox, int nk, const int32_t* __restrict__ voff,
                    const int32_t* __restrict__ vcount, const int4* __restrict__ vin, int4* __restrict__ vout,
                    int32_t* __restrict__ koff) {
   extern __shared__ int32_t s_cur[];
@@ -248,10 +250,11 @@ __global__ void __launch_bounds__(kSortWarps * 32)
     const int cnt = vcount[key];
     for (int k = lane; k <= nk; k += 32) cur[k] = 0;
     __syncwarp();
-    for (int q = lane; q < cnt; q += 32) {
-      const int4 e = vin[base + q];
-      atomicAdd(&cur[(e.w + ox) * ny + e.z + oy], 1);
-    }
+    auto skey = [&](const int4& e) {
+      const int ry = d3 ? (int)(short)(e.w & 0xffff) : e.z, rx = d3 ? (e.w >> 16) : e.w;
+      return (rx + ox) * ny + ry + oy;
+    };
+    for (int q = lane; q < cnt; q += 32) atomicAdd(&cur[skey(vin[base + q])], 1);
     __syncwarp();
     // exclusive scan of cur[0 .. nk]: lane l takes a run of `per` entries
     const int per = (nk + 1 + 31) / 32, lo = lane * per, hi = min(lo + per, nk + 1);
@@ -280,7 +283,7 @@ __global__ void __launch_bounds__(kSortWarps * 32)
       int k = nk;  // idle lanes share the end slot and write nothing
       if (act) {
         e = vin[base + q];
-        k = (e.w + ox) * ny + e.z + oy;
+        k = skey(e);
       }
       const unsigned peers = __match_any_sync(0xffffffffu, k);
       const int rank = __popc(peers & ((1u << lane) - 1u));
@@ -489,9 +492,15 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   // the owned-tile kernels' source limits: 16 source tiles in 2D, 27 in 3D
   L->vlist = L->owned_ok && ((g->ndim == 2 && L->span.ncombo <= 16) || (g->ndim == 3 && L->span.ncombo <= 27));
   L->max_valid = L->vlist ? L->span.ncombo * L->npts_total : 0;
-  L->kny = L->tile[0] + g->numpoints[0] - 1;
-  L->knk = g->ndim == 2 ? L->kny * (L->tile[1] + g->numpoints[1] - 1) : 0;
-  L->ksort = L->vlist && g->ndim == 2 && L->knk <= tkbn::kSortMaxKeys;
+  // sort key of a list entry: (column offset, row offset) of the last two dims
+  if (g->ndim >= 2) {
+    const int dr = g->ndim - 2, dc = g->ndim - 1;
+    L->kny = L->tile[dr] + g->numpoints[dr] - 1;
+    L->knk = L->kny * (L->tile[dc] + g->numpoints[dc] - 1);
+  } else {
+    L->kny = L->knk = 0;
+  }
+  L->ksort = L->vlist && g->ndim >= 2 && L->knk <= tkbn::kSortMaxKeys;
   L->max_subjobs = 2 * L->nkeys + (L->span.ncombo * L->npts_total + L->adj_chunk - 1) / L->adj_chunk;
   int sbits = 1;
   while (((int64_t)1 << sbits) <= L->adj_chunk + 1) ++sbits;
@@ -650,8 +659,8 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
       const int64_t sb = (L.nkeys + kSortWarps - 1) / kSortWarps;
       const size_t ssmem = (size_t)kSortWarps * (L.knk + 1) * sizeof(int32_t);
       k_tile_keysort<<<(int)(sb < 152 * 8 ? sb : 152 * 8), kSortWarps * 32, ssmem, s>>>(
-          L.nkeys, L.kny, g->numpoints[0] - 1, g->numpoints[1] - 1, L.knk, voff, vcount, vdst, vlist,
-          (int32_t*)(ws + L.off_koff));
+          L.nkeys, g->ndim == 3, L.kny, g->numpoints[g->ndim - 2] - 1, g->numpoints[g->ndim - 1] - 1, L.knk, voff,
+          vcount, vdst, vlist, (int32_t*)(ws + L.off_koff));
     }
   }
   // adjoint sub-jobs (output tiles, heavy ones split), longest first

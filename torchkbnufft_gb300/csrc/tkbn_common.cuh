@@ -248,9 +248,10 @@ struct PointsLayout {
   // per trajectory; the adjoint's sub-jobs are ranges of these lists.
   bool vlist;
   int64_t max_valid;  // upper bound on list entries (ncombo * npts_total)
-  // 2D lists sorted by footprint start (column offset, then row offset): the
-  // entries of each start are one run; koff[tile][k] is the first entry of
-  // start k = (rx + J1 - 1) * kny + (ry + J0 - 1), k = 0 .. knk (knk = end).
+  // Lists sorted by footprint start in the last two dims (column offset, then
+  // row offset): the entries of each start are one run; koff[tile][k] is the
+  // first entry of start k = (rx + Jc - 1) * kny + (ry + Jr - 1), k = 0 .. knk
+  // (knk = end).
   bool ksort;
   int kny, knk;
   size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
