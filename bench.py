@@ -546,6 +546,41 @@ def smooth_maps_3d(ncoil: int, n: int, seed: int) -> np.ndarray:
     return maps[None].astype(np.complex64)
 
 
+def stage_times(fwd, omega, x, smaps, steps, warmup):
+    """Mean time (ms) of each stage of forward + adjoint, timed on the stream."""
+    import torch
+
+    from torchkbnufft_gb300 import _runtime as R
+
+    cd = x.dtype
+    geom = fwd._geom(cd)
+    tables = fwd._tables()
+    scaling = fwd.scaling_coef.to(cd)
+    lay = R.points_layout(geom, omega)
+    names = ["fft_and_scale", "interp_fwd", "interp_adj", "ifft_and_scale"]
+
+    def staged(ev=None):
+        rec = (lambda i: ev[i].record()) if ev is not None else (lambda i: None)
+        rec(0)
+        grid = R.fft_and_scale(geom, x, smaps, scaling, None)
+        rec(1)
+        kdata = R.interp_fwd(geom, lay, tables, grid)
+        rec(2)
+        grid2 = R.interp_adj(geom, lay, tables, kdata)
+        rec(3)
+        R.ifft_and_scale(geom, grid2, smaps, scaling, None, overwrite=True)
+        rec(4)
+
+    for _ in range(warmup):
+        staged()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(steps)]
+    for k in range(steps):
+        staged(evs[k])
+    torch.cuda.synchronize()
+    return {n: round(statistics.mean(e[i].elapsed_time(e[i + 1]) for e in evs), 4) for i, n in enumerate(names)}
+
+
 def run_config(args):
     """Forward+adjoint (or, for spiral-grad, loss + backward) throughput at the
     other configurations; one JSON line each, not the headline metric."""
@@ -612,6 +647,7 @@ def run_config(args):
     else:
         with torch.no_grad():
             ms = timed(lambda: adj(fwd(x, omega, smaps=smaps), omega, smaps=smaps), args.steps, args.warmup)
+            extra = {"stage_ms": stage_times(fwd, omega, x, smaps, args.steps, args.warmup)}
     line = {
         "metric": f"NU points*coils/s ({w})", "value": work / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",

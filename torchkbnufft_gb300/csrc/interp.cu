@@ -216,6 +216,17 @@ __device__ __forceinline__ void load_patch(const Geo<R>& geo, const cplx<R>* __r
   cp_async_wait_all();
 }
 
+// f[j] for a runtime j through a select chain: indexing the register array
+// directly would move the whole factor array to local memory.
+template <typename R, int NJ>
+__device__ __forceinline__ cplx<R> pick_factor(const cplx<R> (&f)[NJ], int j) {
+  cplx<R> v = f[0];
+#pragma unroll
+  for (int q = 1; q < NJ; ++q)
+    if (q == j) v = f[q];
+  return v;
+}
+
 template <typename R, int D, int JC>
 __device__ __forceinline__ cplx<R> gather_point(const Geo<R>& geo, const cplx<R> (&h)[D][NJOf<JC>::N],
                                                 const int* local, const cplx<R>* __restrict__ plane) {
@@ -255,7 +266,7 @@ __device__ __forceinline__ cplx<R> gather_point(const Geo<R>& geo, const cplx<R>
             sz = cfma<R>(h[1 % D][jy], r, sz);
           }
         }
-        acc = cfma<R>(h[0][jz], sz, acc);
+        acc = cfma<R>(pick_factor<R, NJ>(h[0], jz), sz, acc);
       }
     }
   }
@@ -307,7 +318,7 @@ __device__ __forceinline__ void scatter_point(const Geo<R>& geo, const cplx<R> (
 #pragma unroll 1
     for (int jz = 0; jz < NJ; ++jz) {
       if (JC > 0 || jz < geo.J[0]) {
-        const cplx<R> vz = cmulc<R>(v, h[0][jz]);
+        const cplx<R> vz = cmulc<R>(v, pick_factor<R, NJ>(h[0], jz));
 #pragma unroll
         for (int jy = 0; jy < NJ; ++jy) {
           if (JC > 0 || jy < geo.J[1 % D]) {
@@ -1062,14 +1073,14 @@ constexpr int kRegKeyRows = kRegTileY + 5, kRegKeys = kRegKeyRows * (kRegTileX +
 // ko[k(LX, r_lo - 5)] .. ko[k(LX, r_hi - 1) + 1] of the sorted list. With
 // point groups (NG > 1) group g takes the batch positions p = g mod NG.
 template <int CC, int NG, int LXI>
-__device__ __forceinline__ void reg_columns(const int32_t* __restrict__ ko, int r_lo, int r_hi, int q0, int nv,
+__device__ __forceinline__ void reg_columns(const int32_t* ko, int r_lo, int r_hi, int q0, int nv,
                                            int grp, const float2* __restrict__ sfac, const float2* __restrict__ sv,
                                            const int2* __restrict__ sloc, int myrow, bool rowok, int c,
                                            float2 (&racc)[kRegTileX]) {
   constexpr int NJ = 6, LX = LXI - 5;
   const int kb = LXI * kRegKeyRows;
-  int p = max(__ldg(ko + kb + r_lo) - q0, 0);
-  const int e = min(__ldg(ko + kb + r_hi + 5) - q0, nv);
+  int p = max(ko[kb + r_lo] - q0, 0);
+  const int e = min(ko[kb + r_hi + 5] - q0, nv);
   if (NG > 1) p += (grp - p % NG + NG) % NG;
   for (; p < e; p += NG) {
     const int jy = myrow - sloc[p].x;
@@ -1125,7 +1136,10 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
     const int ncl = (int)min((int64_t)min(CC, a.Cc), a.C - c0);
     const bool rowok = myrow < ext[0];
     const int64_t vbase = a.voff[it.key];
-    const int32_t* __restrict__ ko = a.koff + (int64_t)it.key * (kRegKeys + 1);
+    // this tile's run starts, read from shared memory in phase B (published
+    // by the first batch's barrier)
+    int32_t* ko = reinterpret_cast<int32_t*>(sloc + kNBR);
+    for (int k = threadIdx.x; k <= kRegKeys; k += kThreads) ko[k] = a.koff[(int64_t)it.key * (kRegKeys + 1) + k];
     float2 racc[kRegTileX];
 #pragma unroll
     for (int x = 0; x < kRegTileX; ++x) racc[x] = make_float2(0.f, 0.f);
@@ -1246,14 +1260,14 @@ constexpr int kReg3KeyRows = kReg3Y + 5, kReg3Keys = kReg3KeyRows * (kReg3X + 5)
 // Points of the batch with x offset LXI - 5 whose y rows reach [ylo, yhi):
 // entries ko[k(LXI, ylo - 5)] .. ko[k(LXI, yhi - 1) + 1] of the sorted list.
 template <int CC, int NG, int LXI>
-__device__ __forceinline__ void reg3_columns(const int32_t* __restrict__ ko, int ylo, int yhi, int q0, int nv, int grp,
+__device__ __forceinline__ void reg3_columns(const int32_t* ko, int ylo, int yhi, int q0, int nv, int grp,
                                             const float2* __restrict__ sfac, const float2* __restrict__ sv,
                                             const int4* __restrict__ sloc, int mz, int my, bool rowok, int c,
                                             float2 (&racc)[kReg3X]) {
   constexpr int NJ = 6, LX = LXI - 5;
   const int kb = LXI * kReg3KeyRows;
-  int p = max(__ldg(ko + kb + ylo) - q0, 0);
-  const int e = min(__ldg(ko + kb + yhi + 5) - q0, nv);
+  int p = max(ko[kb + ylo] - q0, 0);
+  const int e = min(ko[kb + yhi + 5] - q0, nv);
   if (NG > 1) p += (grp - p % NG + NG) % NG;
   for (; p < e; p += NG) {
     const int4 loc = sloc[p];
@@ -1307,7 +1321,8 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
     const int ncl = (int)min((int64_t)min(CC, a.Cc), a.C - c0);
     const bool rowok = mz < ext[0] && my < ext[1];
     const int64_t vbase = a.voff[it.key];
-    const int32_t* __restrict__ ko = a.koff + (int64_t)it.key * (kReg3Keys + 1);
+    int32_t* ko = reinterpret_cast<int32_t*>(sloc + kNBR);
+    for (int k = threadIdx.x; k <= kReg3Keys; k += kThreads) ko[k] = a.koff[(int64_t)it.key * (kReg3Keys + 1) + k];
     const int y_hi = min(y0 + YB, ext[1]);
     float2 racc[kReg3X];
 #pragma unroll
@@ -1967,14 +1982,16 @@ static bool reg3_eligible(const InterpPlan& ip, const OwnLaunch& o) {
 }
 
 static size_t reg3_smem(int CC) {
-  const size_t staging = (size_t)kNBR * (3 * 6 + CC) * sizeof(float2) + (size_t)kNBR * sizeof(int4);
+  const size_t staging = (size_t)kNBR * (3 * 6 + CC) * sizeof(float2) + (size_t)kNBR * sizeof(int4) +
+                         (size_t)(kReg3Keys + 1) * sizeof(int32_t);
   const int ng = kWarps / (kReg3Rows / (32 / CC));
   const size_t partials = ng > 1 ? (size_t)ng * kReg3Rows * kReg3X * CC * sizeof(float2) : 0;
   return staging > partials ? staging : partials;
 }
 
 static size_t reg_smem(int CC) {
-  const size_t staging = (size_t)kNBR * (2 * 6 + CC) * sizeof(float2) + (size_t)kNBR * sizeof(int2);
+  const size_t staging = (size_t)kNBR * (2 * 6 + CC) * sizeof(float2) + (size_t)kNBR * sizeof(int2) +
+                         (size_t)(kRegKeys + 1) * sizeof(int32_t);
   const int ng = kWarps / (kRegTileY / (32 / CC));
   const size_t partials = ng > 1 ? (size_t)ng * kRegTileY * kRegTileX * CC * sizeof(float2) : 0;
   return staging > partials ? staging : partials;
