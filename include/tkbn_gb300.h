@@ -81,6 +81,11 @@ extern "C" {
                                         is bitwise repeatable (heavy tiles are not spread over
                                         several CTAs). Must be the same in tkbn_points_build
                                         and every call that uses the layout. */
+#define TKBN_LAYOUT_FORWARD_ONLY 4   /* layout without the adjoint's per-tile point lists
+                                        (smaller workspace, for forward-only callers); an
+                                        adjoint on it scans candidates instead (slower). Must
+                                        be the same in tkbn_points_build and every call that
+                                        uses the layout. */
 
 /* Operator geometry (one per KbModule). Unused dims (>= ndim) are ignored. */
 typedef struct tkbn_geometry {
@@ -121,7 +126,10 @@ int tkbn_points_build(const tkbn_geometry* g, const tkbn_points_desc* p, const v
 int tkbn_interp_fwd(const tkbn_geometry* g, const tkbn_points_desc* p, const void* workspace,
                     const void* const* tables, const void* grid, int64_t nbatch, int64_t ncoil,
                     void* kdata, void* stream);
-/* grid = interp^H(kdata). grid is fully overwritten (zeroed first). */
+/* grid = interp^H(kdata). grid is fully overwritten (zeroed first). With 2D
+ * complex64 J = 6 layouts of 16 x 14 tiles the call also fills a per-point
+ * scratch region inside the workspace (the table factors), so adjoint calls
+ * that share one workspace must be ordered (one stream). */
 int tkbn_interp_adj(const tkbn_geometry* g, const tkbn_points_desc* p, const void* workspace,
                     const void* const* tables, const void* kdata, int64_t nbatch, int64_t ncoil,
                     void* grid, void* stream);

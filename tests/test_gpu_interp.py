@@ -292,3 +292,43 @@ def test_adjoint_3d_owned_tiles_deterministic(C):
     assert rel_l2(_np(a), op.interp_adj(y.numpy(), om.numpy())) < TOL64
     c = adj(y.to(DEV), om.to(DEV))  # split heavy tiles (default layout)
     assert rel_l2(_np(c), op.interp_adj(y.numpy(), om.numpy())) < TOL64
+
+
+def _kernels_launched(fn):
+    """Names of the CUDA kernels that fn launches (torch profiler)."""
+    from torch.profiler import ProfilerActivity, profile
+
+    torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        fn()
+        torch.cuda.synchronize()
+    return {e.name for e in prof.events() if e.device_type == torch.autograd.DeviceType.CUDA}
+
+
+@pytest.mark.parametrize("case", ["2d16", "2d4", "3d8"])
+def test_specialised_kernels_are_selected(case):
+    """The benchmark shapes run the register-accumulator adjoint and the coil-pair
+    gather (a layout or eligibility regression would silently fall back to the
+    generic kernels, which are also correct)."""
+    from torchkbnufft_gb300 import _runtime as R
+
+    gen = torch.Generator().manual_seed(31)
+    if case == "3d8":
+        im, C = (16, 16, 16), 8
+    else:
+        im, C = (40, 40), 16 if case == "2d16" else 4
+    gs = tuple(2 * n for n in im)
+    M = 3000
+    om = ((torch.rand((len(im), M), generator=gen, dtype=torch.float64) * 2 - 1) * np.pi).float().to(DEV)
+    mod = tkbn().KbNufft(im_size=im, device=DEV)
+    geom = mod._geom(torch.complex64)
+    tables = mod._tables()
+    lay = R.points_layout(geom, om)
+    grid = torch.randn((1, C) + gs, dtype=torch.complex64, generator=torch.Generator().manual_seed(3)).to(DEV)
+    kdata = R.interp_fwd(geom, lay, tables, grid)
+    names = _kernels_launched(lambda: R.interp_adj(geom, lay, tables, kdata))
+    want = "k_interp_adj_reg3" if case == "3d8" else "k_interp_adj_reg<"
+    assert any(want in n for n in names), names
+    if case != "3d8":
+        names = _kernels_launched(lambda: R.interp_fwd(geom, lay, tables, grid))
+        assert any("k_interp_fwd_pairs" in n for n in names), names

@@ -41,6 +41,7 @@ class Geometry(ctypes.Structure):
 
 TKBN_TABLES_CONJ_SYMMETRIC = 1
 TKBN_ADJ_DETERMINISTIC = 2
+TKBN_LAYOUT_FORWARD_ONLY = 4
 
 
 class PointsDesc(ctypes.Structure):

@@ -189,6 +189,10 @@ __device__ __forceinline__ void cp_async_elem(double2* smem_dst, const double2* 
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
 }
+__device__ __forceinline__ void cp_async_16(float2* smem_dst, const float2* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 template <typename R, int D>
@@ -683,6 +687,8 @@ struct OwnLaunch {
   const int4* vlist;     // 2D: per-tile lists of the points that reach the tile (else null)
   const int32_t* voff;   // first list entry of each tile key
   const int32_t* koff;   // 2D lists sorted by footprint start: first entry of each start (else null)
+  const float2* pfac;    // 2D register adjoint: per sorted point, 12 conjugated table factors (else null)
+  const int4* vsort;     // 2D: each list chunk sorted by footprint start (else null)
 };
 
 template <typename R, int D>
@@ -1054,6 +1060,8 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
 // contributions that are never written; those cells belong to the wrapped
 // tile, which gets the same points with its own column offsets.
 constexpr int kNBR = 256;  // staged points per batch (== kThreads)
+static_assert(kNBR == kListChunk, "a 2D register-adjoint batch is one sorted list chunk");
+constexpr int kSVS = kNBR + 1;  // coil stride of the staged k-space values (bank spread)
 constexpr int kRegTileY = 16, kRegTileX = 14, kRegCoils = 16;
 
 // racc[LX + jx] += vy * fx[jx] for the columns inside the row (TXR cells).
@@ -1064,14 +1072,44 @@ __device__ __forceinline__ void reg_add_cols(float2 (&racc)[TXR], float2 vy, con
     if (LX + jx >= 0 && LX + jx < TXR) racc[LX + jx] = cfma<float>(vy, fx[jx], racc[LX + jx]);
 }
 
+// The six conjugated table factors of sorted point i in dim d (2D, J = 6);
+// the row factors (d = 0) carry conj(phase) as well.
+__device__ __forceinline__ void reg_point_factors(const Geo<float>& geo, const float* __restrict__ tm,
+                                                  const float2* __restrict__ ph, int64_t n, int64_t i, int d,
+                                                  float2* out) {
+  constexpr int D = 2, NJ = 6;
+  const float tv = tm[d * n + i];
+  const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
+  const float Lr = sel<float, D>(geo.Lr, d);
+  const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
+  const float2* tab = sel<const float2*, D>(geo.tab, d);
+  const bool half = sel<bool, D>(geo.half, d);
+  const float2 phv = d == 0 ? ph[i] : make_float2(1.f, 0.f);
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
+    out[j] = cconj<float>(d == 0 ? cmul<float>(te, phv) : te);
+  }
+}
+
+// Pre-pass of the 2D register adjoint: every sorted point's 12 factors once
+// (a point sits in 1.8 tile lists on average), so the adjoint's staging is
+// plain 16-byte copies.
+__global__ void __launch_bounds__(kThreads) k_point_factors2(Geo<float> geo, const float* __restrict__ tm,
+                                                             const float2* __restrict__ ph, int64_t n,
+                                                             float2* __restrict__ pfac) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 2 * n; e += (int64_t)gridDim.x * blockDim.x)
+    reg_point_factors(geo, tm, ph, n, e >> 1, (int)(e & 1), pfac + e * 6);
+}
+
 // Footprint starts of a 16 x 14 tile with J = 6: row offsets -5 .. 15 (21),
 // column offsets -5 .. 13 (19); start k = (rx + 5) * 21 + ry + 5.
 constexpr int kRegKeyRows = kRegTileY + 5, kRegKeys = kRegKeyRows * (kRegTileX + 5);
 
-// Points of the batch (list entries q0 .. q0 + nv - 1) with column offset
-// LX - 5 .. 13 that reach rows [r_lo, r_hi): for each LX, entries
-// ko[k(LX, r_lo - 5)] .. ko[k(LX, r_hi - 1) + 1] of the sorted list. With
-// point groups (NG > 1) group g takes the batch positions p = g mod NG.
+// Points of the batch with column offset LXI - 5 that reach rows
+// [r_lo, r_hi): positions ko[k(LXI, r_lo - 5)] .. ko[k(LXI, r_hi - 1) + 1] of
+// the batch's sorted chunk; sloc[p] = (row offset, list position of its
+// k-space values). With point groups (NG > 1) group g takes p = g mod NG.
 template <int CC, int NG, int LXI>
 __device__ __forceinline__ void reg_columns(const int32_t* ko, int r_lo, int r_hi, int q0, int nv,
                                            int grp, const float2* __restrict__ sfac, const float2* __restrict__ sv,
@@ -1079,15 +1117,16 @@ __device__ __forceinline__ void reg_columns(const int32_t* ko, int r_lo, int r_h
                                            float2 (&racc)[kRegTileX]) {
   constexpr int NJ = 6, LX = LXI - 5;
   const int kb = LXI * kRegKeyRows;
-  int p = max(ko[kb + r_lo] - q0, 0);
-  const int e = min(ko[kb + r_hi + 5] - q0, nv);
+  int p = ko[kb + r_lo];
+  const int e = ko[kb + r_hi + 5];
   if (NG > 1) p += (grp - p % NG + NG) % NG;
   for (; p < e; p += NG) {
-    const int jy = myrow - sloc[p].x;
+    const int2 lp = sloc[p];
+    const int jy = myrow - lp.x;
     const float2* fp = sfac + p * (2 * NJ);
     float2 fy = make_float2(0.f, 0.f);
     if (rowok && (unsigned)jy < (unsigned)NJ) fy = fp[jy];
-    const float2 vy = cmul<float>(sv[p * CC + c], fy);
+    const float2 vy = cmul<float>(sv[c * kSVS + lp.y], fy);
     const float4* fx4 = reinterpret_cast<const float4*>(fp + NJ);
     const float4 f01 = fx4[0], f23 = fx4[1], f45 = fx4[2];
     const float2 fx[6] = {make_float2(f01.x, f01.y), make_float2(f01.z, f01.w), make_float2(f23.x, f23.y),
@@ -1113,9 +1152,9 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
   constexpr int D = 2, NJ = 6;
   constexpr int RPW = 32 / CC, WPT = kRegTileY / RPW, NG = kWarps / WPT;
   static_assert(CC >= 2 && CC <= 16 && (CC & (CC - 1)) == 0, "coils per job");
-  float2* sfac = reinterpret_cast<float2*>(smem_raw);  // [kNBR][12]: conj y factors, conj x factors
-  float2* sv = sfac + kNBR * D * NJ;                   // [kNBR][CC] conj(phase) * kdata per coil
-  int2* sloc = reinterpret_cast<int2*>(sv + kNBR * CC);  // [kNBR] footprint start (y, x) in the tile
+  float2* sfac = reinterpret_cast<float2*>(smem_raw);  // [kNBR][12]: conj y factors (times conj phase), conj x
+  float2* sv = sfac + kNBR * D * NJ;                   // [CC][kSVS] kdata, in list order
+  int2* sloc = reinterpret_cast<int2*>(sv + CC * kSVS);  // [kNBR] (row offset, list position), sorted order
   float2* part = reinterpret_cast<float2*>(smem_raw);    // [NG][16][14][CC] partial tiles (after the batches)
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1136,10 +1175,7 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
     const int ncl = (int)min((int64_t)min(CC, a.Cc), a.C - c0);
     const bool rowok = myrow < ext[0];
     const int64_t vbase = a.voff[it.key];
-    // this tile's run starts, read from shared memory in phase B (published
-    // by the first batch's barrier)
-    int32_t* ko = reinterpret_cast<int32_t*>(sloc + kNBR);
-    for (int k = threadIdx.x; k <= kRegKeys; k += kThreads) ko[k] = a.koff[(int64_t)it.key * (kRegKeys + 1) + k];
+    int32_t* ko = reinterpret_cast<int32_t*>(sloc + kNBR);  // [kRegKeys + 1] the batch's run starts
     float2 racc[kRegTileX];
 #pragma unroll
     for (int x = 0; x < kRegTileX; ++x) racc[x] = make_float2(0.f, 0.f);
@@ -1147,34 +1183,42 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
     // The staging buffers are free here: the previous batch ended with a barrier.
     for (int q0 = it.start; q0 < qend; q0 += kNBR) {
       const int nv = min(kNBR, qend - q0);
+      // A: the batch is one chunk of the tile's list. Thread s copies entry s's
+      // k-space values of every coil (list order: a warp's 32 entries are
+      // mostly runs of consecutive m, so its copies touch few lines); the
+      // chunk's sorted copy gives, per sorted position, the footprint start,
+      // the list position and the table factors; ko = its run starts.
       const int4* ents = a.vlist + vbase + q0;
-      // A: the k-space values of each (point, coil) are copied to shared
-      // memory as they are (cp.async, all in flight at once) while each
-      // (point, dim) thread computes the conjugated table factors; the row
-      // factors carry conj(phase) as well.
-      for (int e = threadIdx.x; e < nv * CC; e += kThreads) {
-        const int pt = e / CC, cl = e % CC;
-        if (cl < ncl)
-          cp_async_elem(sv + e, kdata + (b * a.C + c0 + cl) * a.M + ents[pt].y);
-        else
-          sv[e] = make_float2(0.f, 0.f);
+      const int4* sents = a.vsort + vbase + q0;
+      {
+        const int64_t krow = (vbase + q0) / kListChunk + it.key;
+        for (int k = threadIdx.x; k <= kRegKeys; k += kThreads) ko[k] = a.koff[krow * (kRegKeys + 1) + k];
       }
-      for (int e = threadIdx.x; e < nv * D; e += kThreads) {
-        const int pt = e >> 1, d = e & 1;
-        const int4 ent = ents[pt];
-        if (d == 0) sloc[pt] = make_int2(ent.z, ent.w);
-        const float tv = tm[d * a.n + ent.x];
-        const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
-        const float Lr = sel<float, D>(geo.Lr, d);
-        const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
-        const float2* tab = sel<const float2*, D>(geo.tab, d);
-        const bool half = sel<bool, D>(geo.half, d);
-        const float2 phv = d == 0 ? ph[ent.x] : make_float2(1.f, 0.f);
-        float2* out = sfac + e * NJ;
-#pragma unroll
-        for (int j = 0; j < NJ; ++j) {
-          const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
-          out[j] = cconj<float>(d == 0 ? cmul<float>(te, phv) : te);
+      if ((int)threadIdx.x < nv) {
+        const int s = threadIdx.x;
+        const float2* src = kdata + (b * a.C + c0) * a.M + ents[s].y;
+#pragma unroll 4
+        for (int cl = 0; cl < CC; ++cl) {
+          if (cl < ncl)
+            cp_async_elem(sv + cl * kSVS + s, src + cl * a.M);
+          else
+            sv[cl * kSVS + s] = make_float2(0.f, 0.f);
+        }
+      }
+      if (a.pfac) {
+        // the point's 12 factors, precomputed per sorted point: six 16-byte copies
+        for (int e = threadIdx.x; e < nv * 6; e += kThreads) {
+          const int pt = e / 6, q = e - pt * 6;
+          const int4 ent = sents[pt];
+          if (q == 0) sloc[pt] = make_int2(ent.z, ent.y);
+          cp_async_16(sfac + pt * (D * NJ) + 2 * q, a.pfac + (int64_t)ent.x * (D * NJ) + 2 * q);
+        }
+      } else {
+        for (int e = threadIdx.x; e < nv * D; e += kThreads) {
+          const int pt = e >> 1, d = e & 1;
+          const int4 ent = sents[pt];
+          if (d == 0) sloc[pt] = make_int2(ent.z, ent.y);
+          reg_point_factors(geo, tm, ph, a.n, ent.x, d, sfac + e * NJ);
         }
       }
       cp_async_wait_all();
@@ -1950,7 +1994,9 @@ static OwnLaunch make_own(const InterpPlan& ip, const char* ws, int D) {
   o.span = ip.L.span;
   o.vlist = ip.L.vlist ? (const int4*)(ws + ip.L.off_vlist) : nullptr;
   o.voff = ip.L.vlist ? (const int32_t*)(ws + ip.L.off_voff) : nullptr;
-  o.koff = ip.L.ksort ? (const int32_t*)(ws + ip.L.off_koff) : nullptr;
+  o.koff = (ip.L.ksort || ip.L.csort) ? (const int32_t*)(ws + ip.L.off_koff) : nullptr;
+  o.pfac = nullptr;  // set by the launch that fills it
+  o.vsort = ip.L.csort ? (const int4*)(ws + ip.L.off_vsort) : nullptr;
   return o;
 }
 
@@ -1967,7 +2013,7 @@ static size_t own_smem(const OwnLaunch& o) {
 // per-tile point lists (any coil count; CC = max(2, coils per job)).
 template <typename R, int D, int JC>
 static bool reg_eligible(const InterpPlan& ip, const OwnLaunch& o) {
-  return std::is_same<R, float>::value && D == 2 && JC == 6 && o.vlist && o.koff && o.Cc <= kRegCoils &&
+  return std::is_same<R, float>::value && D == 2 && JC == 6 && o.vlist && o.vsort && o.koff && o.Cc <= kRegCoils &&
          ip.L.tile[0] == kRegTileY && ip.L.tile[1] == kRegTileX && ip.L.knk == kRegKeys;
 }
 
@@ -1990,8 +2036,8 @@ static size_t reg3_smem(int CC) {
 }
 
 static size_t reg_smem(int CC) {
-  const size_t staging = (size_t)kNBR * (2 * 6 + CC) * sizeof(float2) + (size_t)kNBR * sizeof(int2) +
-                         (size_t)(kRegKeys + 1) * sizeof(int32_t);
+  const size_t staging = (size_t)kNBR * 2 * 6 * sizeof(float2) + (size_t)CC * kSVS * sizeof(float2) +
+                         (size_t)kNBR * sizeof(int2) + (size_t)(kRegKeys + 1) * sizeof(int32_t);
   const int ng = kWarps / (kRegTileY / (32 / CC));
   const size_t partials = ng > 1 ? (size_t)ng * kRegTileY * kRegTileX * CC * sizeof(float2) : 0;
   return staging > partials ? staging : partials;
@@ -2016,6 +2062,15 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
   }
   if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
     if (reg_eligible<R, D, JC>(ip, o)) {
+      OwnLaunch orr = o;
+      if (ip.L.pfac && ip.a.n > 0) {
+        // the layout's factor scratch (see tkbn_interp_adj: calls sharing a workspace are ordered)
+        float2* pf = (float2*)const_cast<char*>(ws + ip.L.off_pfac);
+        const int64_t nb = (2 * ip.a.n + kThreads - 1) / kThreads;
+        k_point_factors2<<<(int)(nb < 152 * 16 ? nb : 152 * 16), kThreads, 0, s>>>(
+            geo, (const float*)(ws + ip.L.off_coords), (const float2*)(ws + ip.L.off_phase), ip.a.n, pf);
+        orr.pfac = pf;
+      }
       return with_cc(reg_cc(o.Cc), [&](auto ccv) {
         constexpr int CC = decltype(ccv)::value;
         const size_t rsmem = reg_smem(CC);
@@ -2023,7 +2078,7 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
         int rc = resident_blocks(k_interp_adj_reg<CC>, rsmem, max_jobs, &blocks);
         if (rc) return rc;
         const int vec_ok = ((uintptr_t)grid % 16 == 0) && (geo.K[1] % 2 == 0);
-        k_interp_adj_reg<CC><<<blocks, kThreads, rsmem, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
+        k_interp_adj_reg<CC><<<blocks, kThreads, rsmem, s>>>(geo, orr, (const float*)(ws + ip.L.off_coords),
                                                              (const float2*)(ws + ip.L.off_phase),
                                                              (const float2*)kdata, (float2*)grid, vec_ok);
         return check_cuda(cudaGetLastError(), "interp_adj launch");

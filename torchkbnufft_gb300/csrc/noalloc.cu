@@ -66,6 +66,10 @@ extern "C" int tkbn_interp_fwd_noalloc(const tkbn_geometry* g, const void* const
     tkbn_points_desc p{};
     p.npts = npts;
     p.ntraj = 1;
+    // forward only: the layout needs none of the adjoint's per-tile lists
+    tkbn_geometry gf = *g;
+    gf.flags |= TKBN_LAYOUT_FORWARD_ONLY;
+    g = &gf;
     tkbn_host::PointsLayout L;
     int rc = tkbn_host::points_layout(g, &p, &L);
     if (rc) return rc;

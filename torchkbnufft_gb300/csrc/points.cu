@@ -232,68 +232,78 @@ __global__ void __launch_bounds__(kValidThreads) k_tile_valid(Geo<R> geo, const 
 }
 
 // Lists sorted by footprint start in the last two dims, stable (equal starts
-// keep list order): one warp per tile counts the starts
+// keep list order), one warp per tile: count the starts
 // (k = (rx + ox) * ny + ry + oy; rx, ry the column and row offsets, packed in
-// the entry's last word in 3D), scans the counts into koff[tile][0 .. nk] and
-// places the entries 32 at a time in list order, ranking equal starts within
-// the 32 by lane.
+// the entry's last word in 3D), scan the counts into a koff row and place the
+// entries 32 at a time in list order, ranking equal starts within the 32 by
+// lane. chunk == 0: the whole list, koff row = tile. chunk > 0: each chunk of
+// `chunk` entries separately, koff row (voff[tile] + first) / chunk + tile,
+// and the output entry carries its position in the chunk in place of m.
 constexpr int kSortWarps = 8, kSortMaxKeys = 1024;
 __global__ void __launch_bounds__(kSortWarps * 32)
-    k_tile_keysort(int64_t nkeys, int d3, int ny, int oy, int ox, int nk, const int32_t* __restrict__ voff,
+    k_tile_keysort(int64_t nkeys, int d3, int chunk, int ny, int oy, int ox, int nk, const int32_t* __restrict__ voff,
                    const int32_t* __restrict__ vcount, const int4* __restrict__ vin, int4* __restrict__ vout,
                    int32_t* __restrict__ koff) {
   extern __shared__ int32_t s_cur[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int32_t* cur = s_cur + warp * (nk + 1);
+  auto skey = [&](const int4& e) {
+    const int ry = d3 ? (int)(short)(e.w & 0xffff) : e.z, rx = d3 ? (e.w >> 16) : e.w;
+    return (rx + ox) * ny + ry + oy;
+  };
   for (int64_t key = (int64_t)blockIdx.x * kSortWarps + warp; key < nkeys; key += (int64_t)gridDim.x * kSortWarps) {
-    const int64_t base = voff[key];
-    const int cnt = vcount[key];
-    for (int k = lane; k <= nk; k += 32) cur[k] = 0;
-    __syncwarp();
-    auto skey = [&](const int4& e) {
-      const int ry = d3 ? (int)(short)(e.w & 0xffff) : e.z, rx = d3 ? (e.w >> 16) : e.w;
-      return (rx + ox) * ny + ry + oy;
-    };
-    for (int q = lane; q < cnt; q += 32) atomicAdd(&cur[skey(vin[base + q])], 1);
-    __syncwarp();
-    // exclusive scan of cur[0 .. nk]: lane l takes a run of `per` entries
-    const int per = (nk + 1 + 31) / 32, lo = lane * per, hi = min(lo + per, nk + 1);
-    int sum = 0;
-    for (int k = lo; k < hi; ++k) sum += cur[k];
-    int incl = sum;
+    const int64_t tbase = voff[key];
+    const int tcnt = vcount[key];
+    const int span = chunk > 0 ? chunk : (tcnt > 0 ? tcnt : 1);
+    for (int first = 0; first < tcnt || (first == 0 && chunk == 0); first += span) {
+      const int64_t base = tbase + first;
+      const int cnt = min(span, tcnt - first);
+      for (int k = lane; k <= nk; k += 32) cur[k] = 0;
+      __syncwarp();
+      for (int q = lane; q < cnt; q += 32) atomicAdd(&cur[skey(vin[base + q])], 1);
+      __syncwarp();
+      // exclusive scan of cur[0 .. nk]: lane l takes a run of `per` entries
+      const int per = (nk + 1 + 31) / 32, lo = lane * per, hi = min(lo + per, nk + 1);
+      int sum = 0;
+      for (int k = lo; k < hi; ++k) sum += cur[k];
+      int incl = sum;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    int run = incl - sum;
-    for (int k = lo; k < hi; ++k) {
-      const int c = cur[k];
-      cur[k] = run;
-      run += c;
-    }
-    __syncwarp();
-    int32_t* ko = koff + key * (nk + 1);
-    for (int k = lane; k <= nk; k += 32) ko[k] = cur[k];
-    __syncwarp();
-    for (int q0 = 0; q0 < cnt; q0 += 32) {
-      const int q = q0 + lane;
-      const bool act = q < cnt;
-      int4 e = make_int4(0, 0, 0, 0);
-      int k = nk;  // idle lanes share the end slot and write nothing
-      if (act) {
-        e = vin[base + q];
-        k = skey(e);
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
       }
-      const unsigned peers = __match_any_sync(0xffffffffu, k);
-      const int rank = __popc(peers & ((1u << lane) - 1u));
-      const int pos = cur[k] + rank;
+      int run = incl - sum;
+      for (int k = lo; k < hi; ++k) {
+        const int c = cur[k];
+        cur[k] = run;
+        run += c;
+      }
       __syncwarp();
-      if (act && rank == 0) cur[k] += __popc(peers);
+      const int64_t row = chunk > 0 ? base / chunk + key : key;
+      int32_t* ko = koff + row * (nk + 1);
+      for (int k = lane; k <= nk; k += 32) ko[k] = cur[k];
       __syncwarp();
-      if (act) vout[base + pos] = e;
+      for (int q0 = 0; q0 < cnt; q0 += 32) {
+        const int q = q0 + lane;
+        const bool act = q < cnt;
+        int4 e = make_int4(0, 0, 0, 0);
+        int k = nk;  // idle lanes share the end slot and write nothing
+        if (act) {
+          e = vin[base + q];
+          k = skey(e);
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, k);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        const int pos = cur[k] + rank;
+        __syncwarp();
+        if (act && rank == 0) cur[k] += __popc(peers);
+        __syncwarp();
+        if (chunk > 0) e.y = q;
+        if (act) vout[base + pos] = e;
+      }
+      __syncwarp();
+      if (chunk == 0) break;
     }
-    __syncwarp();
   }
 }
 
@@ -490,7 +500,8 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   // adjoint sub-jobs: at most adj_chunk candidates (list entries in 2D) each
   L->adj_chunk = (g->flags & TKBN_ADJ_DETERMINISTIC) ? (1 << 30) : 1024;
   // the owned-tile kernels' source limits: 16 source tiles in 2D, 27 in 3D
-  L->vlist = L->owned_ok && ((g->ndim == 2 && L->span.ncombo <= 16) || (g->ndim == 3 && L->span.ncombo <= 27));
+  L->vlist = L->owned_ok && !(g->flags & TKBN_LAYOUT_FORWARD_ONLY) &&
+             ((g->ndim == 2 && L->span.ncombo <= 16) || (g->ndim == 3 && L->span.ncombo <= 27));
   L->max_valid = L->vlist ? L->span.ncombo * L->npts_total : 0;
   // sort key of a list entry: (column offset, row offset) of the last two dims
   if (g->ndim >= 2) {
@@ -500,7 +511,12 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   } else {
     L->kny = L->knk = 0;
   }
-  L->ksort = L->vlist && g->ndim >= 2 && L->knk <= tkbn::kSortMaxKeys;
+  L->ksort = L->vlist && g->ndim == 3 && L->knk <= tkbn::kSortMaxKeys;
+  L->csort = L->vlist && g->ndim == 2 && g->dtype == TKBN_C64 && g->numpoints[0] == 6 && g->numpoints[1] == 6 &&
+             L->tile[0] == 16 && L->tile[1] == 14 && L->adj_chunk % tkbn::kListChunk == 0 &&
+             L->knk <= tkbn::kSortMaxKeys;
+  L->pfac = L->csort;
+  L->koff_rows = L->ksort ? L->nkeys : (L->csort ? L->max_valid / tkbn::kListChunk + L->nkeys + 1 : 0);
   L->max_subjobs = 2 * L->nkeys + (L->span.ncombo * L->npts_total + L->adj_chunk - 1) / L->adj_chunk;
   int sbits = 1;
   while (((int64_t)1 << sbits) <= L->adj_chunk + 1) ++sbits;
@@ -567,8 +583,12 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   o = align_up(o + sizeof(int4) * L->max_valid);
   L->off_vtmp = o;
   o = align_up(o + (L->ksort ? sizeof(int4) * L->max_valid : 0));
+  L->off_vsort = o;
+  o = align_up(o + (L->csort ? sizeof(int4) * L->max_valid : 0));
   L->off_koff = o;
-  o = align_up(o + (L->ksort ? 4 * L->nkeys * (L->knk + 1) : 0));
+  o = align_up(o + 4 * (size_t)L->koff_rows * (L->knk + 1));
+  L->off_pfac = o;
+  o = align_up(o + (L->pfac ? (size_t)L->npts_total * 12 * 8 : 0));
   L->off_coords = o;
   o = align_up(o + rsize * g->ndim * n);
   L->off_phase = o;
@@ -652,15 +672,16 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
     tb = L.cub_bytes;
     if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, vcount, voff, (int)L.nkeys, s) != cudaSuccess)
       return set_error(TKBN_ERR_CUDA, "scan failed");
-    int4* vdst = L.ksort ? (int4*)(ws + L.off_vtmp) : vlist;
+    int4* vdst = L.ksort ? (int4*)(ws + L.off_vtmp) : vlist;  // 3D: sorted into vlist below
     kv<<<wblocks, kValidThreads, 0, s>>>(geo, counts, tile_off, coords, vals, n, p->npts, L.nkeys, L.span, voff,
                                          vcount, vdst);
-    if (L.ksort) {
+    if (L.ksort || L.csort) {
       const int64_t sb = (L.nkeys + kSortWarps - 1) / kSortWarps;
       const size_t ssmem = (size_t)kSortWarps * (L.knk + 1) * sizeof(int32_t);
       k_tile_keysort<<<(int)(sb < 152 * 8 ? sb : 152 * 8), kSortWarps * 32, ssmem, s>>>(
-          L.nkeys, g->ndim == 3, L.kny, g->numpoints[g->ndim - 2] - 1, g->numpoints[g->ndim - 1] - 1, L.knk, voff,
-          vcount, vdst, vlist, (int32_t*)(ws + L.off_koff));
+          L.nkeys, g->ndim == 3, L.csort ? kListChunk : 0, L.kny, g->numpoints[g->ndim - 2] - 1,
+          g->numpoints[g->ndim - 1] - 1, L.knk, voff, vcount, vdst, L.csort ? (int4*)(ws + L.off_vsort) : vlist,
+          (int32_t*)(ws + L.off_koff));
     }
   }
   // adjoint sub-jobs (output tiles, heavy ones split), longest first

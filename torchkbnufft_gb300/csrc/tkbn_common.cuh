@@ -8,6 +8,9 @@
 
 namespace tkbn {
 
+// Entries of a tile's point list staged per adjoint batch (2D register adjoint).
+constexpr int kListChunk = 256;
+
 constexpr int kMaxDim = 3;
 constexpr int kMaxJ = 8;  // numpoints supported per dimension
 
@@ -248,16 +251,26 @@ struct PointsLayout {
   // per trajectory; the adjoint's sub-jobs are ranges of these lists.
   bool vlist;
   int64_t max_valid;  // upper bound on list entries (ncombo * npts_total)
-  // Lists sorted by footprint start in the last two dims (column offset, then
-  // row offset): the entries of each start are one run; koff[tile][k] is the
-  // first entry of start k = (rx + Jc - 1) * kny + (ry + Jr - 1), k = 0 .. knk
-  // (knk = end).
-  bool ksort;
+  // Footprint start of a list entry in the last two dims:
+  // k = (rx + Jc - 1) * kny + (ry + Jr - 1), k < knk.
+  //  * 3D (ksort): each tile's list is sorted by start (stable); the entries
+  //    of one start are a run and koff[tile][k] is its first entry
+  //    (koff[tile][knk] = end).
+  //  * 2D complex64 J = 6 16 x 14 layouts (csort): the list keeps its order
+  //    (source tile, then sorted point order: runs of consecutive m), and
+  //    vsort holds each kListChunk-entry chunk of it sorted by start, entry
+  //    {sorted index, position in the chunk, ry, rx}; koff row
+  //    (voff[tile] + first) / kListChunk + tile holds the chunk's run starts.
+  bool ksort, csort;
   int kny, knk;
+  int64_t koff_rows;
+  // csort layouts: room for each sorted point's 12 conjugated table factors,
+  // filled by the register adjoint before it runs
+  bool pfac;
   size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
       off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_phase,
       off_tile_work, off_tile_nsub, off_tile_suboff, off_sj_raw, off_adj_jobs, off_sj_keys_in, off_sj_keys,
-      off_sj_vals_in, off_sj_vals, off_vcount, off_voff, off_vlist, off_vtmp, off_koff, off_cub;
+      off_sj_vals_in, off_sj_vals, off_vcount, off_voff, off_vlist, off_vtmp, off_vsort, off_koff, off_pfac, off_cub;
   size_t cub_bytes;
   size_t total;
 };
