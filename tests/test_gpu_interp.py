@@ -294,19 +294,29 @@ def test_adjoint_3d_owned_tiles_deterministic(C):
     assert rel_l2(_np(c), op.interp_adj(y.numpy(), om.numpy())) < TOL64
 
 
-def _kernels_launched(fn):
-    """Names of the CUDA kernels that fn launches (torch profiler)."""
+def _kernels_launched(fn, tmp_path):
+    """Names of the CUDA kernels that fn launches (the profiler's kernel trace)."""
+    import json
+
     from torch.profiler import ProfilerActivity, profile
 
     torch.cuda.synchronize()
-    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+    # the process's first profiling session can miss kernel records while the
+    # activity tracer starts up: run one throwaway session first
+    with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]):
+        torch.ones(8, device=DEV).sum()
+        torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as prof:
         fn()
         torch.cuda.synchronize()
-    return {e.name for e in prof.events() if e.device_type == torch.autograd.DeviceType.CUDA}
+    path = tmp_path / "trace.json"
+    prof.export_chrome_trace(str(path))
+    events = json.loads(path.read_text()).get("traceEvents", [])
+    return {e.get("name", "") for e in events if e.get("cat") == "kernel"}
 
 
 @pytest.mark.parametrize("case", ["2d16", "2d4", "3d8"])
-def test_specialised_kernels_are_selected(case):
+def test_specialised_kernels_are_selected(case, tmp_path):
     """The benchmark shapes run the register-accumulator adjoint and the coil-pair
     gather (a layout or eligibility regression would silently fall back to the
     generic kernels, which are also correct)."""
@@ -326,9 +336,9 @@ def test_specialised_kernels_are_selected(case):
     lay = R.points_layout(geom, om)
     grid = torch.randn((1, C) + gs, dtype=torch.complex64, generator=torch.Generator().manual_seed(3)).to(DEV)
     kdata = R.interp_fwd(geom, lay, tables, grid)
-    names = _kernels_launched(lambda: R.interp_adj(geom, lay, tables, kdata))
+    names = _kernels_launched(lambda: R.interp_adj(geom, lay, tables, kdata), tmp_path)
     want = "k_interp_adj_reg3" if case == "3d8" else "k_interp_adj_reg<"
     assert any(want in n for n in names), names
     if case != "3d8":
-        names = _kernels_launched(lambda: R.interp_fwd(geom, lay, tables, grid))
+        names = _kernels_launched(lambda: R.interp_fwd(geom, lay, tables, grid), tmp_path)
         assert any("k_interp_fwd_pairs" in n for n in names), names

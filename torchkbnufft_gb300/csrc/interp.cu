@@ -1302,7 +1302,8 @@ constexpr int kReg3Z = 4, kReg3Y = 8, kReg3X = 8, kReg3Rows = kReg3Z * kReg3Y;
 constexpr int kReg3KeyRows = kReg3Y + 5, kReg3Keys = kReg3KeyRows * (kReg3X + 5);
 
 // Points of the batch with x offset LXI - 5 whose y rows reach [ylo, yhi):
-// entries ko[k(LXI, ylo - 5)] .. ko[k(LXI, yhi - 1) + 1] of the sorted list.
+// positions ko[k(LXI, ylo - 5)] .. ko[k(LXI, yhi - 1) + 1] of the batch's
+// sorted chunk; sloc[p] = (z offset, y offset, list position of its values).
 template <int CC, int NG, int LXI>
 __device__ __forceinline__ void reg3_columns(const int32_t* ko, int ylo, int yhi, int q0, int nv, int grp,
                                             const float2* __restrict__ sfac, const float2* __restrict__ sv,
@@ -1310,8 +1311,8 @@ __device__ __forceinline__ void reg3_columns(const int32_t* ko, int ylo, int yhi
                                             float2 (&racc)[kReg3X]) {
   constexpr int NJ = 6, LX = LXI - 5;
   const int kb = LXI * kReg3KeyRows;
-  int p = max(ko[kb + ylo] - q0, 0);
-  const int e = min(ko[kb + yhi + 5] - q0, nv);
+  int p = ko[kb + ylo];
+  const int e = ko[kb + yhi + 5];
   if (NG > 1) p += (grp - p % NG + NG) % NG;
   for (; p < e; p += NG) {
     const int4 loc = sloc[p];
@@ -1322,7 +1323,7 @@ __device__ __forceinline__ void reg3_columns(const int32_t* ko, int ylo, int yhi
       fz = fp[jz];
       fy = fp[NJ + jy];
     }
-    const float2 vzy = cmul<float>(cmul<float>(sv[p * CC + c], fz), fy);
+    const float2 vzy = cmul<float>(cmul<float>(sv[c * kSVS + loc.z], fz), fy);
     const float4* fx4 = reinterpret_cast<const float4*>(fp + 2 * NJ);
     const float4 f01 = fx4[0], f23 = fx4[1], f45 = fx4[2];
     const float2 fx[6] = {make_float2(f01.x, f01.y), make_float2(f01.z, f01.w), make_float2(f23.x, f23.y),
@@ -1342,8 +1343,8 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
   constexpr int RPW = 32 / CC, YB = RPW / kReg3Z, WPT = kReg3Y / YB, NG = kWarps / WPT;
   static_assert(CC >= 2 && CC <= 8 && (CC & (CC - 1)) == 0, "coils per job");
   float2* sfac = reinterpret_cast<float2*>(smem_raw);  // [kNBR][18]: conj z (times conj phase), y, x factors
-  float2* sv = sfac + kNBR * D * NJ;                   // [kNBR][CC] kdata per coil
-  int4* sloc = reinterpret_cast<int4*>(sv + kNBR * CC);  // [kNBR] footprint start (z, y, x) in the tile
+  float2* sv = sfac + kNBR * D * NJ;                   // [CC][kSVS] kdata, in list order
+  int4* sloc = reinterpret_cast<int4*>(sv + CC * kSVS);  // [kNBR] (z offset, y offset, list position), sorted
   float2* part = reinterpret_cast<float2*>(smem_raw);    // [NG][CC][32][8] partial tiles (after the batches)
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1365,8 +1366,7 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
     const int ncl = (int)min((int64_t)min(CC, a.Cc), a.C - c0);
     const bool rowok = mz < ext[0] && my < ext[1];
     const int64_t vbase = a.voff[it.key];
-    int32_t* ko = reinterpret_cast<int32_t*>(sloc + kNBR);
-    for (int k = threadIdx.x; k <= kReg3Keys; k += kThreads) ko[k] = a.koff[(int64_t)it.key * (kReg3Keys + 1) + k];
+    int32_t* ko = reinterpret_cast<int32_t*>(sloc + kNBR);  // [kReg3Keys + 1] the batch's run starts
     const int y_hi = min(y0 + YB, ext[1]);
     float2 racc[kReg3X];
 #pragma unroll
@@ -1374,20 +1374,31 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
     const int qend = it.start + it.len;
     for (int q0 = it.start; q0 < qend; q0 += kNBR) {
       const int nv = min(kNBR, qend - q0);
+      // A: the batch is one chunk of the tile's list: k-space values copied in
+      // list order (thread s: entry s, every coil), footprint starts, list
+      // positions and conjugated table factors (z factors times conj(phase))
+      // in the chunk's sorted order; ko = the chunk's run starts
       const int4* ents = a.vlist + vbase + q0;
-      // A: k-space values copied as they are (cp.async); conjugated table
-      // factors per (point, dim), the z factors times conj(phase)
-      for (int e = threadIdx.x; e < nv * CC; e += kThreads) {
-        const int pt = e / CC, cl = e % CC;
-        if (cl < ncl)
-          cp_async_elem(sv + e, kdata + (b * a.C + c0 + cl) * a.M + ents[pt].y);
-        else
-          sv[e] = make_float2(0.f, 0.f);
+      const int4* sents = a.vsort + vbase + q0;
+      {
+        const int64_t krow = (vbase + q0) / kListChunk + it.key;
+        for (int k = threadIdx.x; k <= kReg3Keys; k += kThreads) ko[k] = a.koff[krow * (kReg3Keys + 1) + k];
+      }
+      if ((int)threadIdx.x < nv) {
+        const int s = threadIdx.x;
+        const float2* src = kdata + (b * a.C + c0) * a.M + ents[s].y;
+#pragma unroll
+        for (int cl = 0; cl < CC; ++cl) {
+          if (cl < ncl)
+            cp_async_elem(sv + cl * kSVS + s, src + cl * a.M);
+          else
+            sv[cl * kSVS + s] = make_float2(0.f, 0.f);
+        }
       }
       for (int e = threadIdx.x; e < nv * D; e += kThreads) {
         const int pt = e / D, d = e - (e / D) * D;
-        const int4 ent = ents[pt];
-        if (d == 0) sloc[pt] = make_int4(ent.z, (int)(short)(ent.w & 0xffff), ent.w >> 16, 0);
+        const int4 ent = sents[pt];
+        if (d == 0) sloc[pt] = make_int4(ent.z, (int)(short)(ent.w & 0xffff), ent.y, 0);
         const float tv = tm[d * a.n + ent.x];
         const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
         const float Lr = sel<float, D>(geo.Lr, d);
@@ -2023,13 +2034,13 @@ static int reg_cc(int Cc) { return Cc < 2 ? 2 : Cc; }
 // 3D: 4 x 8 x 8 tiles, at most 8 coils per job.
 template <typename R, int D, int JC>
 static bool reg3_eligible(const InterpPlan& ip, const OwnLaunch& o) {
-  return std::is_same<R, float>::value && D == 3 && JC == 6 && o.vlist && o.koff && o.Cc <= 8 &&
+  return std::is_same<R, float>::value && D == 3 && JC == 6 && o.vlist && o.vsort && o.koff && o.Cc <= 8 &&
          ip.L.tile[0] == kReg3Z && ip.L.tile[1] == kReg3Y && ip.L.tile[2] == kReg3X && ip.L.knk == kReg3Keys;
 }
 
 static size_t reg3_smem(int CC) {
-  const size_t staging = (size_t)kNBR * (3 * 6 + CC) * sizeof(float2) + (size_t)kNBR * sizeof(int4) +
-                         (size_t)(kReg3Keys + 1) * sizeof(int32_t);
+  const size_t staging = (size_t)kNBR * 3 * 6 * sizeof(float2) + (size_t)CC * kSVS * sizeof(float2) +
+                         (size_t)kNBR * sizeof(int4) + (size_t)(kReg3Keys + 1) * sizeof(int32_t);
   const int ng = kWarps / (kReg3Rows / (32 / CC));
   const size_t partials = ng > 1 ? (size_t)ng * kReg3Rows * kReg3X * CC * sizeof(float2) : 0;
   return staging > partials ? staging : partials;

@@ -511,11 +511,16 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   } else {
     L->kny = L->knk = 0;
   }
-  L->ksort = L->vlist && g->ndim == 3 && L->knk <= tkbn::kSortMaxKeys;
-  L->csort = L->vlist && g->ndim == 2 && g->dtype == TKBN_C64 && g->numpoints[0] == 6 && g->numpoints[1] == 6 &&
-             L->tile[0] == 16 && L->tile[1] == 14 && L->adj_chunk % tkbn::kListChunk == 0 &&
+  // chunk-sorted copies for the register adjoints: 2D 16 x 14 and 3D 4 x 8 x 8
+  // tiles, complex64, J = 6
+  bool j6 = true;
+  for (int d = 0; d < g->ndim; ++d) j6 = j6 && g->numpoints[d] == 6;
+  const bool regtile = (g->ndim == 2 && L->tile[0] == 16 && L->tile[1] == 14) ||
+                       (g->ndim == 3 && L->tile[0] == 4 && L->tile[1] == 8 && L->tile[2] == 8);
+  L->ksort = false;
+  L->csort = L->vlist && g->dtype == TKBN_C64 && j6 && regtile && L->adj_chunk % tkbn::kListChunk == 0 &&
              L->knk <= tkbn::kSortMaxKeys;
-  L->pfac = L->csort;
+  L->pfac = L->csort && g->ndim == 2;
   L->koff_rows = L->ksort ? L->nkeys : (L->csort ? L->max_valid / tkbn::kListChunk + L->nkeys + 1 : 0);
   L->max_subjobs = 2 * L->nkeys + (L->span.ncombo * L->npts_total + L->adj_chunk - 1) / L->adj_chunk;
   int sbits = 1;
