@@ -633,9 +633,17 @@ def run_config(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / steps
 
+    cdt = torch.complex64
     if w == "single":
         n, om, Bc, Cc, smaps = 256, radial_traj(402, 512), 1, 1, None
         desc = "2D single-coil radial, image 256^2, grid 512^2, 402x512 (205824 points), batch 1"
+    elif w == "sense-c128":
+        cdt = torch.complex128
+        image_np, smaps_np, om = make_inputs()
+        n, Bc, Cc = N, B, C
+        smaps = torch.tensor(smaps_np.astype(np.complex128), device=dev)
+        desc = ("2D SENSE NUFFT fwd+adj in complex128, image 320x320, grid 640x640, J=6, L=1024, 16 coils, "
+                "batch 4, golden-angle 404x640 (258560 points)")
     elif w == "kooshball":
         n, om, Bc, Cc = 128, kooshball_traj(20000, 256), 1, 8
         smaps = torch.tensor(smooth_maps_3d(8, 128, 3), device=dev)
@@ -649,11 +657,13 @@ def run_config(args):
     im = (n,) * nd
     M = om.shape[1]
     x = torch.tensor((rng.standard_normal((Bc, 1 if smaps is not None else Cc) + im)
-                      + 1j * rng.standard_normal((Bc, 1 if smaps is not None else Cc) + im)).astype(np.complex64),
-                     device=dev)
+                      + 1j * rng.standard_normal((Bc, 1 if smaps is not None else Cc) + im)),
+                     device=dev).to(cdt)
     omega = torch.tensor(om, device=dev)
-    fwd = tkbn.KbNufft(im_size=im, device=dev)
-    adj = tkbn.KbNufftAdjoint(im_size=im, device=dev)
+    if cdt == torch.complex128:
+        omega = omega.double()
+    fwd = tkbn.KbNufft(im_size=im, dtype=cdt, device=dev)
+    adj = tkbn.KbNufftAdjoint(im_size=im, dtype=cdt, device=dev)
     work = Bc * Cc * M
     extra = {}
     if w == "spiral-grad":
@@ -679,7 +689,7 @@ def run_config(args):
     line = {
         "metric": f"NU points*coils/s ({w})", "value": work / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "c128" if cdt == torch.complex128 else "c64", "data": "synthetic",
         "config": {"workload": desc, "work_per_step": work, **extra},
     }
     print(json.dumps(line))
@@ -693,7 +703,7 @@ def main():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--ref-coils", type=int, default=4)
-    p.add_argument("--workload", default="sense", choices=["sense", "ragged", "single", "kooshball", "spiral-grad"],
+    p.add_argument("--workload", default="sense", choices=["sense", "ragged", "single", "kooshball", "spiral-grad", "sense-c128"],
                    help="sense: the metric's workload (default); the others are reported beside it")
     args = p.parse_args()
     if args.warmup < 3:

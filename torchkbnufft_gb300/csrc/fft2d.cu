@@ -350,9 +350,13 @@ __host__ __device__ constexpr int ct_threads() {
   return NC == 0 ? kFftMaxThreads : CtPlan<NC>::P * kFftF;
 }
 // resident CTAs asked of the register allocator: about 1024 threads per SM
-template <int NC>
+// in single precision, half that in double (twice the registers per value)
+template <int NC, typename R = float>
 __host__ __device__ constexpr int ct_min_blocks() {
-  return NC == 0 ? 1 : (1024 / ct_threads<NC>() > 1 ? 1024 / ct_threads<NC>() : 1);
+  return NC == 0 ? 1
+                 : ((1024 / ct_threads<NC>()) / (int)(sizeof(R) / sizeof(float)) > 1
+                        ? (1024 / ct_threads<NC>()) / (int)(sizeof(R) / sizeof(float))
+                        : 1);
 }
 
 // ------------------------------------------------------------ kernels
@@ -467,7 +471,7 @@ struct NoIo {
 // unit (every global access is a run of F complex values), transformed
 // between global memory and two shared buffers.
 template <typename R, int MODE, int NC>
-__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
+__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC, R>())
     k_fft_cols_io(Fft2dShape s, const cplx<R>* __restrict__ tw, int64_t planes, int64_t C,
                   const cplx<R>* __restrict__ kernel, int64_t kbatch, int by_channel, R scale,
                   cplx<R>* __restrict__ grid) {
@@ -525,7 +529,7 @@ __global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
 }
 
 template <typename R, int MODE, int NC>
-__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
+__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC, R>())
     k_fft_cols(Fft2dShape s, FftPlan1 pl, const cplx<R>* __restrict__ tw, int64_t planes, int64_t C,
                const cplx<R>* __restrict__ kernel, int64_t kbatch, int by_channel, R scale,
                cplx<R>* __restrict__ grid) {
@@ -667,7 +671,7 @@ __global__ void __launch_bounds__(ct_threads<NC>()) k_fft_rows_pad(Fft2dShape s,
 // image [* smaps] * scaling * scale straight from global memory (zero past
 // N1), the last stage writes the grid row.
 template <typename R, int NC>
-__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
+__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC, R>())
     k_fft_rows_pad_io(Fft2dShape s, const cplx<R>* __restrict__ tw, int64_t B, int64_t C, int64_t ci,
                       const cplx<R>* __restrict__ image, const cplx<R>* __restrict__ smaps, int64_t sb,
                       const cplx<R>* __restrict__ scaling, R scale, cplx<R>* __restrict__ grid) {
@@ -716,7 +720,7 @@ __global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
 // writes the sum). The coil sum is taken in the same order as the
 // shared-memory kernel's.
 template <typename R, int NC>
-__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
+__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC, R>())
     k_ifft_rows_crop_io(Fft2dShape s, const cplx<R>* __restrict__ tw, int64_t B, int64_t C,
                         const cplx<R>* __restrict__ grid, const cplx<R>* __restrict__ smaps, int64_t sb,
                         const cplx<R>* __restrict__ scaling, R scale, cplx<R>* __restrict__ out) {
@@ -791,7 +795,7 @@ __global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
 // by conj(smaps) and summed over coils into out[b, 0, n0, :]. The next
 // step's rows are copied in (cp.async) while a step is transformed.
 template <typename R, int NC>
-__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC>())
+__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC, R>())
     k_ifft_rows_crop(Fft2dShape s, FftPlan1 pl, const cplx<R>* __restrict__ tw, int64_t B, int64_t C,
                      const cplx<R>* __restrict__ grid, const cplx<R>* __restrict__ smaps, int64_t sb,
                      const cplx<R>* __restrict__ scaling, R scale, cplx<R>* __restrict__ out) {
@@ -971,10 +975,10 @@ static int fft_launch_shape(K kernel, int threads, size_t smem, int64_t units, i
 }
 
 // Calls fn(std::integral_constant<int, NC>) with NC = n when n has a
-// compile-time plan (complex64 only), else NC = 0 (runtime plan).
+// compile-time plan, else NC = 0 (runtime plan).
 template <typename R, typename Fn>
 static int with_size(int n, Fn&& fn) {
-  if constexpr (std::is_same<R, float>::value) {
+  {
     switch (n) {
       case 256: return fn(std::integral_constant<int, 256>{});
       case 320: return fn(std::integral_constant<int, 320>{});
@@ -1022,7 +1026,7 @@ static int cols_r(const Fft2dShape& s, const FftPlan1& pl, const void* tw, int m
         break;
     }
     return check_cuda(cudaGetLastError(), "fft column pass launch");
-  }
+  } else {
   const size_t smem = 3 * (size_t)pl.n * kFftF * sizeof(cplx<R>);
   const int threads = threads_for<NC>(pl);
   const int64_t units = planes * ((s.K1 + kFftF - 1) / kFftF);
@@ -1046,6 +1050,7 @@ static int cols_r(const Fft2dShape& s, const FftPlan1& pl, const void* tw, int m
       break;
   }
   return check_cuda(cudaGetLastError(), "fft column pass launch");
+  }
 }
 
 template <typename R, int NC>
@@ -1062,16 +1067,17 @@ static int rows_pad_r(const Fft2dShape& s, const FftPlan1& pl, const void* tw, i
                                                             (const cplx<R>*)smaps, sb, (const cplx<R>*)scaling,
                                                             (R)scale, (cplx<R>*)grid);
     return check_cuda(cudaGetLastError(), "fft row pass launch");
+  } else {
+    const size_t smem = 2 * (size_t)pl.n * kFftF * sizeof(cplx<R>);
+    const int threads = threads_for<NC>(pl);
+    int blocks;
+    int rc = fft_launch_shape(k_fft_rows_pad<R, NC>, threads, smem, B * s.N0, &blocks);
+    if (rc) return rc;
+    k_fft_rows_pad<R, NC><<<blocks, threads, smem, st>>>(
+        s, pl, (const cplx<R>*)tw, B, C, ci, (const cplx<R>*)image, (const cplx<R>*)smaps, sb,
+        (const cplx<R>*)scaling, (R)scale, (cplx<R>*)grid);
+    return check_cuda(cudaGetLastError(), "fft row pass launch");
   }
-  const size_t smem = 2 * (size_t)pl.n * kFftF * sizeof(cplx<R>);
-  const int threads = threads_for<NC>(pl);
-  int blocks;
-  int rc = fft_launch_shape(k_fft_rows_pad<R, NC>, threads, smem, B * s.N0, &blocks);
-  if (rc) return rc;
-  k_fft_rows_pad<R, NC><<<blocks, threads, smem, st>>>(
-      s, pl, (const cplx<R>*)tw, B, C, ci, (const cplx<R>*)image, (const cplx<R>*)smaps, sb,
-      (const cplx<R>*)scaling, (R)scale, (cplx<R>*)grid);
-  return check_cuda(cudaGetLastError(), "fft row pass launch");
 }
 
 template <typename R, int NC>
@@ -1088,16 +1094,17 @@ static int rows_crop_r(const Fft2dShape& s, const FftPlan1& pl, const void* tw, 
                                                               (const cplx<R>*)smaps, sb, (const cplx<R>*)scaling,
                                                               (R)scale, (cplx<R>*)out);
     return check_cuda(cudaGetLastError(), "ifft row pass launch");
+  } else {
+    const size_t smem = (3 * (size_t)pl.n * kFftF + s.N1) * sizeof(cplx<R>);
+    const int threads = threads_for<NC>(pl);
+    int blocks;
+    int rc = fft_launch_shape(k_ifft_rows_crop<R, NC>, threads, smem, B * s.N0, &blocks);
+    if (rc) return rc;
+    k_ifft_rows_crop<R, NC><<<blocks, threads, smem, st>>>(
+        s, pl, (const cplx<R>*)tw, B, C, (const cplx<R>*)grid, (const cplx<R>*)smaps, sb, (const cplx<R>*)scaling,
+        (R)scale, (cplx<R>*)out);
+    return check_cuda(cudaGetLastError(), "ifft row pass launch");
   }
-  const size_t smem = (3 * (size_t)pl.n * kFftF + s.N1) * sizeof(cplx<R>);
-  const int threads = threads_for<NC>(pl);
-  int blocks;
-  int rc = fft_launch_shape(k_ifft_rows_crop<R, NC>, threads, smem, B * s.N0, &blocks);
-  if (rc) return rc;
-  k_ifft_rows_crop<R, NC><<<blocks, threads, smem, st>>>(
-      s, pl, (const cplx<R>*)tw, B, C, (const cplx<R>*)grid, (const cplx<R>*)smaps, sb, (const cplx<R>*)scaling,
-      (R)scale, (cplx<R>*)out);
-  return check_cuda(cudaGetLastError(), "ifft row pass launch");
 }
 
 template <typename R>
