@@ -203,16 +203,27 @@ __device__ __forceinline__ void load_patch(const Geo<R>& geo, const cplx<R>* __r
   const int KX = geo.K[D - 1];
   const int rows = cells / PX;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int gx0 = wrap_up(origin[D - 1] + lane, KX);
-  for (int rr = warp; rr < rows; rr += kWarps) {
-    const int64_t rbase = patch_row_base<R, D>(geo, rr, origin);
-    for (int c = 0; c < ncl; ++c) {
-      const cplx<R>* src = grid + (plane0 + c) * gtot + rbase;
-      cplx<R>* dst = patch + c * ps + rr * PX;
-      int gx = gx0;
-      for (int px = lane; px < PX; px += 32) {
-        cp_async_elem(dst + px, src + gx);
-        gx = wrap_up(gx + 32, KX);
+  if (PX <= 16) {
+    // short rows (3D tiles): each half-warp copies one row
+    const int half = lane >> 4, hl = lane & 15;
+    const int gx = wrap_up(origin[D - 1] + hl, KX);
+    for (int rr = 2 * warp + half; rr < rows; rr += 2 * kWarps) {
+      const int64_t rbase = patch_row_base<R, D>(geo, rr, origin);
+      if (hl < PX)
+        for (int c = 0; c < ncl; ++c) cp_async_elem(patch + c * ps + rr * PX + hl, grid + (plane0 + c) * gtot + rbase + gx);
+    }
+  } else {
+    const int gx0 = wrap_up(origin[D - 1] + lane, KX);
+    for (int rr = warp; rr < rows; rr += kWarps) {
+      const int64_t rbase = patch_row_base<R, D>(geo, rr, origin);
+      for (int c = 0; c < ncl; ++c) {
+        const cplx<R>* src = grid + (plane0 + c) * gtot + rbase;
+        cplx<R>* dst = patch + c * ps + rr * PX;
+        int gx = gx0;
+        for (int px = lane; px < PX; px += 32) {
+          cp_async_elem(dst + px, src + gx);
+          gx = wrap_up(gx + 32, KX);
+        }
       }
     }
   }
