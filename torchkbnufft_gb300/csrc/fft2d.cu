@@ -285,10 +285,10 @@ struct CtPlan<1024> {
   static constexpr int R0 = 8, R1 = 8, R2 = 4, R3 = 4, P = 128;
 };
 
-template <typename R, int DIR, int N, int RAD, int NS, int P>
+template <typename R, int DIR, int N, int RAD, int NS, int P, int F = kFftF>
 __device__ __forceinline__ void stage_ct(const cplx<R>* __restrict__ in, cplx<R>* __restrict__ out, int f, int tj,
                                          const cplx<R>* __restrict__ tw) {
-  constexpr int F = kFftF, T = N / RAD, TSTEP = N / (NS * RAD), ITERS = (T + P - 1) / P;
+  constexpr int T = N / RAD, TSTEP = N / (NS * RAD), ITERS = (T + P - 1) / P;
 #pragma unroll
   for (int it = 0; it < ITERS; ++it) {
     const int j = tj + it * P;
@@ -367,6 +367,7 @@ __host__ __device__ constexpr int ct_min_blocks() {
 //   kColToep: forward FFT (zero rows skipped), times kernel * scale,
 //             inverse FFT, rows < N0 written.
 enum ColMode { kColFwd = 0, kColInv = 1, kColToep = 2 };
+constexpr int kColWidth = 8;  // columns per unit of the compile-time column passes
 
 // Transforms that read their first stage straight from global memory and
 // write their last stage straight back (compile-time plans): four passes
@@ -375,9 +376,9 @@ enum ColMode { kColFwd = 0, kColInv = 1, kColToep = 2 };
 // input is padded), st(i, v) takes output element i.
 //   first stage : butterfly j takes inputs j + r N/R0
 //   last stage  : butterfly j gives outputs (j - k) R + k + r Ns
-template <typename R, int DIR, int N, int RAD, int P, class LD>
+template <typename R, int DIR, int N, int RAD, int P, int F, class LD>
 __device__ __forceinline__ void stage_ct_first(LD ld, cplx<R>* __restrict__ out, int f, int tj) {
-  constexpr int F = kFftF, T = N / RAD, ITERS = (T + P - 1) / P;
+  constexpr int T = N / RAD, ITERS = (T + P - 1) / P;
 #pragma unroll
   for (int it = 0; it < ITERS; ++it) {
     const int j = tj + it * P;
@@ -393,10 +394,10 @@ __device__ __forceinline__ void stage_ct_first(LD ld, cplx<R>* __restrict__ out,
   }
 }
 
-template <typename R, int DIR, int N, int RAD, int NS, int P, class ST>
+template <typename R, int DIR, int N, int RAD, int NS, int P, int F, class ST>
 __device__ __forceinline__ void stage_ct_last(const cplx<R>* __restrict__ in, ST st, int f, int tj,
                                               const cplx<R>* __restrict__ tw) {
-  constexpr int F = kFftF, T = N / RAD, TSTEP = N / (NS * RAD), ITERS = (T + P - 1) / P;
+  constexpr int T = N / RAD, TSTEP = N / (NS * RAD), ITERS = (T + P - 1) / P;
 #pragma unroll
   for (int it = 0; it < ITERS; ++it) {
     const int j = tj + it * P;
@@ -422,38 +423,39 @@ __device__ __forceinline__ void stage_ct_last(const cplx<R>* __restrict__ in, ST
 // Whole transform. FROM_GLOBAL: the first stage reads through ld, else from
 // buf0. TO_GLOBAL: the last stage writes through st (returns nullptr), else
 // it stays in shared memory (the returned buffer).
-template <typename R, int DIR, int N, bool FROM_GLOBAL, bool TO_GLOBAL, class LD, class ST>
+template <typename R, int DIR, int N, bool FROM_GLOBAL, bool TO_GLOBAL, int FW = kFftF, class LD, class ST>
 __device__ __forceinline__ cplx<R>* fft_ct_io(LD ld, ST st, cplx<R>* buf0, cplx<R>* buf1, int f, int tj,
                                               const cplx<R>* __restrict__ tw) {
   using Pl = CtPlan<N>;
+  constexpr int P = Pl::P * kFftF / FW;  // threads per transform: FW transforms side by side
   constexpr int S = Pl::R3 > 1 ? 4 : 3;
   static_assert(Pl::R2 > 1, "direct-IO plans have at least three stages");
   constexpr int NS1 = Pl::R0, NS2 = Pl::R0 * Pl::R1, NS3 = Pl::R0 * Pl::R1 * Pl::R2;
   if constexpr (FROM_GLOBAL) {
-    stage_ct_first<R, DIR, N, Pl::R0, Pl::P>(ld, buf1, f, tj);
+    stage_ct_first<R, DIR, N, Pl::R0, P, FW>(ld, buf1, f, tj);
   } else {
-    stage_ct<R, DIR, N, Pl::R0, 1, Pl::P>(buf0, buf1, f, tj, tw);
+    stage_ct<R, DIR, N, Pl::R0, 1, P, FW>(buf0, buf1, f, tj, tw);
   }
   __syncthreads();
-  stage_ct<R, DIR, N, Pl::R1, NS1, Pl::P>(buf1, buf0, f, tj, tw);
+  stage_ct<R, DIR, N, Pl::R1, NS1, P, FW>(buf1, buf0, f, tj, tw);
   __syncthreads();
   if constexpr (S == 4) {
-    stage_ct<R, DIR, N, Pl::R2, NS2, Pl::P>(buf0, buf1, f, tj, tw);
+    stage_ct<R, DIR, N, Pl::R2, NS2, P, FW>(buf0, buf1, f, tj, tw);
     __syncthreads();
     if constexpr (TO_GLOBAL) {
-      stage_ct_last<R, DIR, N, Pl::R3, NS3, Pl::P>(buf1, st, f, tj, tw);
+      stage_ct_last<R, DIR, N, Pl::R3, NS3, P, FW>(buf1, st, f, tj, tw);
       return nullptr;
     } else {
-      stage_ct<R, DIR, N, Pl::R3, NS3, Pl::P>(buf1, buf0, f, tj, tw);
+      stage_ct<R, DIR, N, Pl::R3, NS3, P, FW>(buf1, buf0, f, tj, tw);
       __syncthreads();
       return buf0;
     }
   } else {
     if constexpr (TO_GLOBAL) {
-      stage_ct_last<R, DIR, N, Pl::R2, NS2, Pl::P>(buf0, st, f, tj, tw);
+      stage_ct_last<R, DIR, N, Pl::R2, NS2, P, FW>(buf0, st, f, tj, tw);
       return nullptr;
     } else {
-      stage_ct<R, DIR, N, Pl::R2, NS2, Pl::P>(buf0, buf1, f, tj, tw);
+      stage_ct<R, DIR, N, Pl::R2, NS2, P, FW>(buf0, buf1, f, tj, tw);
       __syncthreads();
       return buf1;
     }
@@ -467,16 +469,17 @@ struct NoIo {
   }
 };
 
-// Column pass with compile-time plan NC: F adjacent columns of one plane per
-// unit (every global access is a run of F complex values), transformed
-// between global memory and two shared buffers.
-template <typename R, int MODE, int NC>
-__global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC, R>())
+// Column pass with compile-time plan NC: FW adjacent columns of one plane
+// per unit (every global access is a run of FW complex values), transformed
+// between global memory and two shared buffers by P * kFftF / FW threads
+// per column.
+template <typename R, int MODE, int NC, int FW>
+__global__ void __launch_bounds__(ct_threads<NC>(), FW == kFftF ? ct_min_blocks<NC, R>() : (sizeof(R) == 4 ? 2 : 1))
     k_fft_cols_io(Fft2dShape s, const cplx<R>* __restrict__ tw, int64_t planes, int64_t C,
                   const cplx<R>* __restrict__ kernel, int64_t kbatch, int by_channel, R scale,
                   cplx<R>* __restrict__ grid) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int F = kFftF, P = CtPlan<NC>::P;
+  constexpr int F = FW, P = CtPlan<NC>::P * kFftF / FW;
   cplx<R>* buf0 = reinterpret_cast<cplx<R>*>(smem_raw);
   cplx<R>* buf1 = buf0 + NC * F;
   const int f = threadIdx.x % F, tj = threadIdx.x / F;
@@ -497,7 +500,7 @@ __global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC, R>())
       if (cok && row < nstore) g[(int64_t)row * K1] = cscale<R>(v, osc);
     };
     if (MODE == kColToep) {
-      cplx<R>* res = fft_ct_io<R, -1, NC, true, false>(ld, NoIo{}, buf0, buf1, f, tj, tw);
+      cplx<R>* res = fft_ct_io<R, -1, NC, true, false, FW>(ld, NoIo{}, buf0, buf1, f, tj, tw);
       const int64_t k = kbatch == 1 ? 0 : (by_channel ? plane % C : plane / C);
       const cplx<R>* kp = kernel + k * gtot + (cok ? col : 0);
       for (int m0 = tj; m0 < NC; m0 += 4 * P) {
@@ -516,13 +519,13 @@ __global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC, R>())
       __syncthreads();
       // second transform from res; the other buffer is its partner
       if (res == buf0)
-        fft_ct_io<R, +1, NC, false, true>(NoIo{}, st, buf0, buf1, f, tj, tw);
+        fft_ct_io<R, +1, NC, false, true, FW>(NoIo{}, st, buf0, buf1, f, tj, tw);
       else
-        fft_ct_io<R, +1, NC, false, true>(NoIo{}, st, buf1, buf0, f, tj, tw);
+        fft_ct_io<R, +1, NC, false, true, FW>(NoIo{}, st, buf1, buf0, f, tj, tw);
     } else if (MODE == kColInv) {
-      fft_ct_io<R, +1, NC, true, true>(ld, st, buf0, buf1, f, tj, tw);
+      fft_ct_io<R, +1, NC, true, true, FW>(ld, st, buf0, buf1, f, tj, tw);
     } else {
-      fft_ct_io<R, -1, NC, true, true>(ld, st, buf0, buf1, f, tj, tw);
+      fft_ct_io<R, -1, NC, true, true, FW>(ld, st, buf0, buf1, f, tj, tw);
     }
     __syncthreads();
   }
@@ -1002,27 +1005,29 @@ template <typename R, int NC>
 static int cols_r(const Fft2dShape& s, const FftPlan1& pl, const void* tw, int mode, int64_t planes, int64_t C,
                   const void* kernel, int64_t kbatch, int by_channel, double scale, void* grid, cudaStream_t st) {
   if constexpr (NC != 0) {
-    // compile-time plan: first and last stages straight from and to the grid
-    const size_t smem = 2 * (size_t)NC * kFftF * sizeof(cplx<R>);
+    // compile-time plan: first and last stages straight from and to the grid,
+    // kColWidth columns side by side (64-byte row runs in single precision)
+    constexpr int FW = kColWidth;
+    const size_t smem = 2 * (size_t)NC * FW * sizeof(cplx<R>);
     const int threads = CtPlan<NC>::P * kFftF;
-    const int64_t units = planes * ((s.K1 + kFftF - 1) / kFftF);
+    const int64_t units = planes * ((s.K1 + FW - 1) / FW);
     int blocks, rc;
     switch (mode) {
       case kColFwd:
-        if ((rc = fft_launch_shape(k_fft_cols_io<R, kColFwd, NC>, threads, smem, units, &blocks))) return rc;
-        k_fft_cols_io<R, kColFwd, NC><<<blocks, threads, smem, st>>>(s, (const cplx<R>*)tw, planes, C, nullptr, 1, 0,
-                                                                     (R)scale, (cplx<R>*)grid);
+        if ((rc = fft_launch_shape(k_fft_cols_io<R, kColFwd, NC, FW>, threads, smem, units, &blocks))) return rc;
+        k_fft_cols_io<R, kColFwd, NC, FW><<<blocks, threads, smem, st>>>(s, (const cplx<R>*)tw, planes, C, nullptr,
+                                                                         1, 0, (R)scale, (cplx<R>*)grid);
         break;
       case kColInv:
-        if ((rc = fft_launch_shape(k_fft_cols_io<R, kColInv, NC>, threads, smem, units, &blocks))) return rc;
-        k_fft_cols_io<R, kColInv, NC><<<blocks, threads, smem, st>>>(s, (const cplx<R>*)tw, planes, C, nullptr, 1, 0,
-                                                                     (R)scale, (cplx<R>*)grid);
+        if ((rc = fft_launch_shape(k_fft_cols_io<R, kColInv, NC, FW>, threads, smem, units, &blocks))) return rc;
+        k_fft_cols_io<R, kColInv, NC, FW><<<blocks, threads, smem, st>>>(s, (const cplx<R>*)tw, planes, C, nullptr,
+                                                                         1, 0, (R)scale, (cplx<R>*)grid);
         break;
       default:
-        if ((rc = fft_launch_shape(k_fft_cols_io<R, kColToep, NC>, threads, smem, units, &blocks))) return rc;
-        k_fft_cols_io<R, kColToep, NC><<<blocks, threads, smem, st>>>(s, (const cplx<R>*)tw, planes, C,
-                                                                      (const cplx<R>*)kernel, kbatch, by_channel,
-                                                                      (R)scale, (cplx<R>*)grid);
+        if ((rc = fft_launch_shape(k_fft_cols_io<R, kColToep, NC, FW>, threads, smem, units, &blocks))) return rc;
+        k_fft_cols_io<R, kColToep, NC, FW><<<blocks, threads, smem, st>>>(s, (const cplx<R>*)tw, planes, C,
+                                                                          (const cplx<R>*)kernel, kbatch,
+                                                                          by_channel, (R)scale, (cplx<R>*)grid);
         break;
     }
     return check_cuda(cudaGetLastError(), "fft column pass launch");
