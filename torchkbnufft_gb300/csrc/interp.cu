@@ -18,6 +18,9 @@
 // The separable sums group the products per dimension; the table bins, cell
 // indices and phase argument are computed exactly as the reference does.
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cstring>
 #include <new>
@@ -194,6 +197,20 @@ __device__ __forceinline__ void cp_async_16(float2* smem_dst, const float2* gsrc
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Tensor-memory-access store of a 3D box from shared memory (bulk group).
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* smem, int x, int y, int z) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];\n" ::"l"(map),
+               "r"(s), "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
 
 template <typename R, int D>
 __device__ __forceinline__ void load_patch(const Geo<R>& geo, const cplx<R>* __restrict__ grid, int64_t plane0,
@@ -1156,10 +1173,14 @@ __device__ __forceinline__ void reg_columns(const int32_t* ko, int r_lo, int r_h
 // the staged points in turn (point p goes to group p mod NG). With more than
 // one group, the groups' partial tiles are summed in a fixed order through
 // shared memory before the write-out, so results stay deterministic.
+// tmap (or null): the grid as a 3D tensor (2 K1 floats, K0 rows, B C planes)
+// with a box of one tile of CC planes; whole unsplit tiles of CC coils are
+// then written by one tensor store from shared memory.
 template <int CC>
 __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& a, const float* __restrict__ tm,
                                         const float2* __restrict__ ph, const float2* __restrict__ kdata,
-                                        float2* __restrict__ grid, int vec_ok, int64_t job, unsigned char* smem_raw) {
+                                        float2* __restrict__ grid, int vec_ok, int64_t job, unsigned char* smem_raw,
+                                        const CUtensorMap* tmap) {
   constexpr int D = 2, NJ = 6;
   constexpr int RPW = 32 / CC, WPT = kRegTileY / RPW, NG = kWarps / WPT;
   static_assert(CC >= 2 && CC <= 16 && (CC & (CC - 1)) == 0, "coils per job");
@@ -1248,8 +1269,25 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
     }
     const int ex = ext[1];
     if (NG == 1) {
-      // C: write this lane's row of its coil plane; split tiles add atomically
-      if (rowok && c < ncl) {
+      // C: whole unsplit tiles of CC coils go out as one tensor store (the
+      // staging buffers are free after the last batch's barrier; rows and
+      // columns past the grid edge fall outside the tensor and are dropped);
+      // otherwise each lane writes its row, split tiles adding atomically
+      if (tmap && it.pad == 0 && ncl == CC && ((uintptr_t)smem_raw & 127) == 0) {
+        float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float2*>(smem_raw) +
+                                                (c * kRegTileY + myrow) * kRegTileX);
+#pragma unroll
+        for (int x = 0; x < kRegTileX; x += 2)
+          dst[x / 2] = make_float4(racc[x].x, racc[x].y, racc[x + 1].x, racc[x + 1].y);
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          tma_store_3d(tmap, smem_raw, 2 * origin[1], origin[0], (int)(b * a.C + c0));
+          bulk_commit();
+          bulk_wait_read();
+        }
+        __syncthreads();
+      } else if (rowok && c < ncl) {
         float2* dst = grid + (b * a.C + c0 + c) * a.gtot + (int64_t)(origin[0] + myrow) * geo.K[1] + origin[1];
         if (it.pad == 0) {
           if (vec_ok) {
@@ -1499,15 +1537,15 @@ __global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg3(Geo<float> geo,
 }
 
 template <int CC>
-__global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg(Geo<float> geo, OwnLaunch a,
-                                                                const float* __restrict__ tm,
-                                                                const float2* __restrict__ ph,
-                                                                const float2* __restrict__ kdata,
-                                                                float2* __restrict__ grid, int vec_ok) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__global__ void __launch_bounds__(kThreads, 3)
+    k_interp_adj_reg(Geo<float> geo, OwnLaunch a, const float* __restrict__ tm, const float2* __restrict__ ph,
+                     const float2* __restrict__ kdata, float2* __restrict__ grid, int vec_ok, int use_tmap,
+                     const __grid_constant__ CUtensorMap tmap) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   const int64_t njobs = a.hdr[1] * a.nbpt * a.ncc;
   for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
-    reg_job<CC>(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw);
+    reg_job<CC>(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw, use_tmap ? &tmap : nullptr);
+  if (use_tmap && threadIdx.x == 0) bulk_wait();  // every tensor store has completed
 }
 
 template <typename R>
@@ -1792,7 +1830,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ragged_adj_reg(const RaggedProb
       __syncthreads();
       cur = pj.x;
     }
-    reg_job<CC>(sp.geo, sp.o, sp.tm, sp.ph, sp.kdata, sp.grid, sp.vec_ok, pj.y, smem_raw);
+    reg_job<CC>(sp.geo, sp.o, sp.tm, sp.ph, sp.kdata, sp.grid, sp.vec_ok, pj.y, smem_raw, nullptr);
   }
 }
 
@@ -1994,6 +2032,32 @@ constexpr int max_combo() {
   return D == 1 ? 8 : (D == 2 ? 16 : 27);
 }
 
+// Tensor map of a complex64 grid (planes x K0 x K1) as floats, box = one
+// 16 x 14 tile of `planes_box` planes, for the register adjoint's tensor
+// stores. False when the driver entry point is missing or encoding fails
+// (the kernel then writes rows itself).
+static bool grid_tensor_map(void* grid, int64_t K0, int64_t K1, int64_t planes, int planes_box, CUtensorMap* out) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    return (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }();
+  if (!encode || (uintptr_t)grid % 16 != 0 || K1 % 2 != 0 || planes < 1) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)(2 * K1), (cuuint64_t)K0, (cuuint64_t)planes};
+  const cuuint64_t strides[2] = {(cuuint64_t)(2 * K1 * 4), (cuuint64_t)(K0 * K1 * 8)};
+  const cuuint32_t box[3] = {2 * kRegTileX, kRegTileY, (cuuint32_t)planes_box};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return encode(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, grid, dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 static OwnLaunch make_own(const InterpPlan& ip, const char* ws, int D) {
   OwnLaunch o;
   o.jobs = (const Item*)(ws + ip.L.off_adj_jobs);
@@ -2100,9 +2164,13 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
         int rc = resident_blocks(k_interp_adj_reg<CC>, rsmem, max_jobs, &blocks);
         if (rc) return rc;
         const int vec_ok = ((uintptr_t)grid % 16 == 0) && (geo.K[1] % 2 == 0);
+        CUtensorMap tmap;
+        std::memset(&tmap, 0, sizeof(tmap));
+        const int use_tmap = CC == kRegCoils && vec_ok && grid_tensor_map(grid, geo.K[0], geo.K[1], o.B * o.C, CC, &tmap);
         k_interp_adj_reg<CC><<<blocks, kThreads, rsmem, s>>>(geo, orr, (const float*)(ws + ip.L.off_coords),
                                                              (const float2*)(ws + ip.L.off_phase),
-                                                             (const float2*)kdata, (float2*)grid, vec_ok);
+                                                             (const float2*)kdata, (float2*)grid, vec_ok, use_tmap,
+                                                             tmap);
         return check_cuda(cudaGetLastError(), "interp_adj launch");
       });
     }
