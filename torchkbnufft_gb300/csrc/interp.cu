@@ -1139,7 +1139,7 @@ constexpr int kRegKeyRows = kRegTileY + 5, kRegKeys = kRegKeyRows * (kRegTileX +
 // the batch's sorted chunk; sloc[p] = (row offset, list position of its
 // k-space values). With point groups (NG > 1) group g takes p = g mod NG.
 template <int CC, int NG, int LXI>
-__device__ __forceinline__ void reg_columns(const int32_t* ko, int r_lo, int r_hi, int q0, int nv,
+__device__ __forceinline__ void reg_columns(const int32_t* ko, int r_lo, int r_hi,
                                            int grp, const float2* __restrict__ sfac, const float2* __restrict__ sv,
                                            const int2* __restrict__ sloc, int myrow, bool rowok, int c,
                                            float2 (&racc)[kRegTileX]) {
@@ -1162,7 +1162,7 @@ __device__ __forceinline__ void reg_columns(const int32_t* ko, int r_lo, int r_h
     reg_add_cols<kRegTileX, LX>(racc, vy, fx);
   }
   if constexpr (LXI + 1 < kRegTileX + 5)
-    reg_columns<CC, NG, LXI + 1>(ko, r_lo, r_hi, q0, nv, grp, sfac, sv, sloc, myrow, rowok, c, racc);
+    reg_columns<CC, NG, LXI + 1>(ko, r_lo, r_hi, grp, sfac, sv, sloc, myrow, rowok, c, racc);
 }
 
 // vec_ok: the grid pointer is 16-byte aligned and K1 is even, so every
@@ -1263,7 +1263,7 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
       {
         const int r_lo = (warp % WPT) * RPW, r_hi = min(r_lo + RPW, ext[0]);
         if (r_lo < r_hi)
-          reg_columns<CC, NG, 0>(ko, r_lo, r_hi, q0, nv, grp, sfac, sv, sloc, myrow, rowok, c, racc);
+          reg_columns<CC, NG, 0>(ko, r_lo, r_hi, grp, sfac, sv, sloc, myrow, rowok, c, racc);
       }
       __syncthreads();
     }
@@ -1354,7 +1354,7 @@ constexpr int kReg3KeyRows = kReg3Y + 5, kReg3Keys = kReg3KeyRows * (kReg3X + 5)
 // positions ko[k(LXI, ylo - 5)] .. ko[k(LXI, yhi - 1) + 1] of the batch's
 // sorted chunk; sloc[p] = (z offset, y offset, list position of its values).
 template <int CC, int NG, int LXI>
-__device__ __forceinline__ void reg3_columns(const int32_t* ko, int ylo, int yhi, int q0, int nv, int grp,
+__device__ __forceinline__ void reg3_columns(const int32_t* ko, int ylo, int yhi, int grp,
                                             const float2* __restrict__ sfac, const float2* __restrict__ sv,
                                             const int4* __restrict__ sloc, int mz, int my, bool rowok, int c,
                                             float2 (&racc)[kReg3X]) {
@@ -1380,7 +1380,7 @@ __device__ __forceinline__ void reg3_columns(const int32_t* ko, int ylo, int yhi
     reg_add_cols<kReg3X, LX>(racc, vzy, fx);
   }
   if constexpr (LXI + 1 < kReg3X + 5)
-    reg3_columns<CC, NG, LXI + 1>(ko, ylo, yhi, q0, nv, grp, sfac, sv, sloc, mz, my, rowok, c, racc);
+    reg3_columns<CC, NG, LXI + 1>(ko, ylo, yhi, grp, sfac, sv, sloc, mz, my, rowok, c, racc);
 }
 
 template <int CC>
@@ -1467,7 +1467,7 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
       // B: runs of the list sorted by (column offset, row offset): for each
       // column offset, the points whose rows reach y0 .. y_hi - 1
       if (y0 < y_hi)
-        reg3_columns<CC, NG, 0>(ko, y0, y_hi, q0, nv, grp, sfac, sv, sloc, mz, my, rowok, c, racc);
+        reg3_columns<CC, NG, 0>(ko, y0, y_hi, grp, sfac, sv, sloc, mz, my, rowok, c, racc);
       __syncthreads();
     }
     const int ex = ext[2];
