@@ -81,6 +81,12 @@ extern "C" {
                                         is bitwise repeatable (heavy tiles are not spread over
                                         several CTAs). Must be the same in tkbn_points_build
                                         and every call that uses the layout. */
+#define TKBN_TABLES_LINEAR_PHASE 8   /* every table is |table[k]| exp(i c (k - J*L/2) / L) to
+                                        within float rounding, with c = 2 arg(table[J*L/2 + L/2])
+                                        (true for KB tables: the fftshift phase is linear in the
+                                        distance); the complex64 2D register adjoint then works
+                                        with real kernel values and applies the phases per point
+                                        and per tile cell. Set only after checking the tables. */
 #define TKBN_LAYOUT_FORWARD_ONLY 4   /* layout without the adjoint's per-tile point lists
                                         (smaller workspace, for forward-only callers); an
                                         adjoint on it scans candidates instead (slower). Must

@@ -13,6 +13,11 @@ from conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
 DEV = torch.device("cuda")
+# per-problem calls and the ragged launch agree to the complex64 parity bar:
+# with linear-phase tables a per-problem 2D adjoint of 16 coils accumulates
+# real kernel values and applies the phases per point and per cell, while the
+# ragged launch multiplies the complex table factors
+TOL = 1e-5
 
 
 def _problems(seed, spec):
@@ -54,10 +59,10 @@ def test_ragged_matches_per_problem_calls():
     rn = tkbn.RaggedNufft(probs)
     ks = rn.forward(images)
     for a, b in zip(ks, rk):
-        assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
+        assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < TOL
     xs = rn.adjoint()
     for a, b in zip(xs, rx):
-        assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
+        assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < TOL
 
 
 def test_ragged_graph_replay_matches_eager():
@@ -76,14 +81,14 @@ def test_ragged_graph_replay_matches_eager():
     rn.replay()
     torch.cuda.synchronize()
     for p in range(len(SPEC)):
-        assert rel_l2(rn.output_view(p).cpu().numpy(), eager[p].cpu().numpy()) < 1e-6
+        assert rel_l2(rn.output_view(p).cpu().numpy(), eager[p].cpu().numpy()) < TOL
     # new inputs through the same graph
     _, images2 = _problems(5, SPEC)
     rn.set_images(images2)
     rn.replay()
     _, rx2 = _reference(probs, images2)
     for p in range(len(SPEC)):
-        assert rel_l2(rn.output_view(p).cpu().numpy(), rx2[p].cpu().numpy()) < 1e-6
+        assert rel_l2(rn.output_view(p).cpu().numpy(), rx2[p].cpu().numpy()) < TOL
 
 
 def test_ragged_with_autotuned_layouts():
@@ -97,9 +102,9 @@ def test_ragged_with_autotuned_layouts():
     ks = rn.forward(images)
     xs = rn.adjoint()
     for a, b in zip(ks, rk):
-        assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
+        assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < TOL
     for a, b in zip(xs, rx):
-        assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
+        assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) < TOL
 
 
 def test_ragged_rejects_batched_trajectories():

@@ -42,6 +42,7 @@ class Geometry(ctypes.Structure):
 TKBN_TABLES_CONJ_SYMMETRIC = 1
 TKBN_ADJ_DETERMINISTIC = 2
 TKBN_LAYOUT_FORWARD_ONLY = 4
+TKBN_TABLES_LINEAR_PHASE = 8
 
 
 class PointsDesc(ctypes.Structure):

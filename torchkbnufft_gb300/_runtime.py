@@ -22,6 +22,7 @@ import weakref
 from dataclasses import dataclass
 from typing import List, Optional, Sequence, Tuple
 
+import numpy as np
 import torch
 
 from . import _lib as L
@@ -298,6 +299,35 @@ def _conj_symmetric(t: torch.Tensor) -> bool:
                         lambda: bool(torch.equal(t[c + 1:], t[:c].flip(0).conj())))
 
 
+def _linear_phase(t: torch.Tensor) -> bool:
+    """|t[k]| exp(i c (k - center) / L) == t[k] to within float rounding, c from the
+    entry L/2 past the centre (the device derives c the same way); L = (len - 1) / J
+    is not known here, so every even L dividing len - 1 into J = 2..8 is tried."""
+
+    def check() -> bool:
+        if not t.is_complex() or t.dtype != torch.complex64:
+            return False
+        h = t.detach().cpu().numpy().astype(np.complex128)
+        n = h.size
+        if n < 3 or n % 2 == 0:
+            return False
+        center = (n - 1) // 2
+        scale = float(np.max(np.abs(h)))
+        if scale == 0.0:
+            return False
+        for J in range(2, 9):
+            if (n - 1) % J or ((n - 1) // J) % 2:
+                continue
+            L = (n - 1) // J
+            c = 2.0 * np.angle(h[center + L // 2])
+            u = (np.arange(n) - center) / L
+            if np.max(np.abs(h - np.abs(h) * np.exp(1j * c * u))) <= 1e-6 * scale:
+                return True
+        return False
+
+    return _cached_prop(("lin", id(t), t._version, t.data_ptr()), t, check)
+
+
 def table_ptrs(tables: Sequence[torch.Tensor], dtype: torch.dtype):
     """Device pointers of the per-dim tables, the tensors kept alive, and geometry flags.
 
@@ -319,6 +349,8 @@ def table_ptrs(tables: Sequence[torch.Tensor], dtype: torch.dtype):
             if same:
                 ptrs[d] = ptrs[0]
     flags = L.TKBN_TABLES_CONJ_SYMMETRIC if all(_conj_symmetric(t) for t in keep) else 0
+    if all(_linear_phase(t) for t in keep):
+        flags |= L.TKBN_TABLES_LINEAR_PHASE
     return L.ptr_array(ptrs), keep, flags
 
 

@@ -1120,14 +1120,98 @@ __device__ __forceinline__ void reg_point_factors(const Geo<float>& geo, const f
   }
 }
 
-// Pre-pass of the 2D register adjoint: every sorted point's 12 factors once
+// Linear-phase tables (TKBN_TABLES_LINEAR_PHASE): table[k] = m(k) e^{i c u_k},
+// u_k = (k - center) / L, m >= 0. A point's factors sit at u_0 - j (u_0 in
+// (J/2 - 1, J/2]), so with E[n] = e^{-i c n} and h^ = h / |h|,
+//   e^{-i c u_0} = conj(h^[2]) E[2]       (h[2]: |u| <= 1, a well-defined phase)
+// and, with tile-local cell (y, x) and footprint start (ry, rx), jy = y - ry:
+//   conj(hy[jy] hx[jx] phase) = my[jy] mx[jx] * Q * R(y, x),
+//   Q = conj(phase hy^[2] hx^[2]) Ey[2 + ry] Ex[2 + rx],  R(y, x) = conj(Ey[y] Ex[x]).
+// The adjoint multiplies the k-space values by Q (per list entry),
+// accumulates with the real my, mx and multiplies the tile by R. The slope c
+// is fitted by least squares to the table's phases over u in (0, 1] (error
+// ~1e-8), and the E tables are evaluated in double.
+constexpr int kLpE0 = 3;              // E tables start at n = -kLpE0
+constexpr int kLpEy = kRegTileY + 5;  // n = -3 .. 17 (entries 2 + ry and cells y)
+constexpr int kLpEx = kRegTileX + 5;  // n = -3 .. 15
+
+// Least-squares slope of dim d's table phase, computed by one whole warp.
+__device__ __forceinline__ double lp_slope_warp(const Geo<float>& geo, int d) {
+  constexpr int D = 2;
+  const int lane = threadIdx.x & 31;
+  const int center = sel<int, D>(geo.center, d), L = sel<int, D>(geo.L, d);
+  const float2* tab = sel<const float2*, D>(geo.tab, d);
+  const bool half = sel<bool, D>(geo.half, d);
+  double su = 0.0, suu = 0.0;
+  for (int k = 1 + lane; k <= L; k += 32) {
+    const float2 h = table_entry<float>(tab, center + k, center, half);
+    const double u = (double)k / (double)L;
+    su += u * (double)atan2f(h.y, h.x);
+    suu += u * u;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    su += __shfl_xor_sync(0xffffffffu, su, o);
+    suu += __shfl_xor_sync(0xffffffffu, suu, o);
+  }
+  return su / suu;
+}
+
+// Per sorted point: {mx[6], my[6], P} with P = conj(phase hy^[2] hx^[2]) (16 floats).
+__device__ __forceinline__ void reg_point_factors_lp(const Geo<float>& geo, const float* __restrict__ tm,
+                                                     const float2* __restrict__ ph, int64_t n, int64_t i,
+                                                     float* out) {
+  constexpr int D = 2, NJ = 6;
+  float2 P = ph[i];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const float tv = tm[d * n + i];
+    const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
+    const float Lr = sel<float, D>(geo.Lr, d);
+    const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
+    const float2* tab = sel<const float2*, D>(geo.tab, d);
+    const bool half = sel<bool, D>(geo.half, d);
+    float* m = out + (d == 0 ? NJ : 0);  // mx first: 16-byte aligned for the adjoint's loads
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
+      m[j] = sqrtf(te.x * te.x + te.y * te.y);
+      if (j == 2) P = cmul<float>(P, make_float2(te.x / m[j], te.y / m[j]));
+    }
+  }
+  out[12] = P.x;
+  out[13] = -P.y;
+  out[14] = 0.f;
+  out[15] = 0.f;
+}
+
+// Pre-pass of the 2D register adjoint: every sorted point's factors once
 // (a point sits in 1.8 tile lists on average), so the adjoint's staging is
-// plain 16-byte copies.
+// plain 16-byte copies. LP: the linear-phase form (16 floats per point).
+// etab (LP): {Ey[kLpEy], Ex[kLpEx]}, written by block 0 (warp d fits dim
+// d's phase slope, its lanes evaluate E_d[n] = e^{-i c n} in double).
+template <bool LP>
 __global__ void __launch_bounds__(kThreads) k_point_factors2(Geo<float> geo, const float* __restrict__ tm,
                                                              const float2* __restrict__ ph, int64_t n,
-                                                             float2* __restrict__ pfac) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 2 * n; e += (int64_t)gridDim.x * blockDim.x)
-    reg_point_factors(geo, tm, ph, n, e >> 1, (int)(e & 1), pfac + e * 6);
+                                                             float2* __restrict__ pfac, float2* __restrict__ etab) {
+  if constexpr (LP) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (blockIdx.x == 0 && warp < 2) {
+      const double c = lp_slope_warp(geo, warp);
+      const int cnt = warp == 0 ? kLpEy : kLpEx;
+      if (lane < cnt) {
+        double sn, cs;
+        sincos(c * (double)(lane - kLpE0), &sn, &cs);
+        etab[(warp == 0 ? 0 : kLpEy) + lane] = make_float2((float)cs, (float)-sn);
+      }
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+      reg_point_factors_lp(geo, tm, ph, n, i, reinterpret_cast<float*>(pfac) + i * 16);
+  } else {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 2 * n;
+         e += (int64_t)gridDim.x * blockDim.x)
+      reg_point_factors(geo, tm, ph, n, e >> 1, (int)(e & 1), pfac + e * 6);
+  }
 }
 
 // Footprint starts of a 16 x 14 tile with J = 6: row offsets -5 .. 15 (21),
@@ -1165,6 +1249,53 @@ __device__ __forceinline__ void reg_columns(const int32_t* ko, int r_lo, int r_h
     reg_columns<CC, NG, LXI + 1>(ko, r_lo, r_hi, grp, sfac, sv, sloc, myrow, rowok, c, racc);
 }
 
+// racc[LX + jx] += vy * m[jx] for the columns inside the row (real factors).
+template <int TXR, int LX>
+__device__ __forceinline__ void reg_add_cols_real(float2 (&racc)[TXR], float2 vy, const float (&m)[6]) {
+#pragma unroll
+  for (int jx = 0; jx < 6; ++jx)
+    if (LX + jx >= 0 && LX + jx < TXR) {
+      racc[LX + jx].x = fmaf(vy.x, m[jx], racc[LX + jx].x);
+      racc[LX + jx].y = fmaf(vy.y, m[jx], racc[LX + jx].y);
+    }
+}
+
+// End of the 2D register adjoint's staging buffers (shared memory): the
+// linear-phase E tables follow.
+__host__ __device__ constexpr size_t reg_rtab_offset(int CC) {
+  return (size_t)kNBR * 2 * 6 * sizeof(float2) + (size_t)CC * kSVS * sizeof(float2) + (size_t)kNBR * sizeof(int2) +
+         (size_t)(kRegKeys + 1) * sizeof(int32_t);
+}
+
+// Linear-phase form of reg_columns: sfr[p] = {mx[6], my[6]} (48 bytes), the
+// staged k-space values already carry Q.
+template <int CC, int NG, int LXI>
+__device__ __forceinline__ void reg_columns_lp(const int32_t* ko, int r_lo, int r_hi, int grp,
+                                              const float* __restrict__ sfr, const float2* __restrict__ sv,
+                                              const int2* __restrict__ sloc, int myrow, bool rowok, int c,
+                                              float2 (&racc)[kRegTileX]) {
+  constexpr int NJ = 6, LX = LXI - 5;
+  const int kb = LXI * kRegKeyRows;
+  int p = ko[kb + r_lo];
+  const int e = ko[kb + r_hi + 5];
+  if (NG > 1) p += (grp - p % NG + NG) % NG;
+  for (; p < e; p += NG) {
+    const int2 lp = sloc[p];
+    const int jy = myrow - lp.x;
+    const float* fp = sfr + p * (2 * NJ);
+    float my = 0.f;
+    if (rowok && (unsigned)jy < (unsigned)NJ) my = fp[NJ + jy];
+    const float2 v = sv[c * kSVS + lp.y];
+    const float2 vy = make_float2(v.x * my, v.y * my);
+    const float4 m03 = *reinterpret_cast<const float4*>(fp);
+    const float2 m45 = *reinterpret_cast<const float2*>(fp + 4);
+    const float m[6] = {m03.x, m03.y, m03.z, m03.w, m45.x, m45.y};
+    reg_add_cols_real<kRegTileX, LX>(racc, vy, m);
+  }
+  if constexpr (LXI + 1 < kRegTileX + 5)
+    reg_columns_lp<CC, NG, LXI + 1>(ko, r_lo, r_hi, grp, sfr, sv, sloc, myrow, rowok, c, racc);
+}
+
 // vec_ok: the grid pointer is 16-byte aligned and K1 is even, so every
 // tile row starts 16-byte aligned and pairs of cells go out as one float4.
 // CC coils per job (2, 4, 8 or 16; one coil runs as CC = 2 with the second
@@ -1176,11 +1307,14 @@ __device__ __forceinline__ void reg_columns(const int32_t* ko, int r_lo, int r_h
 // tmap (or null): the grid as a 3D tensor (2 K1 floats, K0 rows, B C planes)
 // with a box of one tile of CC planes; whole unsplit tiles of CC coils are
 // then written by one tensor store from shared memory.
-template <int CC>
+// LP: linear-phase tables (see kLpE0): real factors from the pre-pass,
+// k-space values times Q per list entry, tile times R; etab = {Ey[kLpEy],
+// Ex[kLpEx]} in shared memory (set up by the kernel).
+template <int CC, bool LP = false>
 __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& a, const float* __restrict__ tm,
                                         const float2* __restrict__ ph, const float2* __restrict__ kdata,
                                         float2* __restrict__ grid, int vec_ok, int64_t job, unsigned char* smem_raw,
-                                        const CUtensorMap* tmap) {
+                                        const CUtensorMap* tmap, const float2* etab = nullptr) {
   constexpr int D = 2, NJ = 6;
   constexpr int RPW = 32 / CC, WPT = kRegTileY / RPW, NG = kWarps / WPT;
   static_assert(CC >= 2 && CC <= 16 && (CC & (CC - 1)) == 0, "coils per job");
@@ -1237,7 +1371,15 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
             sv[cl * kSVS + s] = make_float2(0.f, 0.f);
         }
       }
-      if (a.pfac) {
+      if (LP) {
+        // the point's real factors {mx[6], my[6]}: three 16-byte copies of its record
+        for (int e = threadIdx.x; e < nv * 3; e += kThreads) {
+          const int pt = e / 3, q = e - pt * 3;
+          const int4 ent = sents[pt];
+          if (q == 0) sloc[pt] = make_int2(ent.z, ent.y);
+          cp_async_16(sfac + pt * NJ + 2 * q, a.pfac + (int64_t)ent.x * 8 + 2 * q);
+        }
+      } else if (a.pfac) {
         // the point's 12 factors, precomputed per sorted point: six 16-byte copies
         for (int e = threadIdx.x; e < nv * 6; e += kThreads) {
           const int pt = e / 6, q = e - pt * 6;
@@ -1254,6 +1396,17 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
         }
       }
       cp_async_wait_all();
+      if (LP && (int)threadIdx.x < nv) {
+        // this thread's own copies have landed: the entry's values times
+        // Q = P Ey[2 + ry] Ex[2 + rx]
+        const int s = threadIdx.x;
+        const int4 ent = ents[s];
+        const float2 P = a.pfac[(int64_t)ent.x * 8 + 6];
+        const float2 Q =
+            cmul<float>(P, cmul<float>(etab[kLpE0 + 2 + ent.z], etab[kLpEy + kLpE0 + 2 + ent.w]));
+#pragma unroll 4
+        for (int cl = 0; cl < CC; ++cl) sv[cl * kSVS + s] = cmul<float>(sv[cl * kSVS + s], Q);
+      }
       __syncthreads();
       // B: the list is sorted by footprint start (column offset, then row
       // offset), so for each column offset LX the points that reach this
@@ -1262,12 +1415,24 @@ __device__ __forceinline__ void reg_job(const Geo<float>& geo, const OwnLaunch& 
       // static register indices. Lanes whose row the footprint misses add 0.
       {
         const int r_lo = (warp % WPT) * RPW, r_hi = min(r_lo + RPW, ext[0]);
-        if (r_lo < r_hi)
-          reg_columns<CC, NG, 0>(ko, r_lo, r_hi, grp, sfac, sv, sloc, myrow, rowok, c, racc);
+        if (r_lo < r_hi) {
+          if constexpr (LP)
+            reg_columns_lp<CC, NG, 0>(ko, r_lo, r_hi, grp, reinterpret_cast<const float*>(sfac), sv, sloc, myrow,
+                                      rowok, c, racc);
+          else
+            reg_columns<CC, NG, 0>(ko, r_lo, r_hi, grp, sfac, sv, sloc, myrow, rowok, c, racc);
+        }
       }
       __syncthreads();
     }
     const int ex = ext[1];
+    if constexpr (LP) {
+      // the tile-cell phase R(y, x) = conj(Ey[y] Ex[x]) (tile-local y, x)
+      const float2 ey = cconj<float>(etab[kLpE0 + myrow]);
+#pragma unroll
+      for (int x = 0; x < kRegTileX; ++x)
+        racc[x] = cmul<float>(racc[x], cmul<float>(ey, cconj<float>(etab[kLpEy + kLpE0 + x])));
+    }
     if (NG == 1) {
       // C: whole unsplit tiles of CC coils go out as one tensor store (the
       // staging buffers are free after the last batch's barrier; rows and
@@ -1536,15 +1701,21 @@ __global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg3(Geo<float> geo,
     reg3_job<CC>(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw);
 }
 
-template <int CC>
+template <int CC, bool LP>
 __global__ void __launch_bounds__(kThreads, 3)
     k_interp_adj_reg(Geo<float> geo, OwnLaunch a, const float* __restrict__ tm, const float2* __restrict__ ph,
                      const float2* __restrict__ kdata, float2* __restrict__ grid, int vec_ok, int use_tmap,
                      const __grid_constant__ CUtensorMap tmap) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
+  float2* etab = reinterpret_cast<float2*>(smem_raw + reg_rtab_offset(CC));  // {Ey, Ex}, past the staging
+  if constexpr (LP) {
+    // the phase tables written by the pre-pass, after the per-point records
+    if (threadIdx.x < kLpEy + kLpEx) etab[threadIdx.x] = a.pfac[a.n * 12 + threadIdx.x];
+    __syncthreads();
+  }
   const int64_t njobs = a.hdr[1] * a.nbpt * a.ncc;
   for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
-    reg_job<CC>(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw, use_tmap ? &tmap : nullptr);
+    reg_job<CC, LP>(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw, use_tmap ? &tmap : nullptr, etab);
   if (use_tmap && threadIdx.x == 0) bulk_wait();  // every tensor store has completed
 }
 
@@ -1869,6 +2040,7 @@ struct InterpPlan {
   Launch a;
   size_t smem;
   int64_t max_jobs;
+  int flags;  // the call's geometry flags (TKBN_TABLES_*, layout bits)
 };
 
 enum class Op { kFwd, kAdj, kGrad };
@@ -1878,6 +2050,7 @@ static int prepare(const tkbn_geometry* g, const tkbn_points_desc* p, const void
                    InterpPlan* ip) {
   int rc = points_layout(g, p, &ip->L);
   if (rc) return rc;
+  ip->flags = g->flags;
   if (!ws) return set_error(TKBN_ERR_INVALID, "points workspace is null");
   if (B < 1 || C < 1) return set_error(TKBN_ERR_INVALID, "batch and coil counts must be >= 1");
   if (p->ntraj != 1 && p->ntraj != B)
@@ -2122,8 +2295,7 @@ static size_t reg3_smem(int CC) {
 }
 
 static size_t reg_smem(int CC) {
-  const size_t staging = (size_t)kNBR * 2 * 6 * sizeof(float2) + (size_t)CC * kSVS * sizeof(float2) +
-                         (size_t)kNBR * sizeof(int2) + (size_t)(kRegKeys + 1) * sizeof(int32_t);
+  const size_t staging = reg_rtab_offset(CC) + (size_t)(kLpEy + kLpEx) * sizeof(float2);
   const int ng = kWarps / (kRegTileY / (32 / CC));
   const size_t partials = ng > 1 ? (size_t)ng * kRegTileY * kRegTileX * CC * sizeof(float2) : 0;
   return staging > partials ? staging : partials;
@@ -2149,29 +2321,39 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
   if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
     if (reg_eligible<R, D, JC>(ip, o)) {
       OwnLaunch orr = o;
+      // linear-phase tables: real factors (needs the per-point pre-pass)
+      const bool lp = (ip.flags & TKBN_TABLES_LINEAR_PHASE) && ip.L.pfac;
       if (ip.L.pfac && ip.a.n > 0) {
         // the layout's factor scratch (see tkbn_interp_adj: calls sharing a workspace are ordered)
         float2* pf = (float2*)const_cast<char*>(ws + ip.L.off_pfac);
-        const int64_t nb = (2 * ip.a.n + kThreads - 1) / kThreads;
-        k_point_factors2<<<(int)(nb < 152 * 16 ? nb : 152 * 16), kThreads, 0, s>>>(
-            geo, (const float*)(ws + ip.L.off_coords), (const float2*)(ws + ip.L.off_phase), ip.a.n, pf);
+        const int64_t nb = ((lp ? 1 : 2) * ip.a.n + kThreads - 1) / kThreads;
+        const int grid_b = (int)(nb < 152 * 16 ? nb : 152 * 16);
+        float2* et = pf + ip.a.n * 12;  // past the records: {Ey, Ex} of the linear-phase form
+        if (lp)
+          k_point_factors2<true><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
+                                                              (const float2*)(ws + ip.L.off_phase), ip.a.n, pf, et);
+        else
+          k_point_factors2<false><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
+                                                               (const float2*)(ws + ip.L.off_phase), ip.a.n, pf, et);
         orr.pfac = pf;
       }
       return with_cc(reg_cc(o.Cc), [&](auto ccv) {
         constexpr int CC = decltype(ccv)::value;
         const size_t rsmem = reg_smem(CC);
-        int blocks;
-        int rc = resident_blocks(k_interp_adj_reg<CC>, rsmem, max_jobs, &blocks);
-        if (rc) return rc;
         const int vec_ok = ((uintptr_t)grid % 16 == 0) && (geo.K[1] % 2 == 0);
         CUtensorMap tmap;
         std::memset(&tmap, 0, sizeof(tmap));
         const int use_tmap = CC == kRegCoils && vec_ok && grid_tensor_map(grid, geo.K[0], geo.K[1], o.B * o.C, CC, &tmap);
-        k_interp_adj_reg<CC><<<blocks, kThreads, rsmem, s>>>(geo, orr, (const float*)(ws + ip.L.off_coords),
-                                                             (const float2*)(ws + ip.L.off_phase),
-                                                             (const float2*)kdata, (float2*)grid, vec_ok, use_tmap,
-                                                             tmap);
-        return check_cuda(cudaGetLastError(), "interp_adj launch");
+        auto launch = [&](auto kernel) {
+          int blocks;
+          int rc = resident_blocks(kernel, rsmem, max_jobs, &blocks);
+          if (rc) return rc;
+          kernel<<<blocks, kThreads, rsmem, s>>>(geo, orr, (const float*)(ws + ip.L.off_coords),
+                                                 (const float2*)(ws + ip.L.off_phase), (const float2*)kdata,
+                                                 (float2*)grid, vec_ok, use_tmap, tmap);
+          return check_cuda(cudaGetLastError(), "interp_adj launch");
+        };
+        return lp && orr.pfac ? launch(k_interp_adj_reg<CC, true>) : launch(k_interp_adj_reg<CC, false>);
       });
     }
   }

@@ -593,7 +593,7 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   L->off_koff = o;
   o = align_up(o + 4 * (size_t)L->koff_rows * (L->knk + 1));
   L->off_pfac = o;
-  o = align_up(o + (L->pfac ? (size_t)L->npts_total * 12 * 8 : 0));
+  o = align_up(o + (L->pfac ? (size_t)L->npts_total * 12 * 8 + 512 : 0));  // + linear-phase tables
   L->off_coords = o;
   o = align_up(o + rsize * g->ndim * n);
   L->off_phase = o;
