@@ -1135,54 +1135,60 @@ constexpr int kLpE0 = 3;              // E tables start at n = -kLpE0
 constexpr int kLpEy = kRegTileY + 5;  // n = -3 .. 17 (entries 2 + ry and cells y)
 constexpr int kLpEx = kRegTileX + 5;  // n = -3 .. 15
 
-// Least-squares slope of dim d's table phase, computed by one whole warp.
-__device__ __forceinline__ double lp_slope_warp(const Geo<float>& geo, int d) {
+// Least-squares slopes of both dims' table phases over u = k / L in (0, 1]
+// (the whole block; returns (cy, cx) to every thread).
+__device__ __forceinline__ double2 lp_slopes_block(const Geo<float>& geo) {
   constexpr int D = 2;
-  const int lane = threadIdx.x & 31;
-  const int center = sel<int, D>(geo.center, d), L = sel<int, D>(geo.L, d);
-  const float2* tab = sel<const float2*, D>(geo.tab, d);
-  const bool half = sel<bool, D>(geo.half, d);
-  double su = 0.0, suu = 0.0;
-  for (int k = 1 + lane; k <= L; k += 32) {
-    const float2 h = table_entry<float>(tab, center + k, center, half);
-    const double u = (double)k / (double)L;
-    su += u * (double)atan2f(h.y, h.x);
-    suu += u * u;
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    su += __shfl_xor_sync(0xffffffffu, su, o);
-    suu += __shfl_xor_sync(0xffffffffu, suu, o);
-  }
-  return su / suu;
-}
-
-// Per sorted point: {mx[6], my[6], P} with P = conj(phase hy^[2] hx^[2]) (16 floats).
-__device__ __forceinline__ void reg_point_factors_lp(const Geo<float>& geo, const float* __restrict__ tm,
-                                                     const float2* __restrict__ ph, int64_t n, int64_t i,
-                                                     float* out) {
-  constexpr int D = 2, NJ = 6;
-  float2 P = ph[i];
+  __shared__ double s_red[4][kWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};  // su_y, suu_y, su_x, suu_x
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    const float tv = tm[d * n + i];
-    const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
-    const float Lr = sel<float, D>(geo.Lr, d);
-    const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
+    const int center = sel<int, D>(geo.center, d), L = sel<int, D>(geo.L, d);
     const float2* tab = sel<const float2*, D>(geo.tab, d);
     const bool half = sel<bool, D>(geo.half, d);
-    float* m = out + (d == 0 ? NJ : 0);  // mx first: 16-byte aligned for the adjoint's loads
-#pragma unroll
-    for (int j = 0; j < NJ; ++j) {
-      const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
-      m[j] = sqrtf(te.x * te.x + te.y * te.y);
-      if (j == 2) P = cmul<float>(P, make_float2(te.x / m[j], te.y / m[j]));
+    for (int k = 1 + (int)threadIdx.x; k <= L; k += blockDim.x) {
+      const float2 h = table_entry<float>(tab, center + k, center, half);
+      const double u = (double)k / (double)L;
+      acc[2 * d] += u * (double)atan2f(h.y, h.x);
+      acc[2 * d + 1] += u * u;
     }
   }
-  out[12] = P.x;
-  out[13] = -P.y;
-  out[14] = 0.f;
-  out[15] = 0.f;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+    if (lane == 0) s_red[q][warp] = acc[q];
+  }
+  __syncthreads();
+  double tot[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot[q] += s_red[q][w];
+  __syncthreads();
+  return make_double2(tot[0] / tot[1], tot[2] / tot[3]);
+}
+
+// Per sorted point i, dim d (thread pair 2i, 2i + 1): {mx[6], my[6], P} with
+// P = conj(phase hy^[2] hx^[2]) (16 floats); returns this dim's h^[2].
+__device__ __forceinline__ float2 reg_point_factors_lp(const Geo<float>& geo, const float* __restrict__ tm,
+                                                       int64_t n, int64_t i, int d, float* out) {
+  constexpr int D = 2, NJ = 6;
+  const float tv = tm[d * n + i];
+  const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
+  const float Lr = sel<float, D>(geo.Lr, d);
+  const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
+  const float2* tab = sel<const float2*, D>(geo.tab, d);
+  const bool half = sel<bool, D>(geo.half, d);
+  float* m = out + (d == 0 ? NJ : 0);  // mx first: 16-byte aligned for the adjoint's loads
+  float2 hat = make_float2(1.f, 0.f);
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
+    m[j] = sqrtf(te.x * te.x + te.y * te.y);
+    if (j == 2) hat = make_float2(te.x / m[j], te.y / m[j]);
+  }
+  return hat;
 }
 
 // Pre-pass of the 2D register adjoint: every sorted point's factors once
@@ -1195,18 +1201,33 @@ __global__ void __launch_bounds__(kThreads) k_point_factors2(Geo<float> geo, con
                                                              const float2* __restrict__ ph, int64_t n,
                                                              float2* __restrict__ pfac, float2* __restrict__ etab) {
   if constexpr (LP) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (blockIdx.x == 0 && warp < 2) {
-      const double c = lp_slope_warp(geo, warp);
-      const int cnt = warp == 0 ? kLpEy : kLpEx;
-      if (lane < cnt) {
+    if (blockIdx.x == 0) {
+      const double2 c = lp_slopes_block(geo);
+      const int t = threadIdx.x;
+      if (t < kLpEy + kLpEx) {
+        const bool y = t < kLpEy;
         double sn, cs;
-        sincos(c * (double)(lane - kLpE0), &sn, &cs);
-        etab[(warp == 0 ? 0 : kLpEy) + lane] = make_float2((float)cs, (float)-sn);
+        sincos((y ? c.x : c.y) * (double)((y ? t : t - kLpEy) - kLpE0), &sn, &cs);
+        etab[t] = make_float2((float)cs, (float)-sn);
       }
     }
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-      reg_point_factors_lp(geo, tm, ph, n, i, reinterpret_cast<float*>(pfac) + i * 16);
+    // thread pair (2i, 2i + 1) takes point i's two dims; the pair meets to form P
+    for (int64_t e0 = blockIdx.x * (int64_t)blockDim.x; e0 < 2 * n; e0 += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t e = e0 + threadIdx.x, i = e >> 1;
+      const int d = (int)(e & 1);
+      const bool on = e < 2 * n;
+      float* rec = reinterpret_cast<float*>(pfac) + i * 16;
+      float2 hat = make_float2(1.f, 0.f);
+      if (on) hat = reg_point_factors_lp(geo, tm, n, i, d, rec);
+      const float2 other = make_float2(__shfl_xor_sync(0xffffffffu, hat.x, 1), __shfl_xor_sync(0xffffffffu, hat.y, 1));
+      if (on && d == 0) {
+        const float2 P = cmul<float>(cmul<float>(ph[i], hat), other);
+        rec[12] = P.x;
+        rec[13] = -P.y;
+        rec[14] = 0.f;
+        rec[15] = 0.f;
+      }
+    }
   } else {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 2 * n;
          e += (int64_t)gridDim.x * blockDim.x)
@@ -2326,7 +2347,7 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
       if (ip.L.pfac && ip.a.n > 0) {
         // the layout's factor scratch (see tkbn_interp_adj: calls sharing a workspace are ordered)
         float2* pf = (float2*)const_cast<char*>(ws + ip.L.off_pfac);
-        const int64_t nb = ((lp ? 1 : 2) * ip.a.n + kThreads - 1) / kThreads;
+        const int64_t nb = (2 * ip.a.n + kThreads - 1) / kThreads;
         const int grid_b = (int)(nb < 152 * 16 ? nb : 152 * 16);
         float2* et = pf + ip.a.n * 12;  // past the records: {Ey, Ex} of the linear-phase form
         if (lp)
