@@ -1172,7 +1172,7 @@ __device__ __forceinline__ double2 lp_slopes_block(const Geo<float>& geo) {
 // Per sorted point i, dim d (thread pair 2i, 2i + 1): {mx[6], my[6], P} with
 // P = conj(phase hy^[2] hx^[2]) (16 floats); returns this dim's h^[2].
 __device__ __forceinline__ float2 reg_point_factors_lp(const Geo<float>& geo, const float* __restrict__ tm,
-                                                       int64_t n, int64_t i, int d, float* out) {
+                                                       int64_t n, int64_t i, int d, float* out, bool* off) {
   constexpr int D = 2, NJ = 6;
   const float tv = tm[d * n + i];
   const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
@@ -1182,12 +1182,21 @@ __device__ __forceinline__ float2 reg_point_factors_lp(const Geo<float>& geo, co
   const bool half = sel<bool, D>(geo.half, d);
   float* m = out + (d == 0 ? NJ : 0);  // mx first: 16-byte aligned for the adjoint's loads
   float2 hat = make_float2(1.f, 0.f);
+  const int L = sel<int, D>(geo.L, d);
+  int k0 = 0;
+  bool mis = false;
 #pragma unroll
   for (int j = 0; j < NJ; ++j) {
-    const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
+    const int k = table_bin<float>(tv, base + j, Lr, center, tmax);
+    if (j == 0) k0 = k;
+    // the bins step by exactly L unless fl(tm - g) rounded (|tm| within a few
+    // cells of 0): then this tap's phase is not the linear form's
+    mis = mis || (k != k0 - j * L);
+    const float2 te = table_entry<float>(tab, k, center, half);
     m[j] = sqrtf(te.x * te.x + te.y * te.y);
     if (j == 2) hat = make_float2(te.x / m[j], te.y / m[j]);
   }
+  *off = mis;
   return hat;
 }
 
@@ -1196,10 +1205,14 @@ __device__ __forceinline__ float2 reg_point_factors_lp(const Geo<float>& geo, co
 // plain 16-byte copies. LP: the linear-phase form (16 floats per point).
 // etab (LP): {Ey[kLpEy], Ex[kLpEx]}, written by block 0 (warp d fits dim
 // d's phase slope, its lanes evaluate E_d[n] = e^{-i c n} in double).
+// Points whose bins do not step by exactly L (see reg_point_factors_lp) get
+// P = 0 (no contribution in the register adjoint) and go to `fix` (count in
+// *nfix, reset by the host), whose exact contributions k_adj_lp_fix adds.
 template <bool LP>
 __global__ void __launch_bounds__(kThreads) k_point_factors2(Geo<float> geo, const float* __restrict__ tm,
                                                              const float2* __restrict__ ph, int64_t n,
-                                                             float2* __restrict__ pfac, float2* __restrict__ etab) {
+                                                             float2* __restrict__ pfac, float2* __restrict__ etab,
+                                                             int32_t* __restrict__ fix, int32_t* __restrict__ nfix) {
   if constexpr (LP) {
     if (blockIdx.x == 0) {
       const double2 c = lp_slopes_block(geo);
@@ -1218,10 +1231,16 @@ __global__ void __launch_bounds__(kThreads) k_point_factors2(Geo<float> geo, con
       const bool on = e < 2 * n;
       float* rec = reinterpret_cast<float*>(pfac) + i * 16;
       float2 hat = make_float2(1.f, 0.f);
-      if (on) hat = reg_point_factors_lp(geo, tm, n, i, d, rec);
+      bool mis = false;
+      if (on) hat = reg_point_factors_lp(geo, tm, n, i, d, rec, &mis);
       const float2 other = make_float2(__shfl_xor_sync(0xffffffffu, hat.x, 1), __shfl_xor_sync(0xffffffffu, hat.y, 1));
+      mis = mis || __shfl_xor_sync(0xffffffffu, (int)mis, 1);
       if (on && d == 0) {
-        const float2 P = cmul<float>(cmul<float>(ph[i], hat), other);
+        float2 P = cmul<float>(cmul<float>(ph[i], hat), other);
+        if (mis) {
+          P = make_float2(0.f, 0.f);
+          fix[atomicAdd(nfix, 1)] = (int32_t)i;
+        }
         rec[12] = P.x;
         rec[13] = -P.y;
         rec[14] = 0.f;
@@ -1232,6 +1251,59 @@ __global__ void __launch_bounds__(kThreads) k_point_factors2(Geo<float> geo, con
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 2 * n;
          e += (int64_t)gridDim.x * blockDim.x)
       reg_point_factors(geo, tm, ph, n, e >> 1, (int)(e & 1), pfac + e * 6);
+  }
+}
+
+// Exact contributions of the points the linear-phase adjoint left out: one
+// thread per (listed point, batch item, coil) adds its 36 taps with vector
+// atomics, after the register adjoint has written its tiles.
+__global__ void __launch_bounds__(kThreads) k_adj_lp_fix(Geo<float> geo, OwnLaunch a, const float* __restrict__ tm,
+                                                         const float2* __restrict__ ph,
+                                                         const float2* __restrict__ kdata,
+                                                         const int32_t* __restrict__ fix,
+                                                         const int32_t* __restrict__ nfix, float2* __restrict__ grid) {
+  constexpr int D = 2, NJ = 6;
+  const int64_t nb = a.ntraj == 1 ? a.B : 1;
+  const int64_t total = (int64_t)(*nfix) * nb * a.C;
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = w % a.C, r = w / a.C;
+    const int64_t i = fix[r / nb];
+    const int32_t val = a.vals[i];
+    const int64_t t = val / a.M, m = val - t * a.M;
+    const int64_t b = a.ntraj == 1 ? r % nb : t;
+    float2 hy[NJ], hx[NJ];
+    int gy[NJ], gx[NJ];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const float tv = tm[d * a.n + i];
+      const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
+      const float Lr = sel<float, D>(geo.Lr, d);
+      const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
+      const float2* tab = sel<const float2*, D>(geo.tab, d);
+      const bool half = sel<bool, D>(geo.half, d);
+      const int K = sel<int, D>(geo.K, d);
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        const float2 te =
+            cconj<float>(table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half));
+        if (d == 0) {
+          hy[j] = te;
+          gy[j] = wrap_cell(base + j, K);
+        } else {
+          hx[j] = te;
+          gx[j] = wrap_cell(base + j, K);
+        }
+      }
+    }
+    const float2 v = cmulc<float>(kdata[(b * a.C + c) * a.M + m], ph[i]);
+    float2* plane = grid + (b * a.C + c) * a.gtot;
+#pragma unroll
+    for (int jy = 0; jy < NJ; ++jy) {
+      const float2 vy = cmul<float>(v, hy[jy]);
+#pragma unroll
+      for (int jx = 0; jx < NJ; ++jx)
+        atomic_add_global(plane + (int64_t)gy[jy] * geo.K[1] + gx[jx], cmul<float>(vy, hx[jx]));
+    }
   }
 }
 
@@ -2343,19 +2415,30 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
     if (reg_eligible<R, D, JC>(ip, o)) {
       OwnLaunch orr = o;
       // linear-phase tables: real factors (needs the per-point pre-pass)
-      const bool lp = (ip.flags & TKBN_TABLES_LINEAR_PHASE) && ip.L.pfac;
+      // (a deterministic layout keeps the table path: the linear-phase form
+      // adds its left-out points with atomics)
+      const bool lp = (ip.flags & TKBN_TABLES_LINEAR_PHASE) && !(ip.flags & TKBN_ADJ_DETERMINISTIC) && ip.L.pfac;
+      // the layout's factor scratch (see tkbn_interp_adj: calls sharing a workspace are ordered):
+      // per-point records, then {Ey, Ex} and the left-out count past them, the
+      // left-out list in the records' spare room
+      float2* pf = (float2*)const_cast<char*>(ws + ip.L.off_pfac);
+      float2* et = pf + ip.a.n * 12;
+      int32_t* nfix = reinterpret_cast<int32_t*>(et + kLpEy + kLpEx + 8);
+      int32_t* fix = reinterpret_cast<int32_t*>(pf + ip.a.n * 8);
       if (ip.L.pfac && ip.a.n > 0) {
-        // the layout's factor scratch (see tkbn_interp_adj: calls sharing a workspace are ordered)
-        float2* pf = (float2*)const_cast<char*>(ws + ip.L.off_pfac);
         const int64_t nb = (2 * ip.a.n + kThreads - 1) / kThreads;
         const int grid_b = (int)(nb < 152 * 16 ? nb : 152 * 16);
-        float2* et = pf + ip.a.n * 12;  // past the records: {Ey, Ex} of the linear-phase form
-        if (lp)
+        if (lp) {
+          int rc0 = check_cuda(cudaMemsetAsync(nfix, 0, sizeof(int32_t), s), "reset left-out count");
+          if (rc0) return rc0;
           k_point_factors2<true><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
-                                                              (const float2*)(ws + ip.L.off_phase), ip.a.n, pf, et);
-        else
+                                                              (const float2*)(ws + ip.L.off_phase), ip.a.n, pf, et,
+                                                              fix, nfix);
+        } else {
           k_point_factors2<false><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
-                                                               (const float2*)(ws + ip.L.off_phase), ip.a.n, pf, et);
+                                                               (const float2*)(ws + ip.L.off_phase), ip.a.n, pf, et,
+                                                               fix, nfix);
+        }
         orr.pfac = pf;
       }
       return with_cc(reg_cc(o.Cc), [&](auto ccv) {
@@ -2374,7 +2457,13 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
                                                  (float2*)grid, vec_ok, use_tmap, tmap);
           return check_cuda(cudaGetLastError(), "interp_adj launch");
         };
-        return lp && orr.pfac ? launch(k_interp_adj_reg<CC, true>) : launch(k_interp_adj_reg<CC, false>);
+        if (!(lp && orr.pfac)) return launch(k_interp_adj_reg<CC, false>);
+        int rc = launch(k_interp_adj_reg<CC, true>);
+        if (rc) return rc;
+        k_adj_lp_fix<<<152, kThreads, 0, s>>>(geo, orr, (const float*)(ws + ip.L.off_coords),
+                                               (const float2*)(ws + ip.L.off_phase), (const float2*)kdata, fix, nfix,
+                                               (float2*)grid);
+        return check_cuda(cudaGetLastError(), "interp_adj fix launch");
       });
     }
   }
