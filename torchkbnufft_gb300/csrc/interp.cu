@@ -1135,19 +1135,20 @@ constexpr int kLpE0 = 3;              // E tables start at n = -kLpE0
 constexpr int kLpEy = kRegTileY + 5;  // n = -3 .. 17 (entries 2 + ry and cells y)
 constexpr int kLpEx = kRegTileX + 5;  // n = -3 .. 15
 
-// Least-squares slopes of both dims' table phases over u = k / L in (0, 1]
-// (the whole block; returns (cy, cx) to every thread).
-__device__ __forceinline__ double2 lp_slopes_block(const Geo<float>& geo) {
-  constexpr int D = 2;
-  __shared__ double s_red[4][kWarps];
+// Least-squares slopes of the D dims' table phases over u = k / L in (0, 1]
+// (the whole block of kThreads threads; every thread gets c[0 .. D)).
+template <int D>
+__device__ __forceinline__ void lp_slopes_block(const Geo<float>& geo, double (&c)[D]) {
+  __shared__ double s_red[2 * D][kWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};  // su_y, suu_y, su_x, suu_x
+  double acc[2 * D];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
+    acc[2 * d] = acc[2 * d + 1] = 0.0;
     const int center = sel<int, D>(geo.center, d), L = sel<int, D>(geo.L, d);
     const float2* tab = sel<const float2*, D>(geo.tab, d);
     const bool half = sel<bool, D>(geo.half, d);
-    for (int k = 1 + (int)threadIdx.x; k <= L; k += blockDim.x) {
+    for (int k = 1 + (int)threadIdx.x; k <= L; k += kThreads) {
       const float2 h = table_entry<float>(tab, center + k, center, half);
       const double u = (double)k / (double)L;
       acc[2 * d] += u * (double)atan2f(h.y, h.x);
@@ -1155,18 +1156,22 @@ __device__ __forceinline__ double2 lp_slopes_block(const Geo<float>& geo) {
     }
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < 2 * D; ++q) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
     if (lane == 0) s_red[q][warp] = acc[q];
   }
   __syncthreads();
-  double tot[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-  for (int q = 0; q < 4; ++q)
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot[q] += s_red[q][w];
+  for (int d = 0; d < D; ++d) {
+    double su = 0.0, suu = 0.0;
+    for (int w = 0; w < kWarps; ++w) {
+      su += s_red[2 * d][w];
+      suu += s_red[2 * d + 1][w];
+    }
+    c[d] = su / suu;
+  }
   __syncthreads();
-  return make_double2(tot[0] / tot[1], tot[2] / tot[3]);
 }
 
 // Per sorted point i, dim d (thread pair 2i, 2i + 1): {mx[6], my[6], P} with
@@ -1215,12 +1220,13 @@ __global__ void __launch_bounds__(kThreads) k_point_factors2(Geo<float> geo, con
                                                              int32_t* __restrict__ fix, int32_t* __restrict__ nfix) {
   if constexpr (LP) {
     if (blockIdx.x == 0) {
-      const double2 c = lp_slopes_block(geo);
+      double c[2];
+      lp_slopes_block<2>(geo, c);
       const int t = threadIdx.x;
       if (t < kLpEy + kLpEx) {
         const bool y = t < kLpEy;
         double sn, cs;
-        sincos((y ? c.x : c.y) * (double)((y ? t : t - kLpEy) - kLpE0), &sn, &cs);
+        sincos((y ? c[0] : c[1]) * (double)((y ? t : t - kLpEy) - kLpE0), &sn, &cs);
         etab[t] = make_float2((float)cs, (float)-sn);
       }
     }
@@ -1641,10 +1647,54 @@ __device__ __forceinline__ void reg3_columns(const int32_t* ko, int ylo, int yhi
     reg3_columns<CC, NG, LXI + 1>(ko, ylo, yhi, grp, sfac, sv, sloc, mz, my, rowok, c, racc);
 }
 
-template <int CC>
+// Linear-phase 3D: per sorted position 20 floats {mx[6], pad[2], my[6], mz[6]}
+// (mx 16-byte aligned); E tables E_d[n], n = -kLp3E0 .. 9, per dim.
+constexpr int kLp3Rec = 20, kLp3E0 = 3, kLp3En = 13;
+
+template <int CC, int NG, int LXI>
+__device__ __forceinline__ void reg3_columns_lp(const int32_t* ko, int ylo, int yhi, int grp,
+                                               const float* __restrict__ sfr, const float2* __restrict__ sv,
+                                               const int4* __restrict__ sloc, int mz, int my, bool rowok, int c,
+                                               float2 (&racc)[kReg3X]) {
+  constexpr int NJ = 6, LX = LXI - 5;
+  const int kb = LXI * kReg3KeyRows;
+  int p = ko[kb + ylo];
+  const int e = ko[kb + yhi + 5];
+  if (NG > 1) p += (grp - p % NG + NG) % NG;
+  for (; p < e; p += NG) {
+    const int4 loc = sloc[p];
+    const int jz = mz - loc.x, jy = my - loc.y;
+    const float* fp = sfr + p * kLp3Rec;
+    float w = 0.f;
+    if (rowok && (unsigned)jz < (unsigned)NJ && (unsigned)jy < (unsigned)NJ) w = fp[14 + jz] * fp[8 + jy];
+    const float2 v = sv[c * kSVS + loc.z];
+    const float2 vzy = make_float2(v.x * w, v.y * w);
+    const float4 m03 = *reinterpret_cast<const float4*>(fp);
+    const float2 m45 = *reinterpret_cast<const float2*>(fp + 4);
+    const float m[6] = {m03.x, m03.y, m03.z, m03.w, m45.x, m45.y};
+    reg_add_cols_real<kReg3X, LX>(racc, vzy, m);
+  }
+  if constexpr (LXI + 1 < kReg3X + 5)
+    reg3_columns_lp<CC, NG, LXI + 1>(ko, ylo, yhi, grp, sfr, sv, sloc, mz, my, rowok, c, racc);
+}
+
+// End of the 3D register adjoint's staging buffers (the E tables follow).
+__host__ __device__ constexpr size_t reg3_etab_offset(int CC) {
+  return (((size_t)kNBR * 3 * 6 * sizeof(float2) + (size_t)CC * kSVS * sizeof(float2) + (size_t)kNBR * sizeof(int4) +
+           (size_t)(kReg3Keys + 1) * sizeof(int32_t)) + 7) & ~(size_t)7;
+}
+
+// LP (linear-phase tables, see kLpE0): real kernel values per sorted
+// position, k-space values times Q = conj(phase prod_d h_d^[2]) prod_d
+// E_d[2 + r_d] per list entry, tile times R = conj(prod_d E_d[cell_d]);
+// etab = {Ez, Ey, Ex} in shared memory. A point whose bins do not step by
+// exactly L gets Q = 0 and, from the entry of the tile holding its first
+// footprint cell, goes to lfix (count at 0, indices from 16) for the exact pass.
+template <int CC, bool LP = false>
 __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch& a, const float* __restrict__ tm,
                                          const float2* __restrict__ ph, const float2* __restrict__ kdata,
-                                         float2* __restrict__ grid, int vec_ok, int64_t job, unsigned char* smem_raw) {
+                                         float2* __restrict__ grid, int vec_ok, int64_t job, unsigned char* smem_raw,
+                                         const float2* etab = nullptr, int32_t* lfix = nullptr) {
   constexpr int D = 3, NJ = 6;
   // lane (coil, z, y): a warp covers all kReg3Z planes of YB rows y0 .. y0 + YB - 1
   constexpr int RPW = 32 / CC, YB = RPW / kReg3Z, WPT = kReg3Y / YB, NG = kWarps / WPT;
@@ -1712,23 +1762,84 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
         const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
         const float2* tab = sel<const float2*, D>(geo.tab, d);
         const bool half = sel<bool, D>(geo.half, d);
-        const float2 phv = d == 0 ? ph[ent.x] : make_float2(1.f, 0.f);
-        float2* out = sfac + e * NJ;
+        if constexpr (LP) {
+          // real magnitudes: x at 0, y at 8, z at 14 of the position's record
+          float* out = reinterpret_cast<float*>(sfac) + pt * kLp3Rec + (d == 2 ? 0 : (d == 1 ? 8 : 14));
 #pragma unroll
-        for (int j = 0; j < NJ; ++j) {
-          const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
-          out[j] = cconj<float>(d == 0 ? cmul<float>(te, phv) : te);
+          for (int j = 0; j < NJ; ++j) {
+            const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
+            out[j] = sqrtf(te.x * te.x + te.y * te.y);
+          }
+        } else {
+          const float2 phv = d == 0 ? ph[ent.x] : make_float2(1.f, 0.f);
+          float2* out = sfac + e * NJ;
+#pragma unroll
+          for (int j = 0; j < NJ; ++j) {
+            const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
+            out[j] = cconj<float>(d == 0 ? cmul<float>(te, phv) : te);
+          }
         }
       }
       cp_async_wait_all();
+      if (LP && (int)threadIdx.x < nv) {
+        // this thread's own copies have landed: entry s's values times Q
+        const int s = threadIdx.x;
+        const int4 ent = ents[s];
+        const int r[3] = {ent.z, (int)(short)(ent.w & 0xffff), ent.w >> 16};
+        float2 P = ph[ent.x];
+        float2 E = make_float2(1.f, 0.f);
+        bool mis = false;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const float tv = tm[d * a.n + ent.x];
+          const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
+          const float Lr = sel<float, D>(geo.Lr, d);
+          const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d), L = sel<int, D>(geo.L, d);
+          const int k0 = table_bin<float>(tv, base, Lr, center, tmax);
+          // for |tm| >= 8, tm and every g are within a factor 2 of each other:
+          // fl(tm - g) is exact and the bins step by exactly L
+          if (fabsf(tv) < 8.f) {
+#pragma unroll
+            for (int j = 1; j < NJ; ++j)
+              mis = mis || (table_bin<float>(tv, base + j, Lr, center, tmax) != k0 - j * L);
+          }
+          const float2 te = table_entry<float>(sel<const float2*, D>(geo.tab, d), k0 - 2 * L, center,
+                                               sel<bool, D>(geo.half, d));
+          const float mg = sqrtf(te.x * te.x + te.y * te.y);
+          P = cmul<float>(P, make_float2(te.x / mg, te.y / mg));
+          E = cmul<float>(E, etab[d * kLp3En + kLp3E0 + 2 + r[d]]);
+        }
+        float2 Q = cmul<float>(cconj<float>(P), E);
+        if (mis) {
+          Q = make_float2(0.f, 0.f);
+          // listed once: from its home tile's entry, in the job of batch item 0 and coil chunk 0
+          if (bb == 0 && cc == 0 && r[0] >= 0 && r[0] < kReg3Z && r[1] >= 0 && r[1] < kReg3Y && r[2] >= 0 &&
+              r[2] < kReg3X)
+            lfix[16 + atomicAdd(lfix, 1)] = ent.x;
+        }
+#pragma unroll
+        for (int cl = 0; cl < CC; ++cl) sv[cl * kSVS + s] = cmul<float>(sv[cl * kSVS + s], Q);
+      }
       __syncthreads();
       // B: runs of the list sorted by (column offset, row offset): for each
       // column offset, the points whose rows reach y0 .. y_hi - 1
-      if (y0 < y_hi)
-        reg3_columns<CC, NG, 0>(ko, y0, y_hi, grp, sfac, sv, sloc, mz, my, rowok, c, racc);
+      if (y0 < y_hi) {
+        if constexpr (LP)
+          reg3_columns_lp<CC, NG, 0>(ko, y0, y_hi, grp, reinterpret_cast<const float*>(sfac), sv, sloc, mz, my,
+                                     rowok, c, racc);
+        else
+          reg3_columns<CC, NG, 0>(ko, y0, y_hi, grp, sfac, sv, sloc, mz, my, rowok, c, racc);
+      }
       __syncthreads();
     }
     const int ex = ext[2];
+    if constexpr (LP) {
+      // the tile-cell phase R(z, y, x) = conj(Ez[z] Ey[y] Ex[x]) (tile-local)
+      const float2 ezy = cconj<float>(cmul<float>(etab[kLp3E0 + mz], etab[kLp3En + kLp3E0 + my]));
+#pragma unroll
+      for (int x = 0; x < kReg3X; ++x)
+        racc[x] = cmul<float>(racc[x], cmul<float>(ezy, cconj<float>(etab[2 * kLp3En + kLp3E0 + x])));
+    }
     if (NG == 1) {
       if (rowok && c < ncl) {
         float2* dst = grid + (b * a.C + c0 + c) * a.gtot +
@@ -1782,16 +1893,78 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
   }
 }
 
-template <int CC>
+template <int CC, bool LP>
 __global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg3(Geo<float> geo, OwnLaunch a,
                                                                  const float* __restrict__ tm,
                                                                  const float2* __restrict__ ph,
                                                                  const float2* __restrict__ kdata,
-                                                                 float2* __restrict__ grid, int vec_ok) {
+                                                                 float2* __restrict__ grid, int vec_ok,
+                                                                 int32_t* __restrict__ lfix) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* etab = reinterpret_cast<float2*>(smem_raw + reg3_etab_offset(CC));  // [3][kLp3En], past the staging
+  if constexpr (LP) {
+    // per CTA: the three dims' phase slopes (least squares) and E_d[n] = e^{-i c_d n} in double
+    double c3[3];
+    lp_slopes_block<3>(geo, c3);
+    if (threadIdx.x < 3 * kLp3En) {
+      const int d = threadIdx.x / kLp3En, nidx = threadIdx.x % kLp3En;
+      double sn, cs;
+      sincos(c3[d] * (double)(nidx - kLp3E0), &sn, &cs);
+      etab[threadIdx.x] = make_float2((float)cs, (float)-sn);
+    }
+    __syncthreads();
+  }
   const int64_t njobs = a.hdr[1] * a.nbpt * a.ncc;
   for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
-    reg3_job<CC>(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw);
+    reg3_job<CC, LP>(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw, etab, lfix);
+}
+
+// Exact contributions of the points the 3D linear-phase adjoint left out
+// (one thread per (listed point, batch item, coil), 216 taps with vector
+// atomics), after the register pass.
+__global__ void __launch_bounds__(kThreads) k_adj_lp_fix3(Geo<float> geo, OwnLaunch a, const float* __restrict__ tm,
+                                                          const float2* __restrict__ ph,
+                                                          const float2* __restrict__ kdata,
+                                                          const int32_t* __restrict__ lfix,
+                                                          float2* __restrict__ grid) {
+  constexpr int D = 3, NJ = 6;
+  const int64_t nb = a.ntraj == 1 ? a.B : 1;
+  const int64_t total = (int64_t)lfix[0] * nb * a.C;
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = w % a.C, r = w / a.C;
+    const int64_t i = lfix[16 + r / nb];
+    const int32_t val = a.vals[i];
+    const int64_t t = val / a.M, m = val - t * a.M;
+    const int64_t b = a.ntraj == 1 ? r % nb : t;
+    float2 h[D][NJ];
+    int g[D][NJ];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const float tv = tm[d * a.n + i];
+      const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        h[d][j] = cconj<float>(table_entry<float>(
+            sel<const float2*, D>(geo.tab, d),
+            table_bin<float>(tv, base + j, sel<float, D>(geo.Lr, d), sel<int, D>(geo.center, d),
+                             sel<int, D>(geo.tmax, d)),
+            sel<int, D>(geo.center, d), sel<bool, D>(geo.half, d)));
+        g[d][j] = wrap_cell(base + j, sel<int, D>(geo.K, d));
+      }
+    }
+    const float2 v = cmulc<float>(kdata[(b * a.C + c) * a.M + m], ph[i]);
+    float2* plane = grid + (b * a.C + c) * a.gtot;
+    for (int jz = 0; jz < NJ; ++jz) {
+      const float2 vz = cmul<float>(v, h[0][jz]);
+#pragma unroll
+      for (int jy = 0; jy < NJ; ++jy) {
+        const float2 vzy = cmul<float>(vz, h[1][jy]);
+        const int64_t row = ((int64_t)g[0][jz] * geo.K[1] + g[1][jy]) * geo.K[2];
+#pragma unroll
+        for (int jx = 0; jx < NJ; ++jx) atomic_add_global(plane + row + g[2][jx], cmul<float>(vzy, h[2][jx]));
+      }
+    }
+  }
 }
 
 template <int CC, bool LP>
@@ -2380,8 +2553,7 @@ static bool reg3_eligible(const InterpPlan& ip, const OwnLaunch& o) {
 }
 
 static size_t reg3_smem(int CC) {
-  const size_t staging = (size_t)kNBR * 3 * 6 * sizeof(float2) + (size_t)CC * kSVS * sizeof(float2) +
-                         (size_t)kNBR * sizeof(int4) + (size_t)(kReg3Keys + 1) * sizeof(int32_t);
+  const size_t staging = reg3_etab_offset(CC) + (size_t)3 * kLp3En * sizeof(float2);
   const int ng = kWarps / (kReg3Rows / (32 / CC));
   const size_t partials = ng > 1 ? (size_t)ng * kReg3Rows * kReg3X * CC * sizeof(float2) : 0;
   return staging > partials ? staging : partials;
@@ -2472,14 +2644,28 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
       return with_cc(reg_cc(o.Cc), [&](auto ccv) {
         constexpr int CC = decltype(ccv)::value < 8 ? decltype(ccv)::value : 8;
         const size_t rsmem = reg3_smem(CC);
-        int blocks;
-        int rc = resident_blocks(k_interp_adj_reg3<CC>, rsmem, max_jobs, &blocks);
-        if (rc) return rc;
         const int vec_ok = ((uintptr_t)grid % 16 == 0) && (geo.K[2] % 2 == 0);
-        k_interp_adj_reg3<CC><<<blocks, kThreads, rsmem, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
-                                                              (const float2*)(ws + ip.L.off_phase),
-                                                              (const float2*)kdata, (float2*)grid, vec_ok);
-        return check_cuda(cudaGetLastError(), "interp_adj launch");
+        // linear-phase tables: real kernel values (not for deterministic layouts:
+        // the left-out points are added with atomics)
+        const bool lp = (ip.flags & TKBN_TABLES_LINEAR_PHASE) && !(ip.flags & TKBN_ADJ_DETERMINISTIC) && ip.L.lfix;
+        int32_t* lfix = lp ? (int32_t*)const_cast<char*>(ws + ip.L.off_lfix) : nullptr;
+        auto launch = [&](auto kernel) {
+          int blocks;
+          int rc = resident_blocks(kernel, rsmem, max_jobs, &blocks);
+          if (rc) return rc;
+          kernel<<<blocks, kThreads, rsmem, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
+                                                 (const float2*)(ws + ip.L.off_phase), (const float2*)kdata,
+                                                 (float2*)grid, vec_ok, lfix);
+          return check_cuda(cudaGetLastError(), "interp_adj launch");
+        };
+        if (!lp) return launch(k_interp_adj_reg3<CC, false>);
+        int rc = check_cuda(cudaMemsetAsync(lfix, 0, sizeof(int32_t), s), "reset left-out count");
+        if (!rc) rc = launch(k_interp_adj_reg3<CC, true>);
+        if (rc) return rc;
+        k_adj_lp_fix3<<<152, kThreads, 0, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
+                                                (const float2*)(ws + ip.L.off_phase), (const float2*)kdata, lfix,
+                                                (float2*)grid);
+        return check_cuda(cudaGetLastError(), "interp_adj fix launch");
       });
     }
   }

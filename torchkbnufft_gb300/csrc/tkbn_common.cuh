@@ -267,10 +267,13 @@ struct PointsLayout {
   // csort layouts: room for each sorted point's 12 conjugated table factors,
   // filled by the register adjoint before it runs
   bool pfac;
+  // 3D chunk-sorted layouts: list of points the linear-phase adjoint leaves
+  // out (count first, then indices)
+  bool lfix;
   size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
       off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_phase,
       off_tile_work, off_tile_nsub, off_tile_suboff, off_sj_raw, off_adj_jobs, off_sj_keys_in, off_sj_keys,
-      off_sj_vals_in, off_sj_vals, off_vcount, off_voff, off_vlist, off_vtmp, off_vsort, off_koff, off_pfac, off_cub;
+      off_sj_vals_in, off_sj_vals, off_vcount, off_voff, off_vlist, off_vtmp, off_vsort, off_koff, off_pfac, off_lfix, off_cub;
   size_t cub_bytes;
   size_t total;
 };
