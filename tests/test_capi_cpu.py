@@ -88,3 +88,28 @@ def test_cpu_tensors_are_rejected():
     om = torch.rand(2, 10) * 2 - 1
     with pytest.raises(RuntimeError, match="CUDA"):
         ob(x, om)
+
+
+def test_linear_phase_table_check():
+    """The host sets TKBN_TABLES_LINEAR_PHASE only for tables of the form
+    |h(u)| e^{icu}: the module's Kaiser-Bessel tables pass, a table with one
+    entry's phase perturbed does not, and a magnitude change keeps the form."""
+    import cmath
+
+    import torch
+
+    import torchkbnufft_gb300 as tk
+    from torchkbnufft_gb300 import _runtime as R
+
+    for im in [(320, 320), (40, 32, 48), (64,)]:
+        m = tk.KbNufft(im_size=im)
+        for d in range(len(im)):
+            assert R._linear_phase(getattr(m, f"table_{d}"))
+    t = tk.KbNufft(im_size=(320, 320)).table_0
+    bad = t.clone()
+    bad[3000] *= complex(cmath.exp(0.01j))
+    assert not R._linear_phase(bad)
+    scaled = t.clone()
+    scaled[100] *= 1.01
+    assert R._linear_phase(scaled)
+    assert not R._linear_phase(t.to(torch.complex128))  # the linear-phase kernels are complex64

@@ -342,3 +342,45 @@ def test_specialised_kernels_are_selected(case, tmp_path):
     if case != "3d8":
         names = _kernels_launched(lambda: R.interp_fwd(geom, lay, tables, grid), tmp_path)
         assert any("k_interp_fwd_pairs" in n for n in names), names
+
+
+def _bins_mismatched(om, op, K):
+    """Per dim, the points whose table bins do not step by exactly L from tap to
+    tap (the reference's fl(tm - g) rounds), in the oracle's arithmetic."""
+    rdt = np.float32
+    tm = O.normalized_freq(om, K, rdt)
+    base = O.point_indices(tm, op.numpoints, rdt)
+    out = []
+    for d in range(len(K)):
+        L, J = op.table_oversamp[d], op.numpoints[d]
+        bins = np.stack([np.rint((tm[d] - (base[d] + j).astype(rdt)) * rdt(L)) for j in range(J)]).astype(np.int64)
+        out.append(np.any(bins != bins[0] - np.arange(J)[:, None] * L, axis=0))
+    return out
+
+
+@pytest.mark.parametrize("ndim", [2, 3])
+@pytest.mark.parametrize("subset", ["centre_heavy", "left_out_only"])
+def test_linear_phase_adjoint_exact_pass(ndim, subset, tmp_path):
+    """Points within a few cells of tm = 0 (the k-space centre) can have table
+    bins that do not step by exactly L (the reference's fl(tm - g) rounds);
+    the linear-phase register adjoint leaves them to an exact atomic pass.
+    Cases: 3/4 of the points near the centre, and only the left-out points
+    (with a mismatch in every dimension among them)."""
+    from torchkbnufft_gb300 import _runtime as R
+
+    gen = torch.Generator().manual_seed(41)
+    K, C, M = ((160, 144), 16, 30000) if ndim == 2 else ((40, 32, 48), 8, 20000)
+    y = _rand(gen, (1, C, M), torch.complex64)
+    om = _traj(gen, (ndim, M)).float()
+    om[..., : 3 * M // 4] *= 0.01
+    op = O.Operator(K, K, cdtype=np.complex64)
+    if subset == "left_out_only":
+        per_dim = _bins_mismatched(om.numpy(), op, K)
+        assert all(m.any() for m in per_dim), [int(m.sum()) for m in per_dim]
+        keep = torch.tensor(np.any(per_dim, axis=0))
+        y, om = y[..., keep].contiguous(), om[:, keep].contiguous()
+    adj = tkbn().KbInterpAdjoint(im_size=K, grid_size=K, dtype=torch.complex64, device=DEV)
+    assert R.table_ptrs(adj._tables(), torch.complex64)[2] & 8  # linear-phase tables
+    names = _kernels_launched(lambda: adj(y.to(DEV), om.to(DEV)), tmp_path)
+    assert any("k_adj_lp_fix" in n for n in names), names
+    assert rel_l2(_np(adj(y.to(DEV), om.to(DEV))), op.interp_adj(y.numpy(), om.numpy())) < TOL64

@@ -301,8 +301,9 @@ def _conj_symmetric(t: torch.Tensor) -> bool:
 
 def _linear_phase(t: torch.Tensor) -> bool:
     """|t[k]| exp(i c (k - center) / L) == t[k] to within float rounding, c from the
-    entry L/2 past the centre (the device derives c the same way); L = (len - 1) / J
-    is not known here, so every even L dividing len - 1 into J = 2..8 is tried."""
+    entry L/2 past the centre (the device fits c by least squares over the entries
+    with u in (0, 1]); L = (len - 1) / J is not known here, so every even L dividing
+    len - 1 into J = 2..8 is tried."""
 
     def check() -> bool:
         if not t.is_complex() or t.dtype != torch.complex64:

@@ -1240,7 +1240,9 @@ __global__ void __launch_bounds__(kThreads) k_point_factors2(Geo<float> geo, con
       bool mis = false;
       if (on) hat = reg_point_factors_lp(geo, tm, n, i, d, rec, &mis);
       const float2 other = make_float2(__shfl_xor_sync(0xffffffffu, hat.x, 1), __shfl_xor_sync(0xffffffffu, hat.y, 1));
-      mis = mis || __shfl_xor_sync(0xffffffffu, (int)mis, 1);
+      // every lane takes part in the shuffle (not behind a short-circuit ||)
+      const int other_mis = __shfl_xor_sync(0xffffffffu, (int)mis, 1);
+      mis = mis || other_mis != 0;
       if (on && d == 0) {
         float2 P = cmul<float>(cmul<float>(ph[i], hat), other);
         if (mis) {
