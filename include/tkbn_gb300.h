@@ -92,6 +92,14 @@ extern "C" {
                                         adjoint on it scans candidates instead (slower). Must
                                         be the same in tkbn_points_build and every call that
                                         uses the layout. */
+#define TKBN_ADJ_REUSE_FACTORS 16    /* tkbn_interp_adj / tkbn_nufft_adj only: the workspace
+                                        still holds the per-point table factors that an earlier
+                                        adjoint call on it computed, with the same tables (same
+                                        contents at the same addresses) and the same other
+                                        flags, so this call does not recompute them. They
+                                        depend on the trajectory and the tables only, not on
+                                        the k-space data. No other call writes them; a new
+                                        tkbn_points_build invalidates them. */
 
 /* Operator geometry (one per KbModule). Unused dims (>= ndim) are ignored. */
 typedef struct tkbn_geometry {

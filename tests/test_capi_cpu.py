@@ -113,3 +113,21 @@ def test_linear_phase_table_check():
     scaled[100] *= 1.01
     assert R._linear_phase(scaled)
     assert not R._linear_phase(t.to(torch.complex128))  # the linear-phase kernels are complex64
+
+
+def test_adjoint_factor_reuse_key():
+    """An adjoint reuses the layout's per-point factors only for the very table
+    tensors (unmodified) and table flags they were computed with."""
+    import torch
+
+    from torchkbnufft_gb300 import _runtime as R
+
+    a, b = torch.ones(5, dtype=torch.complex64), torch.ones(5, dtype=torch.complex64)
+    stored = ((a, b), (a._version, b._version), 9)
+    assert R.factors_reusable(stored, [a, b], 9)
+    assert not R.factors_reusable(None, [a, b], 9)
+    assert not R.factors_reusable(stored, [a, b], 1)  # other table flags
+    assert not R.factors_reusable(stored, [a, a.clone()], 9)  # same contents, another tensor
+    assert not R.factors_reusable(stored, [a], 9)
+    a.mul_(2)
+    assert not R.factors_reusable(stored, [a, b], 9)  # changed in place

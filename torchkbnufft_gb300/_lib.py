@@ -43,6 +43,7 @@ TKBN_TABLES_CONJ_SYMMETRIC = 1
 TKBN_ADJ_DETERMINISTIC = 2
 TKBN_LAYOUT_FORWARD_ONLY = 4
 TKBN_TABLES_LINEAR_PHASE = 8
+TKBN_ADJ_REUSE_FACTORS = 16
 
 
 class PointsDesc(ctypes.Structure):

@@ -188,10 +188,35 @@ class PointsLayout:
         self.workspace = torch.empty(self.nbytes, dtype=torch.uint8, device=self.device)
         om = omega.detach().to(real_of(torch.complex64 if geom.dtype == L.TKBN_C64 else torch.complex128)).contiguous()
         self._omega_keepalive = om
+        # (tables, their versions, table flags) whose per-point adjoint factors
+        # the workspace holds, or None; the tables are kept alive, so identity
+        # and version pin their contents
+        self._factors = None
         L.check(
             L.lib().tkbn_points_build(ctypes.byref(g), ctypes.byref(self.desc), om.data_ptr(),
                                       self.workspace.data_ptr(), self.nbytes, stream_handle(self.device))
         )
+
+    def adjoint_call(self, tables: Sequence[torch.Tensor], table_flags: int, call) -> None:
+        """Runs ``call(flags)``, an adjoint entry point on this layout's workspace,
+        with the layout's flags and TKBN_ADJ_REUSE_FACTORS when the workspace
+        holds the factors of these same, unmodified table tensors."""
+        flags = table_flags | self.flags
+        if factors_reusable(self._factors, tables, table_flags):
+            flags |= L.TKBN_ADJ_REUSE_FACTORS
+        self._factors = None
+        call(flags)
+        self._factors = (tuple(tables), tuple(t._version for t in tables), table_flags)
+
+
+def factors_reusable(stored, tables: Sequence[torch.Tensor], table_flags: int) -> bool:
+    """True when ``stored`` (tables, versions, flags) names exactly these table
+    tensors, none modified since, with the same table flags."""
+    if stored is None:
+        return False
+    tabs, versions, flags = stored
+    return (flags == table_flags and len(tabs) == len(tables) and
+            all(a is b and b._version == v for a, b, v in zip(tabs, tables, versions)))
 
 
 _layout_cache: "collections.OrderedDict" = collections.OrderedDict()
@@ -412,9 +437,9 @@ def interp_adj(geom: GeomKey, lay: PointsLayout, tables, kdata: torch.Tensor) ->
     B, C = kdata.shape[:2]
     grid = torch.empty((B, C) + geom.grid_size, dtype=kdata.dtype, device=dev)
     tp, keep, fl = table_ptrs(tables, kdata.dtype)
-    L.check(L.lib().tkbn_interp_adj(ctypes.byref(geom_struct(geom, fl | lay.flags)), ctypes.byref(lay.desc),
-                                    lay.workspace.data_ptr(), tp, kdata.data_ptr(), B, C, grid.data_ptr(),
-                                    stream_handle(dev)))
+    lay.adjoint_call(keep, fl, lambda flags: L.check(L.lib().tkbn_interp_adj(
+        ctypes.byref(geom_struct(geom, flags)), ctypes.byref(lay.desc), lay.workspace.data_ptr(), tp,
+        kdata.data_ptr(), B, C, grid.data_ptr(), stream_handle(dev))))
     return grid
 
 
@@ -517,10 +542,10 @@ def nufft_adj(geom: GeomKey, lay: PointsLayout, tables, scaling, kdata, smaps, n
     co = 1 if smaps is not None else C
     image = torch.empty((B, co) + geom.im_size, dtype=kdata.dtype, device=dev)
     tp, keep, fl = table_ptrs(tables, kdata.dtype)
-    L.check(L.lib().tkbn_nufft_adj(ctypes.byref(geom_struct(geom, fl | lay.flags)), ctypes.byref(lay.desc),
-                                   lay.workspace.data_ptr(),
-                                   plan.handle, tp, _c(scaling), kdata.data_ptr(), _c(smaps), sb, B, C,
-                                   norm_code(norm), grid.data_ptr(), image.data_ptr(), stream_handle(dev)))
+    lay.adjoint_call(keep, fl, lambda flags: L.check(L.lib().tkbn_nufft_adj(
+        ctypes.byref(geom_struct(geom, flags)), ctypes.byref(lay.desc), lay.workspace.data_ptr(), plan.handle, tp,
+        _c(scaling), kdata.data_ptr(), _c(smaps), sb, B, C, norm_code(norm), grid.data_ptr(), image.data_ptr(),
+        stream_handle(dev))))
     return image
 
 

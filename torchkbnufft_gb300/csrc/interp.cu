@@ -2602,7 +2602,10 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
       if (ip.L.pfac && ip.a.n > 0) {
         const int64_t nb = (2 * ip.a.n + kThreads - 1) / kThreads;
         const int grid_b = (int)(nb < 152 * 16 ? nb : 152 * 16);
-        if (lp) {
+        if (ip.flags & TKBN_ADJ_REUSE_FACTORS) {
+          // the caller vouches that an earlier call on this workspace left the
+          // factors (and the left-out list) of these tables and flags in place
+        } else if (lp) {
           int rc0 = check_cuda(cudaMemsetAsync(nfix, 0, sizeof(int32_t), s), "reset left-out count");
           if (rc0) return rc0;
           k_point_factors2<true><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
