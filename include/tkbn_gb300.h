@@ -202,7 +202,11 @@ typedef struct tkbn_ragged_problem {
 typedef struct tkbn_ragged_plan_s* tkbn_ragged_plan;
 
 /* Reads the layouts' work lists (synchronises the device), allocates the
- * merged job lists. Adjoints need grids with K_d >= T_d + J_d - 1. */
+ * merged job lists. Adjoints need grids with K_d >= T_d + J_d - 1. For 2D
+ * complex64 register-adjoint layouts it also fills each problem's per-point
+ * factor scratch (the one tkbn_interp_adj fills) once, from the problem's
+ * tables; while the plan is in use, no other adjoint call may run on those
+ * workspaces. */
 int tkbn_ragged_plan_create(const tkbn_ragged_problem* problems, int64_t nproblems, tkbn_ragged_plan* plan);
 int tkbn_ragged_plan_destroy(tkbn_ragged_plan plan);
 /* kdata_p = interp(grid_p) for every problem p, one launch. */

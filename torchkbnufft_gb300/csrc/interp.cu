@@ -2879,6 +2879,18 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
                          "read adjoint sub-jobs")))
       return rc;
     const bool use_reg = reg_eligible<R, D, JC>(ip, d.o);
+    if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
+      if (use_reg && ip.L.pfac && ip.a.n > 0) {
+        // the plan's trajectories and tables are fixed: the register adjoint's
+        // per-point factors are computed once, into the problem's workspace
+        float2* pf = (float2*)const_cast<char*>(ws + ip.L.off_pfac);
+        const int64_t nb = (2 * ip.a.n + kThreads - 1) / kThreads;
+        k_point_factors2<false><<<(int)(nb < 152 * 16 ? nb : 152 * 16), kThreads>>>(
+            d.geo, d.tm, d.ph, ip.a.n, pf, nullptr, nullptr, nullptr);
+        if ((rc = check_cuda(cudaGetLastError(), "ragged factor pre-pass"))) return rc;
+        d.o.pfac = pf;
+      }
+    }
     if (!use_reg) {
       const size_t sm = own_smem<R, D, JC>(d.o);
       if (sm > 220 * 1024) return set_error(TKBN_ERR_UNSUPPORTED, "adjoint tile needs %zu bytes of shared memory", sm);
@@ -2892,6 +2904,8 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
     for (int64_t j = 0; j < hdr[1]; ++j)
       if (sj[(size_t)j].pad && sj[(size_t)j].start == 0) zero.push_back({sj[(size_t)j].len, (int)q, (int)j});
   }
+  // the factor pre-passes (legacy stream) end before the plan is returned
+  if (int rc = check_cuda(cudaStreamSynchronize(0), "ragged factor pre-pass")) return rc;
   lpt_sort(fwd);
   for (auto& v : fwdp) lpt_sort(v);
   for (auto& v : reg) lpt_sort(v);

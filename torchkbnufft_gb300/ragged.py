@@ -16,7 +16,9 @@ coil count share the work of each stage:
 Each problem is ``(im_size, omega, ncoil)`` with omega ``(d, M)`` (one
 trajectory per problem); images are ``(1, ncoil, *im_size)`` coil images (no
 coil maps), k-space data ``(1, ncoil, M)``, the reference's layouts. The
-optional autotuner picks the layout's tile shape per image size.
+optional autotuner picks the layout's tile shape per image size. The plan
+computes each 2D problem's per-point adjoint factors once, into that problem's
+layout workspace; the layouts are private to the plan.
 """
 
 from __future__ import annotations
