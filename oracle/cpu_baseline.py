@@ -1,4 +1,4 @@
-"""CPU port of the reference table path used as the timed CPU baseline — BASELINE INFRASTRUCTURE.
+"""CPU port of the reference table path used as the timed CPU baseline — TEST / CPU-BASELINE INFRASTRUCTURE.
 
 Forward: ``image * smaps * scaling`` -> zero-pad -> FFT -> table interpolation;
 adjoint: table interpolation adjoint -> unnormalised IFFT -> crop ->

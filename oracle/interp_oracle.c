@@ -1,5 +1,5 @@
 /*
- * C restatement of the reference table interpolation — TEST / BASELINE
+ * C restatement of the reference table interpolation — TEST / CPU-BASELINE
  * INFRASTRUCTURE ONLY (used by tests and by the CPU-baseline leg of bench.py,
  * never by the product library).
  *
