@@ -47,6 +47,19 @@ def test_python_binding_covers_header():
     assert set(_declared()) == set(_lib.SIGNATURES)
 
 
+def test_python_constants_match_header():
+    """Every integer #define of the header has a Python constant of the same value."""
+    from torchkbnufft_gb300 import _lib
+
+    src = open(os.path.join(ROOT, "include", "tkbn_gb300.h")).read()
+    defs = dict(re.findall(r"^#define\s+(TKBN_\w+)\s+\(?(-?\d+)\)?", src, re.M))
+    assert "TKBN_ADJ_REUSE_FACTORS" in defs and "TKBN_TABLES_LINEAR_PHASE" in defs
+    for name, value in defs.items():
+        if name == "TKBN_GB300_H":
+            continue
+        assert getattr(_lib, name, None) == int(value), name
+
+
 def test_abi_version(lib):
     assert lib.tkbn_abi_version() == 1
 

@@ -13,6 +13,7 @@ import threading
 
 from . import _build
 
+TKBN_ABI_VERSION = 1
 TKBN_OK = 0
 TKBN_ERR_INVALID = -1
 TKBN_ERR_UNSUPPORTED = -2
@@ -122,7 +123,7 @@ def load(path: str | None = None, build_if_missing: bool = True) -> ctypes.CDLL:
             fn = getattr(cdll, name)
             fn.argtypes = argtypes
             fn.restype = ctypes.c_char_p if name == "tkbn_last_error" else ctypes.c_int
-        if cdll.tkbn_abi_version() != 1:
+        if cdll.tkbn_abi_version() != TKBN_ABI_VERSION:
             raise RuntimeError("tkbn ABI version mismatch")
         _lib = cdll
         return _lib
