@@ -13,8 +13,13 @@ import pytest
 from conftest import ROOT
 
 
+def _header():
+    with open(os.path.join(ROOT, "include", "tkbn_gb300.h")) as f:
+        return f.read()
+
+
 def _declared():
-    src = open(os.path.join(ROOT, "include", "tkbn_gb300.h")).read()
+    src = _header()
     return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(tkbn_\w+)\s*\(", src, re.M)))
 
 
@@ -51,7 +56,7 @@ def test_python_constants_match_header():
     """Every integer #define of the header has a Python constant of the same value."""
     from torchkbnufft_gb300 import _lib
 
-    src = open(os.path.join(ROOT, "include", "tkbn_gb300.h")).read()
+    src = _header()
     defs = dict(re.findall(r"^#define\s+(TKBN_\w+)\s+\(?(-?\d+)\)?", src, re.M))
     assert "TKBN_ADJ_REUSE_FACTORS" in defs and "TKBN_TABLES_LINEAR_PHASE" in defs
     for name, value in defs.items():

@@ -200,13 +200,16 @@ class PointsLayout:
     def adjoint_call(self, tables: Sequence[torch.Tensor], table_flags: int, call) -> None:
         """Runs ``call(flags)``, an adjoint entry point on this layout's workspace,
         with the layout's flags and TKBN_ADJ_REUSE_FACTORS when the workspace
-        holds the factors of these same, unmodified table tensors."""
-        flags = table_flags | self.flags
-        if factors_reusable(self._factors, tables, table_flags):
-            flags |= L.TKBN_ADJ_REUSE_FACTORS
-        self._factors = None
-        call(flags)
-        self._factors = (tuple(tables), tuple(t._version for t in tables), table_flags)
+        holds the factors of these same, unmodified table tensors. The record
+        and the enqueue happen under one lock, so threads sharing a cached
+        layout keep the record in the order their calls reach the stream."""
+        with _lock:
+            flags = table_flags | self.flags
+            if factors_reusable(self._factors, tables, table_flags):
+                flags |= L.TKBN_ADJ_REUSE_FACTORS
+            self._factors = None
+            call(flags)
+            self._factors = (tuple(tables), tuple(t._version for t in tables), table_flags)
 
 
 def factors_reusable(stored, tables: Sequence[torch.Tensor], table_flags: int) -> bool:
