@@ -69,10 +69,9 @@ def calc_tensor_spmatrix(omega: Tensor, im_size: Sequence[int], grid_size: Optio
     idx = torch.tensor(np.stack((rows, col.reshape(-1).astype(np.int64))), dtype=torch.long, device=device)
     shape = torch.Size((M, int(np.prod(grid_size))))
     # the indices are in range by construction (column wrap mod K, rows 0..M-1)
-    real = torch.sparse_coo_tensor(idx, torch.tensor(coef.real.reshape(-1), dtype=dtype, device=device), shape,
-                                   check_invariants=False)
-    imag = torch.sparse_coo_tensor(idx, torch.tensor(coef.imag.reshape(-1), dtype=dtype, device=device), shape,
-                                   check_invariants=False)
+    with torch.sparse.check_sparse_tensor_invariants(enable=False):
+        real = torch.sparse_coo_tensor(idx, torch.tensor(coef.real.reshape(-1), dtype=dtype, device=device), shape)
+        imag = torch.sparse_coo_tensor(idx, torch.tensor(coef.imag.reshape(-1), dtype=dtype, device=device), shape)
     return real, imag
 
 
@@ -82,10 +81,11 @@ class _CSR:
     def __init__(self, real: Tensor, imag: Tensor, cdtype: torch.dtype, device: torch.device):
         rdt = R.real_of(cdtype)
         # the indices are those of two valid sparse tensors of this shape
-        both = torch.sparse_coo_tensor(
-            torch.cat((real._indices(), imag._indices()), dim=1),
-            torch.cat((real._values().to(rdt).to(cdtype), 1j * imag._values().to(rdt).to(cdtype))),
-            real.shape, check_invariants=False).coalesce()
+        with torch.sparse.check_sparse_tensor_invariants(enable=False):
+            both = torch.sparse_coo_tensor(
+                torch.cat((real._indices(), imag._indices()), dim=1),
+                torch.cat((real._values().to(rdt).to(cdtype), 1j * imag._values().to(rdt).to(cdtype))),
+                real.shape).coalesce()
         idx = both.indices().to(device)
         self.nrows, self.ncols = int(real.shape[0]), int(real.shape[1])
         self.nnz = int(idx.shape[1])
