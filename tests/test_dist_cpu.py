@@ -1,0 +1,64 @@
+"""The bench's multi-process path on CPU: two gloo ranks on 127.0.0.1.
+
+``bench.py`` under torchrun runs one replica per rank: ``dist_setup`` reads
+the rank from the environment, ``barrier`` brackets the timed region,
+``max_over_ranks`` reduces each timing to the slowest rank, and the reference
+arm runs on rank 0 only (the other ranks return without work).
+"""
+
+import argparse
+import contextlib
+import io
+import json
+import os
+import socket
+import sys
+import time
+
+import torch.multiprocessing as mp
+
+from conftest import ROOT
+
+
+def _free_port() -> int:
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank: int, world: int, port: int, out_dir: str) -> None:
+    os.environ.update({"WORLD_SIZE": str(world), "RANK": str(rank), "LOCAL_RANK": str(rank),
+                       "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    sys.path.insert(0, ROOT)
+    import torch
+    import torch.distributed as dist
+
+    import bench
+
+    got = {}
+    got["setup"] = list(bench.dist_setup())
+    bench.barrier(world)
+    got["max"] = bench.max_over_ranks(float(10 * (rank + 1)), world, torch.device("cpu"))
+    if rank == 1:
+        args = argparse.Namespace(gpus=world, steps=3, warmup=3, ref_coils=4)
+        buf = io.StringIO()
+        t0 = time.perf_counter()
+        with contextlib.redirect_stdout(buf):
+            bench.run_reference(args)
+        got["ref_seconds"] = time.perf_counter() - t0
+        got["ref_output"] = buf.getvalue()
+    bench.barrier(world)
+    dist.destroy_process_group()
+    with open(os.path.join(out_dir, f"rank{rank}.json"), "w") as f:
+        json.dump(got, f)
+
+
+def test_two_gloo_ranks(tmp_path):
+    world = 2
+    mp.spawn(_rank, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
+    res = [json.loads((tmp_path / f"rank{r}.json").read_text()) for r in range(world)]
+    for r, got in enumerate(res):
+        assert got["setup"] == [world, r, r]
+        assert got["max"] == 10.0 * world  # the slowest rank's time on every rank
+    assert res[1]["ref_output"] == ""  # the reference arm prints on rank 0 only
+    assert res[1]["ref_seconds"] < 5.0  # and does no work elsewhere
