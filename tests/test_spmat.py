@@ -24,6 +24,27 @@ def test_calc_tensor_spmatrix_matches_reference(name):
     assert np.abs(imag.to_dense().numpy() - g["mat_imag"]).max() < 2e-6
 
 
+@pytest.mark.parametrize("name", ["spmat_2d", "spmat_3d"])
+def test_build_numpy_spmatrix_matches_reference(name):
+    """``nufft_utils.build_numpy_spmatrix`` (the reference's complex scipy COO
+    builder, same signature) holds the fixture's matrix as real + i imag."""
+    import scipy.sparse
+
+    import torchkbnufft_gb300 as tkbn
+
+    g = load_golden("live_" + name)
+    im_size = g["image"].shape[2:]
+    om = torch.tensor(g["omega"])
+    im, gs, J, ns, _, order, alpha, _, _ = tkbn.nufft_utils.validate_args(im_size, None, 6, None, 2**10, 2.34, 0.0,
+                                                                          om.dtype, om.device)
+    coo = tkbn.nufft_utils.build_numpy_spmatrix(om.numpy(), numpoints=J, im_size=im, grid_size=gs, n_shift=ns,
+                                                order=order, alpha=alpha)
+    assert scipy.sparse.issparse(coo) and coo.format == "coo" and coo.shape == g["mat_real"].shape
+    dense = coo.toarray()
+    assert np.abs(dense.real - g["mat_real"]).max() < 2e-6
+    assert np.abs(dense.imag - g["mat_imag"]).max() < 2e-6
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["spmat_2d", "spmat_3d"])
 def test_spmat_nufft_matches_reference(name):

@@ -255,3 +255,48 @@ def init_fn(
         torch.tensor(order, dtype=real_dtype, device=device),
         torch.tensor(alpha, dtype=real_dtype, device=device),
     )
+
+
+def _exact_coefs(om: np.ndarray, npts: int, K: int, alpha: float, order: float):
+    """Exact KB weights of each point's ``npts`` neighbours along one dim, and
+    their kernel arguments (distance to each neighbour, in cells)."""
+    gam = 2 * np.pi / K
+    dist = om / gam - np.floor(om / gam - npts / 2)
+    arg = dist[:, None] - np.arange(1, npts + 1)[None, :]
+    coef = np.zeros(arg.shape, dtype=np.float64)
+    inside = np.abs(arg) < npts / 2
+    coef[inside] = special.iv(order, alpha * np.sqrt(1 - (arg[inside] / (npts / 2)) ** 2)) / special.iv(order, alpha)
+    return coef, arg
+
+
+def build_numpy_spmatrix(omega: np.ndarray, numpoints: Sequence[int], im_size: Sequence[int],
+                         grid_size: Sequence[int], n_shift: Sequence[int], order: Sequence[float],
+                         alpha: Sequence[float]):
+    """Complex interpolation matrix ``(M, prod(grid_size))`` as a scipy COO matrix
+    (``torchkbnufft/_nufft/utils.py:16-119``, same signature and entries).
+
+    Entry (m, cell) is the conjugated product over dims of the exact KB weight
+    times the kernel's linear phase ``exp(i gamma (N - 1)/2 u)``, times the
+    fftshift phase ``exp(i omega_m . n_shift)``; neighbour columns wrap mod K.
+    Entries are listed point by point (J^d per point), duplicates not summed.
+    """
+    from scipy.sparse import coo_matrix
+
+    om = np.asarray(omega, dtype=np.float64)
+    nd, M = om.shape
+    coefs, cols = [], []
+    for d in range(nd):
+        K, N, J = int(grid_size[d]), int(im_size[d]), int(numpoints[d])
+        c, arg = _exact_coefs(om[d], J, K, float(alpha[d]), float(order[d]))
+        gam = 2 * np.pi / K
+        coefs.append(c * np.exp(1j * gam * (N - 1) / 2 * arg))
+        first = np.floor(om[d] / gam - J / 2)
+        cols.append(np.mod(np.arange(1, J + 1)[None, :] + first[:, None], K) * int(np.prod(grid_size[d + 1:])))
+    coef, col = coefs[0], cols[0]
+    for d in range(1, nd):
+        coef = (coef[:, :, None] * coefs[d][:, None, :]).reshape(M, -1)
+        col = (col[:, :, None] + cols[d][:, None, :]).reshape(M, -1)
+    coef = np.conj(coef) * np.exp(1j * (om.T @ np.asarray(n_shift, dtype=np.float64)))[:, None]
+    rows = np.repeat(np.arange(M), coef.shape[1])
+    return coo_matrix((coef.reshape(-1), (rows, col.reshape(-1).astype(np.int64))),
+                      shape=(M, int(np.prod(grid_size))))

@@ -22,23 +22,12 @@ from typing import Optional, Sequence, Tuple, Union
 
 import numpy as np
 import torch
-from scipy import special
 from torch import Tensor
 
 from . import _lib as L
 from . import _runtime as R
+from . import _setup as S
 from ._setup import validate_args
-
-
-def _exact_coefs(om, npts, K, alpha, order):
-    """Per-dim KB weights and kernel arguments of each point's J neighbours."""
-    gam = 2 * np.pi / K
-    dist = om / gam - np.floor(om / gam - npts / 2)
-    arg = dist[:, None] - np.arange(1, npts + 1)[None, :]
-    coef = np.zeros(arg.shape, dtype=np.float64)
-    inside = np.abs(arg) < npts / 2
-    coef[inside] = special.iv(order, alpha * np.sqrt(1 - (arg[inside] / (npts / 2)) ** 2)) / special.iv(order, alpha)
-    return coef, arg
 
 
 def calc_tensor_spmatrix(omega: Tensor, im_size: Sequence[int], grid_size: Optional[Sequence[int]] = None,
@@ -50,28 +39,13 @@ def calc_tensor_spmatrix(omega: Tensor, im_size: Sequence[int], grid_size: Optio
         raise ValueError("Sparse matrix calculation not implemented for batched omega.")
     im_size, grid_size, numpoints, n_shift, table_oversamp, order, alpha, dtype, device = validate_args(
         im_size, grid_size, numpoints, n_shift, table_oversamp, kbwidth, order, omega.dtype, omega.device)
-    om = omega.detach().cpu().numpy().astype(np.float64)
-    nd, M = om.shape
-    coefs, cols = [], []
-    for d in range(nd):
-        K, N, J = int(grid_size[d]), int(im_size[d]), int(numpoints[d])
-        c, arg = _exact_coefs(om[d], J, K, float(alpha[d]), float(order[d]))
-        gam = 2 * np.pi / K
-        coefs.append(c * np.exp(1j * gam * (N - 1) / 2 * arg))
-        first = np.floor(om[d] / gam - J / 2)
-        cols.append(np.mod(np.arange(1, J + 1)[None, :] + first[:, None], K) * int(np.prod(grid_size[d + 1:])))
-    coef, col = coefs[0], cols[0]
-    for d in range(1, nd):
-        coef = (coef[:, :, None] * coefs[d][:, None, :]).reshape(M, -1)
-        col = (col[:, :, None] + cols[d][:, None, :]).reshape(M, -1)
-    coef = np.conj(coef) * np.exp(1j * (om.T @ np.asarray(n_shift, dtype=np.float64)))[:, None]
-    rows = np.repeat(np.arange(M), coef.shape[1])
-    idx = torch.tensor(np.stack((rows, col.reshape(-1).astype(np.int64))), dtype=torch.long, device=device)
-    shape = torch.Size((M, int(np.prod(grid_size))))
+    coo = S.build_numpy_spmatrix(omega.detach().cpu().numpy(), numpoints, im_size, grid_size, n_shift, order, alpha)
+    idx = torch.tensor(np.stack((coo.row, coo.col)).astype(np.int64), dtype=torch.long, device=device)
+    shape = torch.Size(coo.shape)
     # the indices are in range by construction (column wrap mod K, rows 0..M-1)
     with torch.sparse.check_sparse_tensor_invariants(enable=False):
-        real = torch.sparse_coo_tensor(idx, torch.tensor(coef.real.reshape(-1), dtype=dtype, device=device), shape)
-        imag = torch.sparse_coo_tensor(idx, torch.tensor(coef.imag.reshape(-1), dtype=dtype, device=device), shape)
+        real = torch.sparse_coo_tensor(idx, torch.tensor(np.real(coo.data), dtype=dtype, device=device), shape)
+        imag = torch.sparse_coo_tensor(idx, torch.tensor(np.imag(coo.data), dtype=dtype, device=device), shape)
     return real, imag
 
 
