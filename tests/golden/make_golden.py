@@ -12,6 +12,8 @@ Two kinds of fixtures are written:
 * ``live_*.npz`` — outputs of the reference's public API run here on seeded
   inputs, complex64 unless the name says c128. These pin the oracle and the
   CUDA path to the reference's table mode at the working precision.
+  ``live_setup_*`` hold every buffer of a complex128 KbNufft and the complex
+  buffers of a complex64 one (tables, scaling coefficients, parsed arguments).
 
 The tests only read the ``.npz`` files; nothing at test time needs the reference.
 ``TKBN_GOLDEN_ONLY=<prefix>`` rewrites only the live fixtures with that prefix.
@@ -149,6 +151,24 @@ def live_cases():
                            image=_np(image), kdata_in=_np(kin),
                            kdata=_np(fwd(image, om, interp_mats=(real, imag))),
                            image_adj=_np(adj(kin, om, interp_mats=(real, imag))))
+
+    # host setup: every buffer of a complex128 KbNufft (tables, scaling
+    # coefficients, parsed arguments), small table oversampling except the
+    # default-argument 1D case
+    for name, kw in (
+        ("setup_1d_default", dict(im_size=(64,))),
+        ("setup_2d", dict(im_size=(20, 24), table_oversamp=256)),
+        ("setup_2d_custom", dict(im_size=(17, 12), grid_size=(30, 26), numpoints=(4, 5), table_oversamp=(128, 64),
+                                 kbwidth=2.1, order=(0.0, 0.5))),
+        ("setup_3d", dict(im_size=(6, 8, 5), numpoints=(2, 4, 6), table_oversamp=64)),
+    ):
+        mod = tkbn.KbNufft(dtype=torch.complex128, **kw)
+        arrs = {k: _np(v) for k, v in mod.state_dict().items()}
+        # the working-precision module's floating buffers (built in complex64, not cast)
+        mod64 = tkbn.KbNufft(dtype=torch.complex64, **kw)
+        arrs.update({"c64_" + k: _np(v) for k, v in mod64.state_dict().items() if v.is_complex()})
+        arrs["kwargs"] = np.array(repr(kw))
+        cases[name] = arrs
 
     only = os.environ.get("TKBN_GOLDEN_ONLY")
     for name, arrs in cases.items():
