@@ -32,7 +32,7 @@ sensitive to it (table-bin selection and the fftshift phase):
 from __future__ import annotations
 
 import itertools
-from typing import List, Optional, Sequence
+from typing import List, Sequence
 
 import numpy as np
 
