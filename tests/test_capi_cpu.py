@@ -149,3 +149,24 @@ def test_adjoint_factor_reuse_key():
     assert not R.factors_reusable(stored, [a], 9)
     a.mul_(2)
     assert not R.factors_reusable(stored, [a, b], 9)  # changed in place
+
+
+def test_missing_library_raises_instead_of_falling_back():
+    """Without the CUDA library the package raises; there is no CPU path to fall back to."""
+    import sys
+
+    code = (
+        "import torchkbnufft_gb300._build as B, torchkbnufft_gb300._lib as L\n"
+        "B.lib_path = lambda: '/nonexistent/libtkbn_gb300.so'\n"
+        "try:\n"
+        "    L.load(build_if_missing=False)\n"
+        "except RuntimeError as e:\n"
+        "    print('raised:', e)\n"
+        "try:\n"
+        "    L.load(path='/nonexistent/libtkbn_gb300.so')\n"
+        "except OSError:\n"
+        "    print('raised: OSError')\n"
+    )
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert "raised: CUDA library not built" in out.stdout and "raised: OSError" in out.stdout, out.stdout
