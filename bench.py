@@ -20,9 +20,11 @@ flush is inserted between steps.
           CUDA-event duration, against the measured HBM copy bandwidth.
   cpu_baseline: the CPU port of the reference table path on a bounded sample.
 
-``--impl reference`` times the CPU port of the reference path (the reference
-is pure Python and cannot run here) on the host cores on the same workload
-definition and prints the same line with ``"impl": "reference"``.
+``--impl reference`` times the CPU port of the reference path on the host
+cores on the same workload definition and prints the same line with
+``"impl": "reference"``. ``--impl reference-gpu`` times the unmodified
+reference (installed in baseline/_ref) through its own modules on the GPU, a
+second comparator.
 """
 
 from __future__ import annotations
@@ -697,12 +699,77 @@ def run_config(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- second comparator: the reference on the GPU
+
+
+def run_reference_gpu(args):
+    """The unmodified reference, installed in baseline/_ref, through its own
+    public API (KbNufft forward and KbNufftAdjoint with the maps) on the same
+    device and workload as the GPU arm. Inputs are resident on the device. On a
+    GPU it is timed with CUDA events on the current stream. Runs on rank 0 only.
+    ``--device`` overrides the device (cpu for a check without a GPU)."""
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    ref_dir = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isfile(os.path.join(ref_dir, "torchkbnufft", "__init__.py")):
+        print(json.dumps({"impl": "reference-gpu", "unavailable": "the reference is not installed in baseline/_ref"}))
+        return
+    import warnings
+
+    import torch
+
+    sys.path.insert(0, ref_dir)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        import torchkbnufft as ref
+    dev = torch.device(args.device or "cuda")
+    image_np, smaps_np, omega_np = make_inputs()
+    x, s, om = (torch.tensor(a, device=dev) for a in (image_np, smaps_np, omega_np))
+    fwd = ref.KbNufft(im_size=(N, N), device=dev)
+    adj = ref.KbNufftAdjoint(im_size=(N, N), device=dev)
+
+    def step():
+        with torch.no_grad():
+            return adj(fwd(x, om, smaps=s), om, smaps=s)
+
+    for _ in range(args.warmup):
+        step()
+    if dev.type == "cuda":
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / args.steps
+    else:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    work = B * C * omega_np.shape[1]
+    print(json.dumps({
+        "impl": "reference-gpu", "metric": METRIC, "value": work / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {"workload": "2D SENSE NUFFT fwd+adj, image 320x320, grid 640x640, J=6, L=1024, 16 coils, "
+                               "batch 4, golden-angle 404x640 (258560 points)",
+                   "device": str(dev), "path": "the reference's own table path, unmodified (baseline/_ref)",
+                   "work_per_step": work},
+    }))
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=5)
-    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference", "reference-gpu"],
+                   help="reference: the reference path on the host cores; reference-gpu: the reference's "
+                        "own PyTorch path on the GPU (a second comparator)")
+    p.add_argument("--device", default=None, help="device of the reference-gpu arm (default cuda)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--ref-coils", type=int, default=4)
     p.add_argument("--workload", default="sense", choices=["sense", "ragged", "single", "kooshball", "spiral-grad", "sense-c128"],
@@ -712,6 +779,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.impl == "reference-gpu":
+        run_reference_gpu(args)
     elif args.workload == "ragged":
         run_ragged(args)
     elif args.workload != "sense":
