@@ -83,15 +83,16 @@ def live_cases():
     interp_case("interp_3d", (1, 2, 12, 14, 10), 300, seed=4)
     interp_case("interp_2d_c128", (1, 2, 24, 28), 300, cdtype=torch.complex128, seed=5)
 
-    def nufft_case(name, B, C, im_size, M, norm, cdtype=torch.complex64, grid_size=None, seed=0, batched=False):
+    def nufft_case(name, B, C, im_size, M, norm, cdtype=torch.complex64, grid_size=None, seed=0, batched=False,
+                   numpoints=6):
         rdtype = torch.float32 if cdtype == torch.complex64 else torch.float64
         gen = torch.Generator().manual_seed(seed)
         image = _cplx(gen, (B, 1) + im_size, cdtype)
         smaps = _cplx(gen, (B, C) + im_size, cdtype)
         om = _traj(gen, (B, len(im_size), M) if batched else (len(im_size), M), rdtype)
         kin = _cplx(gen, (B, C, M), cdtype)
-        fwd = tkbn.KbNufft(im_size=im_size, grid_size=grid_size, dtype=cdtype)
-        adj = tkbn.KbNufftAdjoint(im_size=im_size, grid_size=grid_size, dtype=cdtype)
+        fwd = tkbn.KbNufft(im_size=im_size, grid_size=grid_size, numpoints=numpoints, dtype=cdtype)
+        adj = tkbn.KbNufftAdjoint(im_size=im_size, grid_size=grid_size, numpoints=numpoints, dtype=cdtype)
         img_c = _cplx(gen, (B, C) + im_size, cdtype)
         cases[name] = dict(
             image=_np(image), smaps=_np(smaps), omega=_np(om), kdata_in=_np(kin), image_coils=_np(img_c),
@@ -101,6 +102,7 @@ def live_cases():
             image_plain=_np(adj(kin, om, norm=norm)),
             norm=np.array("ortho" if norm == "ortho" else ""),
             grid_size=np.array(grid_size if grid_size is not None else [2 * n for n in im_size]),
+            numpoints=np.array(numpoints if isinstance(numpoints, tuple) else (numpoints,) * len(im_size)),
         )
 
     nufft_case("nufft_2d", 2, 4, (24, 20), 600, None, seed=10)
@@ -110,6 +112,10 @@ def live_cases():
     nufft_case("nufft_3d", 1, 3, (10, 12, 8), 400, None, seed=14)
     nufft_case("nufft_2d_grid", 1, 2, (20, 22), 300, None, grid_size=(30, 40), seed=15)
     nufft_case("nufft_2d_c128", 1, 2, (20, 22), 300, "ortho", cdtype=torch.complex128, seed=16)
+    # the reference test suite's own shapes (tests/conftest.py test_params): batch 5, 4 coils,
+    # 112 points, odd image sizes and per-dim numpoints
+    nufft_case("nufft_refparams_2d", 5, 4, (33, 24), 112, None, seed=17, numpoints=(4, 6))
+    nufft_case("nufft_refparams_3d", 5, 4, (11, 33, 24), 112, "ortho", seed=18, numpoints=(2, 4, 6))
 
     # Toeplitz kernel + normal operator
     for name, im_size, M, norm, batched, seed in (

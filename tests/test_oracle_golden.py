@@ -51,12 +51,13 @@ def test_live_interp(name):
 
 
 @pytest.mark.parametrize("name", ["nufft_1d", "nufft_2d", "nufft_2d_ortho", "nufft_2d_batched", "nufft_3d",
-                                  "nufft_2d_grid", "nufft_2d_c128"])
+                                  "nufft_2d_grid", "nufft_2d_c128", "nufft_refparams_2d", "nufft_refparams_3d"])
 def test_live_nufft(name):
     g = load_golden("live_" + name)
     cd = g["image"].dtype
     norm = str(g["norm"]) or None
-    op = O.Operator(g["image"].shape[2:], grid_size=tuple(int(x) for x in g["grid_size"]), cdtype=cd)
+    J = tuple(int(x) for x in g["numpoints"]) if "numpoints" in g else 6
+    op = O.Operator(g["image"].shape[2:], grid_size=tuple(int(x) for x in g["grid_size"]), numpoints=J, cdtype=cd)
     tol = 2e-6 if cd == np.complex64 else 1e-12
     assert rel_l2(op.forward(g["image"], g["omega"], smaps=g["smaps"], norm=norm), g["kdata_sense"]) < tol
     assert rel_l2(op.adjoint(g["kdata_in"], g["omega"], smaps=g["smaps"], norm=norm), g["image_sense"]) < tol
