@@ -99,7 +99,10 @@ extern "C" {
                                         flags, so this call does not recompute them. They
                                         depend on the trajectory and the tables only, not on
                                         the k-space data. No other call writes them; a new
-                                        tkbn_points_build invalidates them. */
+                                        tkbn_points_build invalidates them. A call captured
+                                        into a CUDA graph that sets it makes the graph depend
+                                        on the factors staying in place; leave it unset there
+                                        and the graph recomputes them on every replay. */
 
 /* Operator geometry (one per KbModule). Unused dims (>= ndim) are ignored. */
 typedef struct tkbn_geometry {

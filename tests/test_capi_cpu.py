@@ -170,3 +170,29 @@ def test_missing_library_raises_instead_of_falling_back():
     out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, timeout=120)
     assert out.returncode == 0, out.stderr
     assert "raised: CUDA library not built" in out.stdout and "raised: OSError" in out.stdout, out.stdout
+
+
+def test_adjoint_factor_reuse_is_off_under_graph_capture(monkeypatch):
+    """A call captured into a CUDA graph always carries the pre-pass and leaves
+    no record (nothing ran at capture time); eager calls reuse as before."""
+    import torch
+
+    from torchkbnufft_gb300 import _lib as L
+    from torchkbnufft_gb300 import _runtime as R
+
+    lay = object.__new__(R.PointsLayout)  # the host logic only: no workspace
+    lay.flags, lay.device, lay._factors = 0, torch.device("cuda", 0), None
+    tabs = [torch.ones(5, dtype=torch.complex64)]
+    seen = []
+    capturing = [False]
+    monkeypatch.setattr(R, "stream_capturing", lambda device: capturing[0])
+    lay.adjoint_call(tabs, 9, seen.append)  # eager: computes, records
+    lay.adjoint_call(tabs, 9, seen.append)  # eager: reuses
+    capturing[0] = True
+    lay.adjoint_call(tabs, 9, seen.append)  # captured: recomputes, no record
+    capturing[0] = False
+    lay.adjoint_call(tabs, 9, seen.append)  # eager after capture: recomputes
+    lay.adjoint_call(tabs, 9, seen.append)  # and reuses again
+    reuse = [bool(f & L.TKBN_ADJ_REUSE_FACTORS) for f in seen]
+    assert reuse == [False, True, False, False, True]
+    assert all(f & ~L.TKBN_ADJ_REUSE_FACTORS == 9 for f in seen)

@@ -202,14 +202,28 @@ class PointsLayout:
         with the layout's flags and TKBN_ADJ_REUSE_FACTORS when the workspace
         holds the factors of these same, unmodified table tensors. The record
         and the enqueue happen under one lock, so threads sharing a cached
-        layout keep the record in the order their calls reach the stream."""
+        layout keep the record in the order their calls reach the stream.
+
+        Under CUDA graph capture nothing runs when it is enqueued, so a captured
+        call always recomputes the factors (the graph carries its own pre-pass)
+        and leaves no record behind for the calls after it."""
         with _lock:
+            capturing = stream_capturing(self.device)
             flags = table_flags | self.flags
-            if factors_reusable(self._factors, tables, table_flags):
+            if not capturing and factors_reusable(self._factors, tables, table_flags):
                 flags |= L.TKBN_ADJ_REUSE_FACTORS
             self._factors = None
             call(flags)
-            self._factors = (tuple(tables), tuple(t._version for t in tables), table_flags)
+            if not capturing:
+                self._factors = (tuple(tables), tuple(t._version for t in tables), table_flags)
+
+
+def stream_capturing(device: torch.device) -> bool:
+    """Whether torch's current stream on ``device`` is capturing a CUDA graph."""
+    if device.index is None or device.index == torch.cuda.current_device():
+        return torch.cuda.is_current_stream_capturing()
+    with torch.cuda.device(device):
+        return torch.cuda.is_current_stream_capturing()
 
 
 def factors_reusable(stored, tables: Sequence[torch.Tensor], table_flags: int) -> bool:
