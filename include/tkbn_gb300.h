@@ -8,8 +8,9 @@
  *
  * Ownership: the caller owns every buffer passed in (inputs, outputs and
  * workspaces). The library allocates nothing except inside
- * tkbn_fft_plan_create (the cuFFT plan and its work area), which
- * tkbn_fft_plan_destroy releases.
+ * tkbn_fft_plan_create (the cuFFT plan or the fused passes' twiddle tables)
+ * and tkbn_ragged_plan_create (the merged job lists), which
+ * tkbn_fft_plan_destroy and tkbn_ragged_plan_destroy release.
  *
  * Streams: all work is enqueued on the given stream; no entry point
  * synchronises the host, so sequences of calls can be captured in a CUDA
