@@ -219,11 +219,15 @@ class PointsLayout:
 
 
 def stream_capturing(device: torch.device) -> bool:
-    """Whether torch's current stream on ``device`` is capturing a CUDA graph."""
-    if device.index is None or device.index == torch.cuda.current_device():
-        return torch.cuda.is_current_stream_capturing()
-    with torch.cuda.device(device):
-        return torch.cuda.is_current_stream_capturing()
+    """Whether torch's current stream on ``device`` is capturing a CUDA graph.
+    A query that fails reads as not capturing (the eager behaviour)."""
+    try:
+        if device.index is None or device.index == torch.cuda.current_device():
+            return bool(torch.cuda.is_current_stream_capturing())
+        with torch.cuda.device(device):
+            return bool(torch.cuda.is_current_stream_capturing())
+    except (AttributeError, RuntimeError):
+        return False
 
 
 def factors_reusable(stored, tables: Sequence[torch.Tensor], table_flags: int) -> bool:
