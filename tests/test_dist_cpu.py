@@ -62,3 +62,24 @@ def test_two_gloo_ranks(tmp_path):
         assert got["max"] == 10.0 * world  # the slowest rank's time on every rank
     assert res[1]["ref_output"] == ""  # the reference arm prints on rank 0 only
     assert res[1]["ref_seconds"] < 5.0  # and does no work elsewhere
+
+
+def test_reference_arm_line():
+    """``bench.py --impl reference`` (the CPU port on the host cores) prints one
+    JSON line with the headline metric, a cpu_baseline describing the run and
+    an e2e block with the line's own value and no copies."""
+    import subprocess
+
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "3"],
+                         capture_output=True, text=True, cwd=ROOT, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["higher_is_better"] is True and line["value"] > 0 and line["config"]["workload"]
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"] and cb["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
