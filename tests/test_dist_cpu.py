@@ -1,9 +1,13 @@
-"""The bench's multi-process path on CPU: two gloo ranks on 127.0.0.1.
+"""The bench's host-side contract on CPU.
 
-``bench.py`` under torchrun runs one replica per rank: ``dist_setup`` reads
-the rank from the environment, ``barrier`` brackets the timed region,
-``max_over_ranks`` reduces each timing to the slowest rank, and the reference
-arm runs on rank 0 only (the other ranks return without work).
+Multi-process path, with two gloo ranks on 127.0.0.1. ``bench.py`` under
+torchrun runs one replica per rank. ``dist_setup`` reads the rank from the
+environment, ``barrier`` brackets the timed region, and ``max_over_ranks``
+reduces each timing to the slowest rank. The reference arm runs on rank 0
+only; the other ranks return without work.
+
+Also checked: the JSON line of the reference arm (the CPU port), which needs
+no GPU.
 """
 
 import argparse
