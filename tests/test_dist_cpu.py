@@ -87,3 +87,17 @@ def test_reference_arm_line():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"] and cb["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+
+
+def test_algorithmic_bytes_of_the_headline_workload():
+    """The roofline's byte counts at the headline workload: forward and adjoint
+    NUFFT as the per-unit formulas give them (8 B per complex64, 4 B per
+    coordinate), and the interpolation kernels' own inputs and outputs."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    M = 404 * 640
+    b = bench.algorithmic_bytes(M)
+    assert b["forward"] == 1_029_017_600 and b["adjoint"] == 871_731_200
+    # gather: grid read + kdata write + sorted coordinates, phase and index
+    assert b["gather"] == 8 * 4 * 16 * 640 * 640 + 8 * 4 * 16 * M + 12 * M == 345_200_640
