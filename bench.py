@@ -216,28 +216,40 @@ def max_over_ranks(x: float, world: int, device) -> float:
 # ---------------------------------------------------------------- CPU baseline (port of the reference path)
 
 
-def cpu_sample_run(image, smaps, omega, coils: int, batch: int = 1):
-    """One forward+adjoint of the reference table path (CPU port) on a sample:
-    `batch` images, the first `coils` coils, the full trajectory."""
+def rel_l2(a, b) -> float:
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+def cpu_full_step(image, smaps, omega):
+    """One forward+adjoint of the reference table path (CPU port) on the full
+    workload: all B images, all C coils, the full trajectory. Returns
+    (k-space data, adjoint image)."""
     from oracle import cpu_baseline
 
-    return cpu_baseline.forward_adjoint(image[:batch], smaps[:batch, :coils], omega)
+    return cpu_baseline.forward_adjoint(image, smaps, omega)
 
 
-def cpu_baseline_leg(image, smaps, omega, reps: int = 2, coils: int = 4):
+def cpu_baseline_leg(image, smaps, omega, reps: int = 2):
+    """Times the CPU port on the full workload (min of ``reps`` steps after
+    one untimed step); returns the cpu_baseline object and the untimed step's
+    outputs (the parity reference)."""
     from oracle import cpu_baseline
 
-    cpu_sample_run(image, smaps, omega, coils)  # warm-up (table build, thread pool)
+    ref = cpu_full_step(image, smaps, omega)
     times = []
     for _ in range(reps):
         t0 = time.perf_counter()
-        cpu_sample_run(image, smaps, omega, coils)
+        cpu_full_step(image, smaps, omega)
         times.append(time.perf_counter() - t0)
     t = min(times)
     M = omega.shape[1]
-    return {"value": coils * M / t, "unit": UNIT, "cores": cpu_baseline.threads(), "kind": "port",
-            "sample": f"batch 1 of {B}, {coils} of {C} coils, all {M} points; min of {reps} forward+adjoint runs "
-                      f"({t:.3f} s each); {cpu_baseline.describe()}"}
+    work = image.shape[0] * smaps.shape[1] * M
+    return {"value": work / t, "unit": UNIT, "cores": cpu_baseline.threads(), "kind": "port",
+            "sample": f"the full workload (batch {image.shape[0]}, {smaps.shape[1]} coils, {M} points) per step; "
+                      f"min of {reps} forward+adjoint steps ({t:.3f} s each) after one untimed; "
+                      f"{cpu_baseline.describe()}"}, ref
 
 
 # ---------------------------------------------------------------- arms
@@ -250,23 +262,24 @@ def run_reference(args):
     image, smaps, omega = make_inputs()
     from oracle import cpu_baseline
 
-    coils = args.ref_coils
     M = omega.shape[1]
     for _ in range(args.warmup):
-        cpu_sample_run(image, smaps, omega, coils)
+        cpu_full_step(image, smaps, omega)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        cpu_sample_run(image, smaps, omega, coils)
+        cpu_full_step(image, smaps, omega)
     dt = (time.perf_counter() - t0) / args.steps
-    value = coils * M / dt
+    work = B * C * M
+    value = work / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
         "config": {"workload": "2D SENSE NUFFT fwd+adj, image 320x320, grid 640x640, J=6, L=1024, 16 coils, "
-                               "batch 4, golden-angle 404x640", "sample_per_step": f"batch 1, {coils} coils, {M} points"},
+                               "batch 4, golden-angle 404x640 (258560 points)", "same_config": True,
+                   "work_per_step": work},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_baseline.threads(), "kind": "port",
-                         "sample": f"batch 1 of {B}, {coils} of {C} coils, all {M} points per step; "
+                         "sample": f"the full workload (batch {B}, {C} coils, {M} points) every step; "
                                    f"{cpu_baseline.describe()}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -411,9 +424,19 @@ def run_gpu(args):
 
     if rank != 0:
         return
+    # the CPU port on the full workload: its timing is the cpu_baseline leg
+    # (N=1 only) and its outputs are the parity reference of this line
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_leg(image_np, smaps_np, omega_np)
+        cpu, (k_ref, x_ref) = cpu_baseline_leg(image_np, smaps_np, omega_np)
+    else:
+        k_ref, x_ref = cpu_full_step(image_np, smaps_np, omega_np)
+    with torch.no_grad():
+        k_gpu = fwd(image, omega, smaps=smaps)
+        x_gpu = adj(torch.tensor(k_ref, device=dev), omega, smaps=smaps)
+        st_gpu = step_staged()
+        parity = {"forward": rel_l2(k_gpu.cpu().numpy(), k_ref), "adjoint": rel_l2(x_gpu.cpu().numpy(), x_ref),
+                  "forward_adjoint_step": rel_l2(st_gpu.cpu().numpy(), x_ref)}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -428,7 +451,10 @@ def run_gpu(args):
             "pipeline_gbs": round(pipeline_gbs, 1),
             "pipeline_algorithmic_bytes": byts["forward"] + byts["adjoint"],
             "parity_gate_rel_l2_staged_vs_module": gate,
+            "parity_oracle": "CPU port of the reference table path (oracle/cpu_baseline.py), same inputs, "
+                             "full workload; adjoint of the port's k-space data",
         },
+        "rel_l2_vs_oracle": parity,
         "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": f"{peak_src} hbm_gbs",
                      "algorithmic_bytes_per_launch": kbytes, "traffic": ncu_traffic(kernel)},
@@ -519,6 +545,17 @@ def run_ragged(args):
         eager_ms = timed(rn.forward_adjoint, args.steps, args.warmup)
         rn.capture()
         graph_ms = timed(rn.replay, args.steps, args.warmup)
+        # every problem against the CPU port of the reference path: the
+        # forward of its image, the adjoint of the port's k-space data
+        from oracle import cpu_baseline as P
+
+        xs_np = [x.cpu().numpy() for x in images]
+        ks = rn.forward(images)
+        want_k = [P.nufft_forward(xn, om, None) for xn, (_, om, _) in zip(xs_np, spec)]
+        e_fwd = max(rel_l2(a.cpu().numpy(), b) for a, b in zip(ks, want_k))
+        xs = rn.adjoint([torch.tensor(k, device=dev) for k in want_k])
+        e_adj = max(rel_l2(a.cpu().numpy(), P.nufft_adjoint(k, om, im, None))
+                    for a, k, (im, om, _) in zip(xs, want_k, spec))
     line = {
         "metric": "NU points*coils/s (ragged batch fwd+adj, 64 problems, graph-captured)", "value": work / (graph_ms * 1e-3),
         "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": graph_ms,
@@ -529,6 +566,8 @@ def run_ragged(args):
                    "graph_ms_per_step": graph_ms, "speedup_graph_vs_plain": plain_ms / graph_ms,
                    "tiles": {f"{k[0]}x{k[1]}": v for k, v in rn.tiles.items()},
                    "parity_gate_rel_l2_vs_per_problem": gate},
+        "rel_l2_vs_oracle": {"forward_max_over_problems": e_fwd, "adjoint_max_over_problems": e_adj,
+                             "problems_compared": len(spec)},
         "gpu_launches": None,
     }
     print(json.dumps(line))
@@ -674,29 +713,81 @@ def run_config(args):
         xr = x.clone().requires_grad_(True)
         om_r = omega.clone().requires_grad_(True)
 
+        def move_trajectory():
+            # a trajectory-optimisation step changes ktraj in place (here a
+            # sign step of 1e-5 rad, no host sync), so the next call rebuilds
+            # the bin-sorted layout and the adjoint's per-point factors
+            with torch.no_grad():
+                g = om_r.grad if om_r.grad is not None else torch.ones_like(om_r)
+                om_r.sub_(1e-5 * torch.sign(g))
+
+        def fwd_step():
+            move_trajectory()
+            with torch.no_grad():
+                adj(fwd(x, om_r, smaps=smaps), om_r, smaps=smaps)
+
         def grad_step():
+            move_trajectory()
             xr.grad = None
             om_r.grad = None
             y = adj(fwd(xr, om_r, smaps=smaps), om_r, smaps=smaps)
             loss = (y - xr).abs().pow(2).sum()
             loss.backward()
 
-        with torch.no_grad():
-            fwd_ms = timed(lambda: adj(fwd(x, omega, smaps=smaps), omega, smaps=smaps), args.steps, args.warmup)
+        fwd_ms = timed(fwd_step, args.steps, args.warmup)
         ms = timed(grad_step, args.steps, args.warmup)
+        from torchkbnufft_gb300 import _runtime as R
+
         extra = {"forward_AHA_ms": fwd_ms, "grad_step_ms": ms, "backward_over_forward": (ms - fwd_ms) / fwd_ms,
-                 "note": "a step is the forward A^H A x, the loss and its backward (x and ktraj gradients)"}
+                 "trajectory": "updated in place every step (layout rebuild and factor pre-pass timed)",
+                 "layout_cache_entries_after": R.layout_cache_info()[0],
+                 "note": "a step is the ktraj update, the forward A^H A x, the loss and its backward "
+                         "(x and ktraj gradients); the forward-only step is the update and A^H A x"}
     else:
         with torch.no_grad():
             ms = timed(lambda: adj(fwd(x, omega, smaps=smaps), omega, smaps=smaps), args.steps, args.warmup)
             extra = {"stage_ms": stage_times(fwd, omega, x, smaps, args.steps, args.warmup)}
+    parity = config_parity(w, fwd, adj, x, omega, smaps, om, im)
     line = {
         "metric": f"NU points*coils/s ({w})", "value": work / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128" if cdt == torch.complex128 else "c64", "data": "synthetic",
         "config": {"workload": desc, "work_per_step": work, **extra},
+        "rel_l2_vs_oracle": parity,
     }
     print(json.dumps(line))
+
+
+def config_parity(w, fwd, adj, x, omega, smaps, om, im):
+    """Forward and adjoint of the workload's inputs against the CPU port of the
+    reference path (oracle/cpu_baseline.py): the full workload, except the
+    kooshball, whose port side runs at a seeded 4096-point subset (forward at
+    those points; adjoint of k-space data that is zero elsewhere)."""
+    import torch
+
+    from oracle import cpu_baseline as P
+
+    xn = x.detach().cpu().numpy()
+    sn = None if smaps is None else smaps.detach().cpu().numpy().astype(xn.dtype)
+    omn = om.astype(np.float64) if xn.dtype == np.complex128 else om
+    with torch.no_grad():
+        y = fwd(x, omega, smaps=smaps)
+        if w == "kooshball":
+            sub = np.sort(np.random.default_rng(1003).choice(om.shape[1], 4096, replace=False))
+            subd = torch.tensor(sub, device=y.device)
+            k_ref = P.nufft_forward(xn, omn[:, sub], sn)
+            e_fwd = rel_l2(y[..., subd].cpu().numpy(), k_ref)
+            kfull = torch.zeros_like(y)
+            kfull[..., subd] = torch.tensor(k_ref, device=y.device)
+            del y
+            e_adj = rel_l2(adj(kfull, omega, smaps=smaps).cpu().numpy(), P.nufft_adjoint(k_ref, omn[:, sub], im, sn))
+            return {"forward": e_fwd, "adjoint": e_adj, "points_compared": 4096}
+        k_ref = P.nufft_forward(xn, omn, sn)
+        e_fwd = rel_l2(y.cpu().numpy(), k_ref)
+        del y
+        x_ref = P.nufft_adjoint(k_ref, omn, im, sn)
+        e_adj = rel_l2(adj(torch.tensor(k_ref, device=x.device), omega, smaps=smaps).cpu().numpy(), x_ref)
+    return {"forward": e_fwd, "adjoint": e_adj}
 
 
 # ---------------------------------------------------------------- second comparator: the reference on the GPU
@@ -771,7 +862,6 @@ def main():
                         "own PyTorch path on the GPU (a second comparator)")
     p.add_argument("--device", default=None, help="device of the reference-gpu arm (default cuda)")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--ref-coils", type=int, default=4)
     p.add_argument("--workload", default="sense", choices=["sense", "ragged", "single", "kooshball", "spiral-grad", "sense-c128"],
                    help="sense: the metric's workload (default); the others are reported beside it")
     args = p.parse_args()

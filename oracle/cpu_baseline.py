@@ -91,6 +91,26 @@ def interp_adjoint(op: O.Operator, kdata: np.ndarray, omega: np.ndarray) -> np.n
     return out
 
 
+class PortOperator(O.Operator):
+    """The oracle's ``Operator`` with its interpolation run by the C port
+    (one shared ``(d, M)`` trajectory), for benchmark-size trajectories in
+    ``kbnufft_oracle.toeplitz_kernel`` / ``density_compensation``."""
+
+    def interp(self, grid, omega):
+        om = np.asarray(omega)
+        if om.ndim == 3:
+            return np.concatenate([interp_forward(self, grid[b:b + 1], om[b]) for b in range(om.shape[0])])
+        return interp_forward(self, grid, om)
+
+    def interp_adj(self, kdata, omega, grid_size=None):
+        if grid_size is not None and tuple(grid_size) != tuple(self.grid_size):
+            raise ValueError("the C port adjoint writes the operator's own grid size")
+        om = np.asarray(omega)
+        if om.ndim == 3:
+            return np.concatenate([interp_adjoint(self, kdata[b:b + 1], om[b]) for b in range(om.shape[0])])
+        return interp_adjoint(self, kdata, om)
+
+
 def _op(im_size, cdtype):
     key = (tuple(im_size), np.dtype(cdtype))
     if key not in _ops:
@@ -98,20 +118,45 @@ def _op(im_size, cdtype):
     return _ops[key]
 
 
-def forward_adjoint(image: np.ndarray, smaps: np.ndarray, omega: np.ndarray) -> np.ndarray:
-    """One SENSE forward NUFFT and one adjoint NUFFT of its output (complex64)."""
+def nufft_forward(image: np.ndarray, omega: np.ndarray, smaps=None, im_size=None) -> np.ndarray:
+    """``KbNufft.forward`` (modules/kbnufft.py:125-228): ``image * smaps * scaling``
+    -> zero-pad -> FFT -> table interpolation at ``omega`` (d, M). complex64 or
+    complex128, following the image's dtype. ``smaps`` None: image (B, C, *N)."""
     import scipy.fft as sfft
 
-    im_size = image.shape[2:]
+    im_size = tuple(image.shape[2:]) if im_size is None else tuple(im_size)
     op = _op(im_size, image.dtype)
     nd = len(im_size)
     ax = tuple(range(-nd, 0))
-    w = threads()
-    x = image * smaps * op.scaling
+    x = image * smaps if smaps is not None else image
+    x = x * op.scaling
     pad = [(0, 0), (0, 0)] + [(0, g - n) for g, n in zip(op.grid_size, im_size)]
-    grid = sfft.fftn(np.pad(x, pad), axes=ax, workers=w).astype(image.dtype, copy=False)
-    kdata = interp_forward(op, grid, omega)
+    grid = sfft.fftn(np.pad(x, pad), axes=ax, workers=threads()).astype(image.dtype, copy=False)
+    del x
+    return interp_forward(op, grid, omega)
+
+
+def nufft_adjoint(kdata: np.ndarray, omega: np.ndarray, im_size, smaps=None) -> np.ndarray:
+    """``KbNufftAdjoint.forward`` (modules/kbnufft.py:307-410): table
+    interpolation adjoint -> unnormalised IFFT -> crop -> ``* conj(scaling)``
+    -> ``sum_c conj(smaps)`` when maps are given."""
+    import scipy.fft as sfft
+
+    im_size = tuple(im_size)
+    op = _op(im_size, kdata.dtype)
+    nd = len(im_size)
+    ax = tuple(range(-nd, 0))
     g2 = interp_adjoint(op, kdata, omega)
-    img = sfft.ifftn(g2, axes=ax, norm="forward", workers=w).astype(image.dtype, copy=False)
+    img = sfft.ifftn(g2, axes=ax, norm="forward", workers=threads()).astype(kdata.dtype, copy=False)
+    del g2
     img = img[(Ellipsis,) + tuple(slice(0, n) for n in im_size)] * np.conj(op.scaling)
+    if smaps is None:
+        return img
     return np.sum(img * np.conj(smaps), axis=1, keepdims=True)
+
+
+def forward_adjoint(image: np.ndarray, smaps: np.ndarray, omega: np.ndarray):
+    """One SENSE forward NUFFT and one adjoint NUFFT of its output; returns
+    (k-space data, adjoint image)."""
+    kdata = nufft_forward(image, omega, smaps)
+    return kdata, nufft_adjoint(kdata, omega, image.shape[2:], smaps)

@@ -302,20 +302,24 @@ def toep_apply(image, kernel, smaps=None, norm=None):
 
 
 def toeplitz_kernel(omega, im_size, weights=None, norm=None, grid_size=None, numpoints=6,
-                    table_oversamp=2**10, kbwidth=2.34, order=0.0):
-    """``calc_toeplitz_kernel`` restated (``torchkbnufft/_nufft/toep.py:11-307``)."""
+                    table_oversamp=2**10, kbwidth=2.34, order=0.0, operator_cls=None):
+    """``calc_toeplitz_kernel`` restated (``torchkbnufft/_nufft/toep.py:11-307``).
+
+    ``operator_cls`` (default ``Operator``) supplies the interpolation; the
+    CPU port's subclass runs it in C for benchmark-size trajectories."""
+    operator_cls = Operator if operator_cls is None else operator_cls
     omega = np.asarray(omega)
     if omega.ndim == 3:
         ks = []
         for i in range(omega.shape[0]):
             w = None if weights is None else np.asarray(weights)[i]
             ks.append(toeplitz_kernel(omega[i], im_size, w, norm, grid_size, numpoints, table_oversamp,
-                                      kbwidth, order))
+                                      kbwidth, order, operator_cls))
         return np.stack(ks)
     rdt = omega.dtype
     cdt = np.complex64 if rdt == np.float32 else np.complex128
     nd = omega.shape[0]
-    op = Operator(im_size, grid_size, numpoints, [0] * nd, table_oversamp, kbwidth, order, cdt)
+    op = operator_cls(im_size, grid_size, numpoints, [0] * nd, table_oversamp, kbwidth, order, cdt)
     if weights is None:
         w = np.ones((1, 1, omega.shape[-1]), dtype=cdt)
     else:
@@ -362,8 +366,11 @@ def toeplitz_kernel(omega, im_size, weights=None, norm=None, grid_size=None, num
 
 
 def density_compensation(ktraj, im_size, num_iterations=10, grid_size=None, numpoints=6, n_shift=None,
-                         table_oversamp=2**10, kbwidth=2.34, order=0.0):
-    """Pipe iteration ``w <- w / |A A^H w|`` (``torchkbnufft/_nufft/dcomp.py:10-119``)."""
+                         table_oversamp=2**10, kbwidth=2.34, order=0.0, operator_cls=None):
+    """Pipe iteration ``w <- w / |A A^H w|`` (``torchkbnufft/_nufft/dcomp.py:10-119``).
+
+    ``operator_cls`` as in ``toeplitz_kernel``."""
+    operator_cls = Operator if operator_cls is None else operator_cls
     ktraj = np.asarray(ktraj)
     B = 1
     if ktraj.ndim == 3:
@@ -372,7 +379,7 @@ def density_compensation(ktraj, im_size, num_iterations=10, grid_size=None, nump
         else:
             B = ktraj.shape[0]
     cdt = np.complex64 if ktraj.dtype == np.float32 else np.complex128
-    op = Operator(im_size, grid_size, numpoints, n_shift, table_oversamp, kbwidth, order, cdt)
+    op = operator_cls(im_size, grid_size, numpoints, n_shift, table_oversamp, kbwidth, order, cdt)
     sig = np.ones((B, 1, ktraj.shape[-1]), dtype=cdt)
     for _ in range(num_iterations):
         sig = sig / np.abs(op.interp(op.interp_adj(sig, ktraj), ktraj))

@@ -1,8 +1,9 @@
 """Generate the golden fixtures in this folder from the reference implementation.
 
-Run in a container where the reference (mmuckley/torchkbnufft) is importable::
+Run where the reference (mmuckley/torchkbnufft) source tree is available,
+giving its location as the argument or in ``TKBN_REFERENCE``::
 
-    PYTHONPATH=/root/reference python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <path to the reference source tree>
 
 Two kinds of fixtures are written:
 
@@ -29,7 +30,7 @@ import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("TKBN_REFERENCE", "/root/reference")
+REF = None  # the reference source tree, from the command line or TKBN_REFERENCE
 
 
 def _np(t):
@@ -176,6 +177,26 @@ def live_cases():
         arrs["kwargs"] = np.array(repr(kw))
         cases[name] = arrs
 
+    # gradient of the trajectory-optimisation loss ||A^H A x - x||^2 (summed over
+    # the batch) with respect to the image, through the reference's autograd
+    # (its table interpolation Functions, _autograd/interp.py:78-178, and torch's
+    # FFT backward); variable-density spiral k(t) = pi t^1.5 exp(i(2 pi 16 t + 2 pi j / nil))
+    for name, B, C, im_size, nil, ns, seed in (("grad_x_spiral", 2, 4, (48, 48), 8, 384, 50),):
+        gen = torch.Generator().manual_seed(seed)
+        t = np.arange(ns) / ns
+        k = np.concatenate([np.pi * t ** 1.5 * np.exp(1j * (2 * np.pi * 16 * t + 2 * np.pi * j / nil))
+                            for j in range(nil)])
+        om = torch.tensor(np.stack([k.imag, k.real]).astype(np.float32))
+        image = _cplx(gen, (B, 1) + im_size, torch.complex64)
+        smaps = _cplx(gen, (B, C) + im_size, torch.complex64) / 2
+        fwd = tkbn.KbNufft(im_size=im_size)
+        adj = tkbn.KbNufftAdjoint(im_size=im_size)
+        x = image.clone().requires_grad_(True)
+        y = adj(fwd(x, om, smaps=smaps), om, smaps=smaps)
+        loss = (y - x).abs().pow(2).sum()
+        loss.backward()
+        cases[name] = dict(image=_np(image), smaps=_np(smaps), omega=_np(om), loss=_np(loss), grad=_np(x.grad))
+
     only = os.environ.get("TKBN_GOLDEN_ONLY")
     for name, arrs in cases.items():
         if only and not name.startswith(only):
@@ -184,6 +205,9 @@ def live_cases():
 
 
 if __name__ == "__main__":
+    REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TKBN_REFERENCE")
+    if not REF or not os.path.isdir(os.path.join(REF, "torchkbnufft")):
+        sys.exit("usage: make_golden.py <reference source tree> (or set TKBN_REFERENCE)")
     sys.path.insert(0, REF)
     if not os.environ.get("TKBN_GOLDEN_ONLY"):
         convert_reference_pickles()

@@ -9,7 +9,11 @@ Caches (per process):
   ``tolist()`` would synchronise the device on every call);
 * trajectory layouts (bin-sorted points): keyed by the omega tensor object,
   its version counter, shape and the geometry, so a trajectory that is
-  modified in place or freed is never reused;
+  modified in place or freed is never reused. A miss for a trajectory drops
+  its entries of older versions (an optimiser stepping omega in place keeps
+  one layout, not one per step), an entry goes when its trajectory is freed,
+  and the cache holds at most ``TKBN_LAYOUT_CACHE_BYTES`` of workspaces
+  (default 4 GiB; the newest layout is always kept) and 128 entries;
 * cuFFT plans: keyed by geometry, batch*coils and device.
 """
 
@@ -17,6 +21,7 @@ from __future__ import annotations
 
 import collections
 import ctypes
+import os
 import threading
 import weakref
 from dataclasses import dataclass
@@ -196,6 +201,47 @@ class PointsLayout:
             L.lib().tkbn_points_build(ctypes.byref(g), ctypes.byref(self.desc), om.data_ptr(),
                                       self.workspace.data_ptr(), self.nbytes, stream_handle(self.device))
         )
+        # cross-stream ordering: the build's stream, an event after the build,
+        # the streams already ordered after it, and the stream of the last
+        # adjoint (adjoints write the per-point factor scratch in the workspace)
+        build_stream = torch.cuda.current_stream(self.device)
+        self._built = None
+        self._ready_streams = {build_stream.cuda_stream}
+        self._adj_stream = build_stream
+        if not stream_capturing(self.device):
+            self._built = torch.cuda.Event()
+            self._built.record(build_stream)
+
+    def stream_for_call(self, adjoint: bool) -> int:
+        """Orders a call on torch's current stream after the work it depends on
+        and returns that stream's handle.
+
+        Every call waits (once per stream) for the layout build when it runs
+        on another stream than the build, and the workspace is marked as used
+        by that stream, so the caching allocator keeps it until the stream's
+        work is done even after the layout is evicted. Adjoint calls also wait
+        for the last adjoint on this layout when that ran on another stream:
+        they write and read the per-point factor scratch. Forward calls only
+        read what the build wrote. Under CUDA graph capture nothing is added
+        (a captured sequence is ordered by its own stream)."""
+        s = torch.cuda.current_stream(self.device)
+        h = s.cuda_stream
+        if stream_capturing(self.device):
+            return h
+        with _lock:
+            if h not in self._ready_streams:
+                if self._built is not None:
+                    s.wait_event(self._built)
+                self.workspace.record_stream(s)
+                self._ready_streams.add(h)
+            if adjoint:
+                prev = self._adj_stream
+                if prev is not None and prev.cuda_stream != h:
+                    ev = torch.cuda.Event()
+                    ev.record(prev)
+                    s.wait_event(ev)
+                self._adj_stream = s
+        return h
 
     def adjoint_call(self, tables: Sequence[torch.Tensor], table_flags: int, call) -> None:
         """Runs ``call(flags)``, an adjoint entry point on this layout's workspace,
@@ -244,6 +290,26 @@ _layout_cache: "collections.OrderedDict" = collections.OrderedDict()
 _LAYOUT_CACHE_MAX = 128
 
 
+def _layout_cache_bytes_max() -> int:
+    try:
+        return int(os.environ.get("TKBN_LAYOUT_CACHE_BYTES", 4 << 30))
+    except ValueError:
+        return 4 << 30
+
+
+def _drop_layouts_of(base_id: int, keep_key=None) -> None:
+    """Drops every cached layout of the trajectory object ``base_id`` except ``keep_key``."""
+    for k in [k for k in _layout_cache if k[0] == base_id and k != keep_key]:
+        del _layout_cache[k]
+
+
+def _on_trajectory_freed(base_id: int):
+    def cb(_ref):
+        with _lock:
+            _drop_layouts_of(base_id)
+    return cb
+
+
 def points_layout(geom: GeomKey, omega: torch.Tensor, tile=None, chunk: int = 0,
                   deterministic: Optional[bool] = None) -> PointsLayout:
     """Cached layout of omega. ``deterministic`` (default: torch's deterministic-algorithms
@@ -258,11 +324,27 @@ def points_layout(geom: GeomKey, omega: torch.Tensor, tile=None, chunk: int = 0,
         if hit is not None and hit[0]() is base:
             _layout_cache.move_to_end(key)
             return hit[1]
+        # entries of this trajectory object at another version or storage can
+        # never be hit again (versions only grow); entries of a dead object
+        # whose id was reused are dropped as well
+        stale = [k for k, v in _layout_cache.items() if k[0] == id(base) and
+                 (v[0]() is not base or k[1] != key[1] or k[2] != key[2])]
+        for k in stale:
+            del _layout_cache[k]
         lay = PointsLayout(geom, omega, tile, chunk, deterministic)
-        _layout_cache[key] = (weakref.ref(base), lay)
-        while len(_layout_cache) > _LAYOUT_CACHE_MAX:
-            _layout_cache.popitem(last=False)
+        _layout_cache[key] = (weakref.ref(base, _on_trajectory_freed(id(base))), lay)
+        cap = _layout_cache_bytes_max()
+        total = sum(v[1].nbytes for v in _layout_cache.values())
+        while len(_layout_cache) > 1 and (len(_layout_cache) > _LAYOUT_CACHE_MAX or total > cap):
+            _, (_, old) = _layout_cache.popitem(last=False)
+            total -= old.nbytes
         return lay
+
+
+def layout_cache_info() -> Tuple[int, int]:
+    """(entries, workspace bytes) held by the layout cache."""
+    with _lock:
+        return len(_layout_cache), sum(v[1].nbytes for v in _layout_cache.values())
 
 
 def clear_caches() -> None:
@@ -447,7 +529,7 @@ def interp_fwd(geom: GeomKey, lay: PointsLayout, tables, grid: torch.Tensor) -> 
     tp, keep, fl = table_ptrs(tables, grid.dtype)
     L.check(L.lib().tkbn_interp_fwd(ctypes.byref(geom_struct(geom, fl | lay.flags)), ctypes.byref(lay.desc),
                                     lay.workspace.data_ptr(), tp, grid.data_ptr(), B, C, kdata.data_ptr(),
-                                    stream_handle(dev)))
+                                    lay.stream_for_call(False)))
     return kdata
 
 
@@ -460,7 +542,7 @@ def interp_adj(geom: GeomKey, lay: PointsLayout, tables, kdata: torch.Tensor) ->
     tp, keep, fl = table_ptrs(tables, kdata.dtype)
     lay.adjoint_call(keep, fl, lambda flags: L.check(L.lib().tkbn_interp_adj(
         ctypes.byref(geom_struct(geom, flags)), ctypes.byref(lay.desc), lay.workspace.data_ptr(), tp,
-        kdata.data_ptr(), B, C, grid.data_ptr(), stream_handle(dev))))
+        kdata.data_ptr(), B, C, grid.data_ptr(), lay.stream_for_call(True))))
     return grid
 
 
@@ -478,7 +560,7 @@ def interp_grad_omega(geom: GeomKey, lay: PointsLayout, tables, grid: torch.Tens
     dp, keep2, _ = table_ptrs(dtabs, grid.dtype)
     L.check(L.lib().tkbn_interp_grad_omega(ctypes.byref(geom_struct(geom, lay.flags)), ctypes.byref(lay.desc),
                                            lay.workspace.data_ptr(), tp, dp, grid.data_ptr(), v.data_ptr(), B, C,
-                                           grad.data_ptr(), stream_handle(dev)))
+                                           grad.data_ptr(), lay.stream_for_call(False)))
     return grad
 
 
@@ -543,7 +625,7 @@ def nufft_fwd(geom: GeomKey, lay: PointsLayout, tables, scaling, image, smaps, n
     L.check(L.lib().tkbn_nufft_fwd(ctypes.byref(geom_struct(geom, fl | lay.flags)), ctypes.byref(lay.desc),
                                    lay.workspace.data_ptr(),
                                    plan.handle, tp, _c(scaling), image.data_ptr(), _c(smaps), sb, B, C,
-                                   norm_code(norm), grid.data_ptr(), kdata.data_ptr(), stream_handle(dev)))
+                                   norm_code(norm), grid.data_ptr(), kdata.data_ptr(), lay.stream_for_call(False)))
     return kdata
 
 
@@ -566,7 +648,7 @@ def nufft_adj(geom: GeomKey, lay: PointsLayout, tables, scaling, kdata, smaps, n
     lay.adjoint_call(keep, fl, lambda flags: L.check(L.lib().tkbn_nufft_adj(
         ctypes.byref(geom_struct(geom, flags)), ctypes.byref(lay.desc), lay.workspace.data_ptr(), plan.handle, tp,
         _c(scaling), kdata.data_ptr(), _c(smaps), sb, B, C, norm_code(norm), grid.data_ptr(), image.data_ptr(),
-        stream_handle(dev))))
+        lay.stream_for_call(True))))
     return image
 
 

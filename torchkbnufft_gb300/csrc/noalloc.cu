@@ -12,10 +12,17 @@
 //
 // Set-up: the first call on each device (with that device current) looks up
 // the array's device address with cudaGetSymbolAddress; make that first call
-// before any stream capture. Every call shares the one array and overwrites
-// it, so calls that overlap on the GPU (other streams, other host threads)
-// race; serialise them. The layout build clears everything that must start at
-// zero on each call.
+// before any stream capture. The address is cached per device together with
+// the CUDA context it belongs to: when the device's context changes (after
+// cudaDeviceReset, or when the primary context is released and created
+// again) the next call looks the address up again, so that call too should
+// come before any stream capture. Every call shares the one array and
+// overwrites it, so calls that overlap on the GPU (other streams, other host
+// threads) race; serialise them. The layout build clears everything that
+// must start at zero on each call.
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include <mutex>
 
@@ -37,7 +44,28 @@ constexpr int kMaxDevices = 64;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
+struct ScratchAddress {
+  CUcontext ctx;  // the context the address belongs to
+  void* addr;
+};
+ScratchAddress g_addr[kMaxDevices] = {};
+
+// The calling thread's current context (null when none is current or the
+// driver entry point is unavailable), through the runtime's driver entry
+// point, so the library needs no link against libcuda.
+CUcontext current_context() {
+  static PFN_cuCtxGetCurrent_v4000 get = []() -> PFN_cuCtxGetCurrent_v4000 {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return (PFN_cuCtxGetCurrent_v4000)fn;
+  }();
+  CUcontext c = nullptr;
+  if (!get || get(&c) != CUDA_SUCCESS) return nullptr;
+  return c;
+}
 
 int scratch_address(void** out) {
   int dev = 0;
@@ -45,13 +73,19 @@ int scratch_address(void** out) {
   if (rc) return rc;
   if (dev < 0 || dev >= kMaxDevices) return tkbn_host::set_error(TKBN_ERR_UNSUPPORTED, "device index %d too large", dev);
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
+  CUcontext ctx = current_context();
+  if (!ctx || ctx != g_addr[dev].ctx || !g_addr[dev].addr) {
+    // also makes the device's primary context current when none is yet
     void* p = nullptr;
     rc = tkbn_host::check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)");
     if (rc) return rc;
-    g_addr[dev] = p;
+    ctx = current_context();
+    g_addr[dev].ctx = ctx;       // null: no context to key on, so look it up on every call
+    g_addr[dev].addr = ctx ? p : nullptr;
+    *out = p;
+    return TKBN_OK;
   }
-  *out = g_addr[dev];
+  *out = g_addr[dev].addr;
   return TKBN_OK;
 }
 
