@@ -315,33 +315,31 @@ def _kernels_launched(fn, tmp_path):
     return {e.get("name", "") for e in events if e.get("cat") == "kernel"}
 
 
-@pytest.mark.parametrize("case", ["2d16", "2d4", "2d1", "2d16det", "3d8"])
+@pytest.mark.parametrize("case", ["2d16", "2d4", "3d8"])
 def test_specialised_kernels_are_selected(case, tmp_path):
-    """The benchmark shapes run the specialised kernels: in 2D the coil-part
-    adjoint (linear-phase tables; a deterministic layout keeps the
-    register-accumulator adjoint with table factors) and the coil-pair gather,
-    in 3D the register adjoint (a layout or eligibility regression would
-    silently fall back to the generic kernels, which are also correct)."""
+    """The benchmark shapes run the register-accumulator adjoint and the coil-pair
+    gather (a layout or eligibility regression would silently fall back to the
+    generic kernels, which are also correct)."""
     from torchkbnufft_gb300 import _runtime as R
 
     gen = torch.Generator().manual_seed(31)
     if case == "3d8":
         im, C = (16, 16, 16), 8
     else:
-        im, C = (40, 40), {"2d16": 16, "2d4": 4, "2d1": 1, "2d16det": 16}[case]
+        im, C = (40, 40), 16 if case == "2d16" else 4
     gs = tuple(2 * n for n in im)
     M = 3000
     om = ((torch.rand((len(im), M), generator=gen, dtype=torch.float64) * 2 - 1) * np.pi).float().to(DEV)
     mod = tkbn().KbNufft(im_size=im, device=DEV)
     geom = mod._geom(torch.complex64)
     tables = mod._tables()
-    lay = R.points_layout(geom, om, deterministic=case == "2d16det")
+    lay = R.points_layout(geom, om)
     grid = torch.randn((1, C) + gs, dtype=torch.complex64, generator=torch.Generator().manual_seed(3)).to(DEV)
     kdata = R.interp_fwd(geom, lay, tables, grid)
     names = _kernels_launched(lambda: R.interp_adj(geom, lay, tables, kdata), tmp_path)
-    want = {"3d8": "k_interp_adj_reg3", "2d16det": "k_interp_adj_reg<"}.get(case, "k_adj_cp<")
+    want = "k_interp_adj_reg3" if case == "3d8" else "k_interp_adj_reg<"
     assert any(want in n for n in names), names
-    if case not in ("3d8", "2d1"):
+    if case != "3d8":
         names = _kernels_launched(lambda: R.interp_fwd(geom, lay, tables, grid), tmp_path)
         assert any("k_interp_fwd_pairs" in n for n in names), names
 
@@ -412,7 +410,7 @@ def test_adjoint_factor_reuse_follows_the_tables(tmp_path):
 
     def prepass_launched(mod):
         names = _kernels_launched(lambda: mod(yd, omd), tmp_path)
-        assert any("k_adj_cp<" in n or "k_interp_adj_reg<" in n for n in names), names
+        assert any("k_interp_adj_reg<" in n for n in names), names
         return any("k_point_factors2" in n for n in names)
 
     assert rel_l2(run(a1), ref1) < TOL64

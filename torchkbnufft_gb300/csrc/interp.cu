@@ -2568,68 +2568,10 @@ static size_t reg_smem(int CC) {
   return staging > partials ? staging : partials;
 }
 
-// The layout's 2D factor scratch: per-point records, then {Ey, Ex} and the
-// left-out count past them, the left-out list in the records' spare room.
-struct FactorScratch {
-  float2 *pf, *et;
-  int32_t *fix, *nfix;
-};
-
-static FactorScratch factor_scratch(const InterpPlan& ip, const char* ws) {
-  FactorScratch f;
-  f.pf = (float2*)const_cast<char*>(ws + ip.L.off_pfac);
-  f.et = f.pf + ip.a.n * 12;
-  f.nfix = reinterpret_cast<int32_t*>(f.et + kLpEy + kLpEx + 8);
-  f.fix = reinterpret_cast<int32_t*>(f.pf + ip.a.n * 8);
-  return f;
-}
-
-// The 2D per-point factor pre-pass (linear-phase records when lp, else the 12
-// conjugated table factors per point), unless the call carries
-// TKBN_ADJ_REUSE_FACTORS: then the caller vouches that an earlier call on
-// this workspace left the factors, E tables and left-out list of these
-// tables and flags in place.
-static int point_factors_prepass(const Geo<float>& geo, const InterpPlan& ip, const char* ws, bool lp,
-                                 const FactorScratch& f, cudaStream_t s) {
-  if (!ip.L.pfac || ip.a.n == 0 || (ip.flags & TKBN_ADJ_REUSE_FACTORS)) return TKBN_OK;
-  const int64_t nb = (2 * ip.a.n + kThreads - 1) / kThreads;
-  const int grid_b = (int)(nb < 152 * 16 ? nb : 152 * 16);
-  if (lp) {
-    int rc = check_cuda(cudaMemsetAsync(f.nfix, 0, sizeof(int32_t), s), "reset left-out count");
-    if (rc) return rc;
-    k_point_factors2<true><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
-                                                        (const float2*)(ws + ip.L.off_phase), ip.a.n, f.pf, f.et,
-                                                        f.fix, f.nfix);
-  } else {
-    k_point_factors2<false><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
-                                                         (const float2*)(ws + ip.L.off_phase), ip.a.n, f.pf, f.et,
-                                                         f.fix, f.nfix);
-  }
-  return check_cuda(cudaGetLastError(), "factor pre-pass launch");
-}
-
 template <typename R, int D, int JC>
 static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* kdata, void* grid,
                             cudaStream_t s) {
   const OwnLaunch o = make_own(ip, ws, D);
-  if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
-    // linear-phase tables on a layout with the 16 x 4 lists: the coil-part
-    // adjoint (interp_cp.cu), then the exact pass for the points it leaves out
-    const bool lp = (ip.flags & TKBN_TABLES_LINEAR_PHASE) && !(ip.flags & TKBN_ADJ_DETERMINISTIC) && ip.L.pfac;
-    if (lp && adj_cp_eligible(ip.L, o.Cc, grid)) {
-      const FactorScratch f = factor_scratch(ip, ws);
-      int rc = point_factors_prepass(geo, ip, ws, true, f, s);
-      // the entry records belong to the same pre-pass (reused with the factors)
-      if (!rc && !(ip.flags & TKBN_ADJ_REUSE_FACTORS)) rc = adj_cp_records(ip.L, ws, f.pf, f.et, s);
-      if (!rc)
-        rc = adj_cp_launch(geo, ip.L, ws, f.et, o.M, o.ntraj, o.B, o.C, o.Cc, o.ncc, o.nbpt, o.gtot, kdata, grid, s);
-      if (rc) return rc;
-      k_adj_lp_fix<<<152, kThreads, 0, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
-                                             (const float2*)(ws + ip.L.off_phase), (const float2*)kdata, f.fix,
-                                             f.nfix, (float2*)grid);
-      return check_cuda(cudaGetLastError(), "interp_adj fix launch");
-    }
-  }
   const size_t smem = own_smem<R, D, JC>(o);
   if (smem > 220 * 1024) return set_error(TKBN_ERR_UNSUPPORTED, "adjoint tile needs %zu bytes of shared memory", smem);
   const int64_t max_jobs = ip.L.max_subjobs * o.nbpt * o.ncc;
@@ -2650,14 +2592,30 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
       // (a deterministic layout keeps the table path: the linear-phase form
       // adds its left-out points with atomics)
       const bool lp = (ip.flags & TKBN_TABLES_LINEAR_PHASE) && !(ip.flags & TKBN_ADJ_DETERMINISTIC) && ip.L.pfac;
-      // the layout's factor scratch (see tkbn_interp_adj: calls sharing a workspace are ordered)
-      const FactorScratch f = factor_scratch(ip, ws);
-      float2* pf = f.pf;
-      int32_t* nfix = f.nfix;
-      int32_t* fix = f.fix;
+      // the layout's factor scratch (see tkbn_interp_adj: calls sharing a workspace are ordered):
+      // per-point records, then {Ey, Ex} and the left-out count past them, the
+      // left-out list in the records' spare room
+      float2* pf = (float2*)const_cast<char*>(ws + ip.L.off_pfac);
+      float2* et = pf + ip.a.n * 12;
+      int32_t* nfix = reinterpret_cast<int32_t*>(et + kLpEy + kLpEx + 8);
+      int32_t* fix = reinterpret_cast<int32_t*>(pf + ip.a.n * 8);
       if (ip.L.pfac && ip.a.n > 0) {
-        int rc0 = point_factors_prepass(geo, ip, ws, lp, f, s);
-        if (rc0) return rc0;
+        const int64_t nb = (2 * ip.a.n + kThreads - 1) / kThreads;
+        const int grid_b = (int)(nb < 152 * 16 ? nb : 152 * 16);
+        if (ip.flags & TKBN_ADJ_REUSE_FACTORS) {
+          // the caller vouches that an earlier call on this workspace left the
+          // factors (and the left-out list) of these tables and flags in place
+        } else if (lp) {
+          int rc0 = check_cuda(cudaMemsetAsync(nfix, 0, sizeof(int32_t), s), "reset left-out count");
+          if (rc0) return rc0;
+          k_point_factors2<true><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
+                                                              (const float2*)(ws + ip.L.off_phase), ip.a.n, pf, et,
+                                                              fix, nfix);
+        } else {
+          k_point_factors2<false><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
+                                                               (const float2*)(ws + ip.L.off_phase), ip.a.n, pf, et,
+                                                               fix, nfix);
+        }
         orr.pfac = pf;
       }
       return with_cc(reg_cc(o.Cc), [&](auto ccv) {

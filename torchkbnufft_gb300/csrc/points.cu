@@ -13,7 +13,6 @@
 
 #include <cstdarg>
 #include <cstdio>
-#include <type_traits>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -313,7 +312,7 @@ __global__ void __launch_bounds__(kSortWarps * 32)
 // atomics into a pre-zeroed tile; unsplit tiles are written with plain stores).
 __global__ void k_fill_subjobs(const int32_t* __restrict__ work, const int32_t* __restrict__ nsub,
                                const int32_t* __restrict__ suboff, int64_t nkeys, int W, Item* __restrict__ jobs,
-                               int64_t* __restrict__ hdr, int hslot) {
+                               int64_t* __restrict__ hdr) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nkeys; k += (int64_t)gridDim.x * blockDim.x) {
     const int ns = nsub[k];
     for (int q = 0; q < ns; ++q) {
@@ -324,194 +323,16 @@ __global__ void k_fill_subjobs(const int32_t* __restrict__ work, const int32_t* 
       it.pad = ns > 1 ? 1 : 0;
       jobs[suboff[k] + q] = it;
     }
-    if (k == nkeys - 1) hdr[hslot] = (int64_t)suboff[k] + ns;
+    if (k == nkeys - 1) hdr[1] = (int64_t)suboff[k] + ns;
   }
 }
 
-__global__ void k_subjob_keys(const Item* __restrict__ jobs, const int64_t* __restrict__ hdr, int hslot,
-                              int64_t max_jobs, int W, uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
-  const int64_t n = hdr[hslot];
+__global__ void k_subjob_keys(const Item* __restrict__ jobs, const int64_t* __restrict__ hdr, int64_t max_jobs, int W,
+                              uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+  const int64_t n = hdr[1];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < max_jobs; i += (int64_t)gridDim.x * blockDim.x) {
     keys[i] = i < n ? (uint32_t)(W - jobs[i].len) : (uint32_t)(W + 1);
     vals[i] = (int32_t)i;
-  }
-}
-
-// Coil-part adjoint lists: per 16 x 4 output tile (key = (t * an0 + ty) * an1
-// + tx), the points whose footprint reaches it, from the binning tiles that
-// hold footprint starts in rows oy - 5 .. oy + ext0 - 1 and columns
-// ox - 5 .. ox + 3 (at most three of each, listed once even when the range
-// wraps; the host's tile limits guarantee three suffice). One CTA per output
-// tile walks the candidates in source-tile, then sorted order, and keeps the
-// valid ones in that order (a block-wide scan of per-thread counts); the
-// first pass (voff == nullptr) counts. Entry: {sorted point index, m,
-// (ry + 5) | (rx + 5) << 8, 0}, offsets relative to the output tile's origin
-// (negative when the footprint starts before it; periodic).
-__global__ void __launch_bounds__(kValidThreads) k_atile_valid(Geo<float> geo, int an0, int an1,
-                                                              const int32_t* __restrict__ counts,
-                                                              const int32_t* __restrict__ tile_off,
-                                                              const float* __restrict__ tm,
-                                                              const int32_t* __restrict__ vals, int64_t n, int64_t M,
-                                                              int64_t nkeys, const int32_t* __restrict__ voff,
-                                                              int32_t* __restrict__ vcount, int4* __restrict__ vlist) {
-  constexpr int MAXS = 3, MAXC = MAXS * MAXS;
-  __shared__ int s_start[MAXC], s_pre[MAXC + 1], s_warp[kValidThreads / 32], s_nc;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int per_t = an0 * an1;
-  for (int64_t key = blockIdx.x; key < nkeys; key += gridDim.x) {
-    const int64_t t = key / per_t;
-    const int rem = (int)(key - t * per_t);
-    const int oy = (rem / an1) * kCpTY, ox = (rem % an1) * kCpTX;
-    const int ext[2] = {min(kCpTY, geo.K[0] - oy), min(kCpTX, geo.K[1] - ox)};
-    const int origin[2] = {oy, ox};
-    __syncthreads();  // the previous key is done with the shared lists
-    if (threadIdx.x == 0) {
-      int tr[MAXS], tc[MAXS], nr = 0, nc = 0;
-      for (int r = oy - 5; r < oy + ext[0]; ++r) {
-        const int tl = wrap_cell(r, geo.K[0]) / geo.T[0];
-        bool seen = false;
-        for (int q = 0; q < nr; ++q) seen = seen || tr[q] == tl;
-        if (!seen) {
-          if (nr < MAXS)
-            tr[nr++] = tl;
-          else
-            atomicOr(&g_status, kStatusBadItem);
-        }
-      }
-      for (int x = ox - 5; x < ox + ext[1]; ++x) {
-        const int tl = wrap_cell(x, geo.K[1]) / geo.T[1];
-        bool seen = false;
-        for (int q = 0; q < nc; ++q) seen = seen || tc[q] == tl;
-        if (!seen) {
-          if (nc < MAXS)
-            tc[nc++] = tl;
-          else
-            atomicOr(&g_status, kStatusBadItem);
-        }
-      }
-      int c = 0;
-      s_pre[0] = 0;
-      for (int a = 0; a < nr; ++a)
-        for (int b = 0; b < nc; ++b) {
-          const int64_t skey = t * geo.ntiles + (int64_t)tr[a] * geo.ntile[1] + tc[b];
-          s_start[c] = tile_off[skey];
-          s_pre[c + 1] = s_pre[c] + counts[skey];
-          ++c;
-        }
-      s_nc = c;
-    }
-    __syncthreads();
-    const int total = s_pre[s_nc];
-    const int64_t out0 = voff ? voff[key] : 0;
-    int cnt = 0;
-    for (int q0 = 0; q0 < total; q0 += 4 * kValidThreads) {
-      bool valid[4];
-      int idx[4], packed[4];
-      int mine = 0, l = 0;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int q = q0 + 4 * (int)threadIdx.x + k;
-        valid[k] = false;
-        idx[k] = packed[k] = 0;
-        if (q < total) {
-          while (s_pre[l + 1] <= q) ++l;
-          const int i = s_start[l] + (q - s_pre[l]);
-          bool v = true;
-          int r[2];
-#pragma unroll
-          for (int d = 0; d < 2; ++d) {
-            const float f = floorf(sub_rn(tm[d * n + i], geo.halfJ[d]));
-            const bool fin = fabsf(f) < 1073741824.f;
-            const int w = fin ? wrap_cell(1 + (int)f, geo.K[d]) : 0;
-            int rr = w - origin[d];
-            if (rr >= (d == 0 ? kCpTY : kCpTX)) rr -= geo.K[d];
-            v = v && fin && (rr > -6) && (rr < ext[d]);
-            r[d] = rr;
-          }
-          valid[k] = v;
-          idx[k] = i;
-          packed[k] = (r[0] + 5) | ((r[1] + 5) << 8);
-          mine += v ? 1 : 0;
-        }
-      }
-      int incl = mine;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-      }
-      if (lane == 31) s_warp[warp] = incl;
-      __syncthreads();
-      int before = 0, chunk = 0;
-#pragma unroll
-      for (int w = 0; w < kValidThreads / 32; ++w) {
-        const int c = s_warp[w];
-        before += w < warp ? c : 0;
-        chunk += c;
-      }
-      if (voff) {
-        int pos = cnt + before + incl - mine;
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          if (valid[k]) vlist[out0 + pos++] = make_int4(idx[k], (int)(vals[idx[k]] - t * M), packed[k], 0);
-      }
-      cnt += chunk;
-      __syncthreads();  // s_warp is rewritten by the next chunk
-    }
-    if (!voff && threadIdx.x == 0) vcount[key] = cnt;
-  }
-}
-
-// Rank of every coil-part list entry within its 32-entry group (groups start
-// at each tile list's first entry) when the group is sorted by footprint start
-// row, stable: stored in bits 16.. of the entry's third word. The fourth word
-// of list entry l of a group holds the start-row key (ry + 5) of sorted slot l
-// (31 past the group's end). One warp per group, 8 warps per CTA.
-__global__ void __launch_bounds__(256) k_atile_rank(int64_t nkeys, const int32_t* __restrict__ voff,
-                                                    const int32_t* __restrict__ vcount, int4* __restrict__ vlist) {
-  __shared__ int s_key[8][32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int wpb = blockDim.x / 32;
-  for (int64_t key = blockIdx.x; key < nkeys; key += gridDim.x) {
-    const int cnt = vcount[key];
-    const int64_t base = voff[key];
-    for (int g = warp; g * kCpGroup < cnt; g += wpb) {
-      const int64_t q = base + (int64_t)g * kCpGroup + lane;
-      const bool act = g * kCpGroup + lane < cnt;
-      int4 e = make_int4(0, 0, 0, 0);
-      int k = 31;
-      if (act) {
-        e = vlist[q];
-        k = e.z & 0xff;
-      }
-      int less = 0;
-      for (int v = 0; v < kCpTY + 5; ++v) {
-        const int c = __popc(__ballot_sync(0xffffffffu, k == v));
-        less += v < k ? c : 0;
-      }
-      const unsigned peers = __match_any_sync(0xffffffffu, k);
-      const int rank = less + __popc(peers & ((1u << lane) - 1u));
-      s_key[warp][lane] = 31;
-      __syncwarp();
-      if (act) s_key[warp][rank] = k;
-      __syncwarp();
-      if (act) {
-        e.z = (e.z & 0xffff) | (rank << 16);
-        e.w = s_key[warp][lane];
-        vlist[q] = e;
-      }
-      __syncwarp();
-    }
-  }
-}
-
-// Sub-job count of each coil-part output tile: its list in pieces of at most W entries.
-__global__ void k_atile_work(const int32_t* __restrict__ vcount, int64_t nkeys, int W, int32_t* __restrict__ work,
-                             int32_t* __restrict__ nsub) {
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nkeys; k += (int64_t)gridDim.x * blockDim.x) {
-    const int w = vcount[k];
-    work[k] = w;
-    nsub[k] = w > W ? (w + W - 1) / W : 1;
   }
 }
 
@@ -699,44 +520,7 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   L->ksort = false;
   L->csort = L->vlist && g->dtype == TKBN_C64 && j6 && regtile && L->adj_chunk % tkbn::kListChunk == 0 &&
              L->knk <= tkbn::kSortMaxKeys;
-  // coil-part adjoint tiling (16 x 4 output tiles): complex64, J = 6, K1 a
-  // multiple of 4, grids of at least one tile plus a footprint, and binning
-  // tiles of at least 16 x 9 cells (an output tile's footprint starts then
-  // lie in at most three binning rows and three binning columns)
-  L->atile = g->ndim == 2 && g->dtype == TKBN_C64 && j6 &&
-             !(g->flags & (TKBN_LAYOUT_FORWARD_ONLY | TKBN_ADJ_DETERMINISTIC)) &&
-             g->grid_size[1] % tkbn::kCpTX == 0 && g->grid_size[0] >= tkbn::kCpTY + 5 &&
-             g->grid_size[1] >= tkbn::kCpTX + 5 && L->tile[0] >= 16 && L->tile[1] >= 9;
-  if (L->atile) {
-    L->antile[0] = (int)((g->grid_size[0] + tkbn::kCpTY - 1) / tkbn::kCpTY);
-    L->antile[1] = (int)(g->grid_size[1] / tkbn::kCpTX);
-    L->natile = (int64_t)p->ntraj * L->antile[0] * L->antile[1];
-    // a footprint meets at most 3 output columns and 2 output rows (3 when
-    // the last row of tiles has fewer than 5 rows)
-    const int lastr = (int)(g->grid_size[0] % tkbn::kCpTY);
-    const int nr = (lastr != 0 && lastr < 5) ? 3 : 2;
-    L->max_valid_a = (int64_t)nr * 3 * L->npts_total;
-    L->max_subjobs_a = L->natile + L->max_valid_a / tkbn::kCpSubjob + 1;
-    if (L->natile >= (int64_t)1 << 31 || L->max_valid_a >= (int64_t)1 << 31) L->atile = false;
-  }
-  if (!L->atile) {
-    L->antile[0] = L->antile[1] = 0;
-    L->natile = L->max_valid_a = L->max_subjobs_a = 0;
-  }
-  {
-    int ab = 1;
-    while (((int64_t)1 << ab) <= tkbn::kCpSubjob + 1) ++ab;
-    L->asj_key_bits = ab;
-  }
-  if (L->atile) {
-    size_t c1 = 0, c2 = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, c1, (uint32_t*)nullptr, (uint32_t*)nullptr, (int32_t*)nullptr,
-                                    (int32_t*)nullptr, (int)L->max_subjobs_a, 0, L->asj_key_bits);
-    cub::DeviceScan::ExclusiveSum(nullptr, c2, (int32_t*)nullptr, (int32_t*)nullptr, (int)L->natile);
-    if (c1 > L->cub_bytes) L->cub_bytes = c1;
-    if (c2 > L->cub_bytes) L->cub_bytes = c2;
-  }
-  L->pfac = (L->csort || L->atile) && g->ndim == 2;
+  L->pfac = L->csort && g->ndim == 2;
   L->lfix = L->csort && g->ndim == 3;
   L->koff_rows = L->ksort ? L->nkeys : (L->csort ? L->max_valid / tkbn::kListChunk + L->nkeys + 1 : 0);
   L->max_subjobs = 2 * L->nkeys + (L->span.ncombo * L->npts_total + L->adj_chunk - 1) / L->adj_chunk;
@@ -813,32 +597,6 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   o = align_up(o + (L->pfac ? (size_t)L->npts_total * 12 * 8 + 512 : 0));  // + linear-phase tables
   L->off_lfix = o;
   o = align_up(o + (L->lfix ? (size_t)4 * L->npts_total + 64 : 0));
-  L->off_avcount = o;
-  o = align_up(o + 4 * L->natile);
-  L->off_avoff = o;
-  o = align_up(o + 4 * (L->natile + 1));
-  L->off_avlist = o;
-  o = align_up(o + sizeof(int4) * L->max_valid_a);
-  L->off_arec = o;
-  o = align_up(o + (size_t)64 * L->max_valid_a);
-  L->off_awork = o;
-  o = align_up(o + 4 * L->natile);
-  L->off_ansub = o;
-  o = align_up(o + 4 * L->natile);
-  L->off_asuboff = o;
-  o = align_up(o + 4 * (L->natile + 1));
-  L->off_asj_raw = o;
-  o = align_up(o + sizeof(tkbn::Item) * L->max_subjobs_a);
-  L->off_ajobs = o;
-  o = align_up(o + sizeof(tkbn::Item) * L->max_subjobs_a);
-  L->off_ask_in = o;
-  o = align_up(o + 4 * L->max_subjobs_a);
-  L->off_ask = o;
-  o = align_up(o + 4 * L->max_subjobs_a);
-  L->off_asv_in = o;
-  o = align_up(o + 4 * L->max_subjobs_a);
-  L->off_asv = o;
-  o = align_up(o + 4 * L->max_subjobs_a);
   L->off_coords = o;
   o = align_up(o + rsize * g->ndim * n);
   L->off_phase = o;
@@ -949,9 +707,8 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
     tb = L.cub_bytes;
     if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, nsub, suboff, (int)L.nkeys, s) != cudaSuccess)
       return set_error(TKBN_ERR_CUDA, "scan failed");
-    k_fill_subjobs<<<blocks_for(L.nkeys), threads, 0, s>>>(work, nsub, suboff, L.nkeys, L.adj_chunk, sj_raw, hdr,
-                                                           1);
-    k_subjob_keys<<<blocks_for(L.max_subjobs), threads, 0, s>>>(sj_raw, hdr, 1, L.max_subjobs, L.adj_chunk, sk_in,
+    k_fill_subjobs<<<blocks_for(L.nkeys), threads, 0, s>>>(work, nsub, suboff, L.nkeys, L.adj_chunk, sj_raw, hdr);
+    k_subjob_keys<<<blocks_for(L.max_subjobs), threads, 0, s>>>(sj_raw, hdr, L.max_subjobs, L.adj_chunk, sk_in,
                                                                  sv_in);
     tb = L.cub_bytes;
     if (cub::DeviceRadixSort::SortPairs(cubtmp, tb, sk_in, sk, sv_in, sv, (int)L.max_subjobs, 0, L.sj_key_bits, s) !=
@@ -959,45 +716,6 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
       return set_error(TKBN_ERR_CUDA, "sub-job sort failed");
     k_gather_items<<<blocks_for(L.max_subjobs), threads, 0, s>>>(sj_raw, sv, L.max_subjobs,
                                                                   (Item*)(ws + L.off_adj_jobs));
-  }
-  // coil-part adjoint: per 16 x 4 output tile lists, group ranks, sub-jobs
-  if constexpr (std::is_same<R, float>::value) {
-    if (L.atile) {
-      int32_t* avcount = (int32_t*)(ws + L.off_avcount);
-      int32_t* avoff = (int32_t*)(ws + L.off_avoff);
-      int4* avlist = (int4*)(ws + L.off_avlist);
-      const int ablocks = (int)(L.natile < 152 * 8 ? L.natile : 152 * 8);
-      k_atile_valid<<<ablocks, kValidThreads, 0, s>>>(geo, L.antile[0], L.antile[1], counts, tile_off, coords, vals,
-                                                      n, p->npts, L.natile, nullptr, avcount, avlist);
-      tb = L.cub_bytes;
-      if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, avcount, avoff, (int)L.natile, s) != cudaSuccess)
-        return set_error(TKBN_ERR_CUDA, "scan failed");
-      k_atile_valid<<<ablocks, kValidThreads, 0, s>>>(geo, L.antile[0], L.antile[1], counts, tile_off, coords, vals,
-                                                      n, p->npts, L.natile, avoff, avcount, avlist);
-      k_atile_rank<<<ablocks, 256, 0, s>>>(L.natile, avoff, avcount, avlist);
-      int32_t* work = (int32_t*)(ws + L.off_awork);
-      int32_t* nsub = (int32_t*)(ws + L.off_ansub);
-      int32_t* suboff = (int32_t*)(ws + L.off_asuboff);
-      Item* sj_raw = (Item*)(ws + L.off_asj_raw);
-      uint32_t* sk_in = (uint32_t*)(ws + L.off_ask_in);
-      uint32_t* sk = (uint32_t*)(ws + L.off_ask);
-      int32_t* sv_in = (int32_t*)(ws + L.off_asv_in);
-      int32_t* sv = (int32_t*)(ws + L.off_asv);
-      k_atile_work<<<blocks_for(L.natile), threads, 0, s>>>(avcount, L.natile, kCpSubjob, work, nsub);
-      tb = L.cub_bytes;
-      if (cub::DeviceScan::ExclusiveSum(cubtmp, tb, nsub, suboff, (int)L.natile, s) != cudaSuccess)
-        return set_error(TKBN_ERR_CUDA, "scan failed");
-      k_fill_subjobs<<<blocks_for(L.natile), threads, 0, s>>>(work, nsub, suboff, L.natile, kCpSubjob, sj_raw, hdr,
-                                                              2);
-      k_subjob_keys<<<blocks_for(L.max_subjobs_a), threads, 0, s>>>(sj_raw, hdr, 2, L.max_subjobs_a, kCpSubjob,
-                                                                     sk_in, sv_in);
-      tb = L.cub_bytes;
-      if (cub::DeviceRadixSort::SortPairs(cubtmp, tb, sk_in, sk, sv_in, sv, (int)L.max_subjobs_a, 0,
-                                          L.asj_key_bits, s) != cudaSuccess)
-        return set_error(TKBN_ERR_CUDA, "sub-job sort failed");
-      k_gather_items<<<blocks_for(L.max_subjobs_a), threads, 0, s>>>(sj_raw, sv, L.max_subjobs_a,
-                                                                      (Item*)(ws + L.off_ajobs));
-    }
   }
   return check_cuda(cudaGetLastError(), "points build launch");
 }

@@ -11,10 +11,6 @@ namespace tkbn {
 // Entries of a tile's point list staged per adjoint batch (2D register adjoint).
 constexpr int kListChunk = 256;
 
-// Coil-part adjoint (interp_cp.cu): output tiles of kCpTY rows x kCpTX columns,
-// lists staged kCpGroup entries at a time, sub-jobs of at most kCpSubjob entries.
-constexpr int kCpTY = 16, kCpTX = 4, kCpGroup = 32, kCpSubjob = 512;
-
 constexpr int kMaxDim = 3;
 constexpr int kMaxJ = 8;  // numpoints supported per dimension
 
@@ -274,21 +270,6 @@ struct PointsLayout {
   // 3D chunk-sorted layouts: list of points the linear-phase adjoint leaves
   // out (count first, then indices)
   bool lfix;
-  // 2D complex64 J = 6 layouts whose grid has K1 % 4 == 0: a second output
-  // tiling for the coil-part adjoint (interp_cp.cu), 16 rows x 4 columns,
-  // with per output tile the list of points whose footprint reaches it
-  // ({factor index, m, packed (ry + 5, rx + 5, rank), slot key} in
-  // source-tile then sorted order; rank = the entry's position in its
-  // 32-entry group sorted by ry; slot key = the start-row key of sorted slot
-  // l of the group), sub-jobs of at most kCpSubjob entries (hdr[2] of them),
-  // and room for the entries' linear-phase records (64 bytes each, in
-  // sorted-slot order, written by the adjoint's factor pre-pass).
-  bool atile;
-  int antile[2];
-  int64_t natile, max_valid_a, max_subjobs_a;
-  int asj_key_bits;
-  size_t off_avcount, off_avoff, off_avlist, off_arec, off_awork, off_ansub, off_asuboff, off_asj_raw, off_ajobs,
-      off_ask_in, off_ask, off_asv_in, off_asv;
   size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
       off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_phase,
       off_tile_work, off_tile_nsub, off_tile_suboff, off_sj_raw, off_adj_jobs, off_sj_keys_in, off_sj_keys,
@@ -298,17 +279,6 @@ struct PointsLayout {
 };
 
 int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayout* out);
-
-// The coil-part adjoint (interp_cp.cu): 2D complex64 linear-phase tables on a
-// layout with atile lists, at most 16 coils per job, 16-byte aligned grid.
-bool adj_cp_eligible(const PointsLayout& L, int64_t Cc, const void* grid);
-// Its per-entry records, from the per-point linear-phase factors (pfac) and
-// E tables (etab): part of the factor pre-pass, once per layout and tables.
-int adj_cp_records(const PointsLayout& L, const char* ws, const float2* pfac, const float2* etab, cudaStream_t s);
-// Launches it (split-tile zeroing, then the kernel) on records in place.
-int adj_cp_launch(const tkbn::Geo<float>& geo, const PointsLayout& L, const char* ws, const float2* etab, int64_t M,
-                  int64_t ntraj, int64_t B, int64_t C, int Cc, int ncc, int64_t nbpt, int64_t gtot,
-                  const void* kdata, void* grid, cudaStream_t s);
 
 // Default tile edge and chunk per dimension count.
 void default_tiles(const tkbn_geometry* g, int tile[3], int* chunk);
