@@ -40,6 +40,8 @@
  *   tkbn_fft_filter        fft_filter                   torchkbnufft/_nufft/fft.py:121-173
  *   tkbn_toep_apply        ToepNufft.forward / toep_batch_loop
  *                          torchkbnufft/modules/kbnufft.py:441-547
+ *   tkbn_toep_kernel_assemble  adjoint_flip_and_concat, reflect_conj_concat,
+ *                          hermitify  torchkbnufft/_nufft/toep.py:185-307
  *   tkbn_spmat_interp(_adjoint) spmat_interp / spmat_interp_adjoint
  *                          torchkbnufft/_nufft/interp.py:13-85
  *   tkbn_ragged_*          a loop of table_interp / table_interp_adjoint calls
@@ -255,6 +257,15 @@ int tkbn_fft_filter(const tkbn_geometry* g, tkbn_fft_plan plan, const void* imag
 int tkbn_toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, const void* kernel,
                     int64_t kernel_batch, const void* smaps, int64_t smaps_batch, int64_t nbatch, int64_t ncoil,
                     int norm, void* grid_scratch, void* out, void* stream);
+/* Toeplitz kernel assembly (calc_toeplitz_kernel's steps between its adjoint
+ * NUFFTs and its FFT, torchkbnufft/_nufft/toep.py:185-307): from
+ * parts[P][N0][N1]..., the 2^(ndim-1) adjoint NUFFT images of the weights at
+ * the trajectory with dims 1..ndim-1 sign-flipped (pattern p: bit ndim-1-d of
+ * p set when dim d is flipped, the order of the reference's recursion),
+ * writes out[2 N0][2 N1]... = scale * the Hermitian kernel before its FFT.
+ * dtype TKBN_C64 or TKBN_C128; out must not alias parts. */
+int tkbn_toep_kernel_assemble(int dtype, int ndim, const int64_t* im_size, const void* parts, double scale,
+                              void* out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -93,6 +93,7 @@ SIGNATURES = {
     "tkbn_nufft_adj": [_GP, _DP, _P, _P, _PP, _P, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P],
     "tkbn_fft_filter": [_GP, _P, _P, _P, _I64, _I64, _I64, _INT, _P, _P, _P],
     "tkbn_toep_apply": [_GP, _P, _P, _P, _I64, _P, _I64, _I64, _I64, _INT, _P, _P, _P],
+    "tkbn_toep_kernel_assemble": [_INT, _INT, _P, _P, ctypes.c_double, _P, _P],
     "tkbn_interp_fwd_noalloc": [_GP, _PP, _P, _I64, _P, _I64, _I64, _P, _P],
     "tkbn_spmat_interp": [_INT, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P],
     "tkbn_spmat_interp_adjoint": [_INT, _I64, _I64, _I64, _P, _P, _P, _P, _I64, _P, _P],

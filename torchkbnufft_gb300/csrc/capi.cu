@@ -30,6 +30,8 @@ int spmat_interp(int dtype, int64_t nrows, int64_t ncols, const int64_t* crow, c
                  const void* x, int64_t nplanes, void* y, cudaStream_t s);
 int spmat_interp_adjoint(int dtype, int64_t nrows, int64_t ncols, int64_t nnz, const int32_t* row, const int32_t* col,
                          const void* val, const void* y, int64_t nplanes, void* x, cudaStream_t s);
+int toep_assemble(int dtype, int ndim, const int64_t* im_size, const void* parts, double scale, void* out,
+                  cudaStream_t s);
 int ragged_plan_create(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan* out);
 int ragged_plan_destroy(tkbn_ragged_plan p);
 int ragged_interp_fwd(tkbn_ragged_plan p, cudaStream_t s);
@@ -185,6 +187,12 @@ int tkbn_toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* imag
   if (!smaps) return set_error(TKBN_ERR_INVALID, "smaps is null (use tkbn_fft_filter without maps)");
   TKBN_GUARD(toep_apply(g, plan, image, kernel, kernel_batch, 0, smaps, smaps_batch, nbatch, ncoil, norm,
                         grid_scratch, out, (cudaStream_t)stream));
+}
+
+int tkbn_toep_kernel_assemble(int dtype, int ndim, const int64_t* im_size, const void* parts, double scale,
+                              void* out, void* stream) {
+  if (parts && out && parts == out) return set_error(TKBN_ERR_INVALID, "out must not alias parts");
+  TKBN_GUARD(toep_assemble(dtype, ndim, im_size, parts, scale, out, (cudaStream_t)stream));
 }
 
 }  // extern "C"

@@ -3,18 +3,25 @@
 The kernel D satisfies ``F^H D F ~= A^H W A`` on the 2x-embedded grid. Its
 2^(d-1) sign-flipped adjoint NUFFTs of the weights (n_shift = 0) run as ONE
 batched adjoint call on the GPU (the flips become a batched trajectory),
-instead of the reference's recursion of separate calls; the Hermitian
-completion, symmetrisation and final FFT follow the reference's steps.
+instead of the reference's recursion of separate calls. The reference's
+flip-and-concatenate, conjugate-reflection and Hermitian-averaging steps
+(``toep.py:185-307``) are one CUDA kernel (``tkbn_toep_kernel_assemble``,
+each output cell read from at most two of the adjoint images, the scale
+folded in), and the final FFT runs through the library's FFT stage.
 """
 
 from __future__ import annotations
 
+import ctypes
 import itertools
+import math
 from typing import Optional, Sequence, Union
 
 import torch
 from torch import Tensor
 
+from . import _lib as L
+from . import _runtime as R
 from .modules import KbNufftAdjoint
 
 
@@ -73,59 +80,18 @@ def _one_kernel(omega, weights, im_size, norm, grid_size, numpoints, table_overs
     pats = _flip_patterns(nd)
     signs = torch.tensor(pats, dtype=omega.dtype, device=omega.device).unsqueeze(-1)  # (P, d, 1)
     om_b = signs * omega.unsqueeze(0)  # (P, d, M)
-    parts = adj(w.expand(len(pats), 1, M).contiguous(), om_b, norm=norm)  # (P, 1, *N)
-    lookup = {p: parts[i:i + 1] for i, p in enumerate(pats)}
+    parts = adj(w.expand(len(pats), 1, M).contiguous(), om_b, norm=norm).contiguous()  # (P, 1, *N)
 
-    def assemble(dim: int, flips: tuple) -> Tensor:
-        # mirrors adjoint_flip_and_concat (toep.py:185-237) without re-running adjoints
-        axis = dim + 2
-        if dim < nd - 1:
-            k1 = assemble(dim + 1, flips)
-            k2 = assemble(dim + 1, flips[:dim] + (-1,) + flips[dim + 1:])
-        else:
-            k1 = lookup[flips]
-            k2 = lookup[flips[:dim] + (-1,) + flips[dim + 1:]]
-        zshape = list(k1.shape)
-        zshape[axis] = 1
-        zero = torch.zeros(zshape, dtype=k1.dtype, device=k1.device)
-        k2 = k2.narrow(axis, 1, k2.shape[axis] - 1)
-        return torch.cat((k1, zero, k2.flip(axis)), axis)
-
-    kern = assemble(1, (1,) * nd) if nd > 1 else parts[0:1]
-    kern = _reflect_conj_concat(kern, 2)
-    kern = _hermitify(kern, 2)
-    im = adj.im_size.to(torch.float64)
-    gs = adj.grid_size.to(torch.float64)
+    geom = adj._geom(cdt)
+    im = geom.im_size
+    big = tuple(2 * n for n in im)
     if norm == "ortho":
-        scale = torch.sqrt(torch.prod(2 * im) / torch.prod(gs)).item()
+        scale = math.sqrt(math.prod(big) / math.prod(geom.grid_size))
     else:
-        scale = (1 / torch.prod(2 * im)).item()
-    dims = tuple(range(-nd, 0))
-    out = torch.fft.fftn(kern, dim=dims, norm="ortho" if norm == "ortho" else None)[0, 0] * scale
-    return out
-
-
-def _reverse_index(t: Tensor, d: int) -> Tensor:
-    n = t.shape[d]
-    idx = torch.remainder(-torch.arange(n, device=t.device), n)
-    return t.index_select(d, idx)
-
-
-def _reflect_conj_concat(kernel: Tensor, dim: int) -> Tensor:
-    """Append the conjugate point reflection along ``dim`` (``toep.py:240-274``)."""
-    tmp = kernel.conj()
-    for d in range(dim, kernel.ndim):
-        tmp = _reverse_index(tmp, d)
-    zshape = list(kernel.shape)
-    zshape[dim] = 1
-    zero = torch.zeros(zshape, dtype=kernel.dtype, device=kernel.device)
-    tmp = torch.cat((zero, tmp.narrow(dim, 1, tmp.shape[dim] - 1)), dim)
-    return torch.cat((kernel, tmp), dim)
-
-
-def _hermitify(kernel: Tensor, dim: int) -> Tensor:
-    """Average with the conjugate point reflection (``toep.py:277-307``)."""
-    rev = kernel
-    for d in range(dim, kernel.ndim):
-        rev = _reverse_index(rev, d)
-    return (kernel + rev.conj()) / 2
+        scale = 1.0 / math.prod(big)
+    kern = torch.empty((1, 1) + big, dtype=cdt, device=omega.device)
+    sizes = (ctypes.c_int64 * 3)(*im, *([1] * (3 - nd)))
+    L.check(L.lib().tkbn_toep_kernel_assemble(R.dtype_code(cdt), nd, ctypes.addressof(sizes), parts.data_ptr(),
+                                              scale, kern.data_ptr(), R.stream_handle(omega.device)))
+    fgeom = R.GeomKey(nd, R.dtype_code(cdt), big, big, (1,) * nd, (1,) * nd, (0.0,) * nd)
+    return R.fft_and_scale(fgeom, kern, None, None, norm)[0, 0]
