@@ -542,6 +542,17 @@ def run_ragged(args):
             out = rn.output_view(p)
             gate = max(gate, float((torch.linalg.vector_norm(out - ref) / torch.linalg.vector_norm(ref)).item()))
         plain_ms = timed(plain_step, args.steps, args.warmup)
+        # the same per-problem module calls captured as one CUDA graph: the
+        # plain path's GPU time without host launch gaps (its kernel floor)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            plain_step()
+        torch.cuda.current_stream().wait_stream(side)
+        pg = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(pg):
+            plain_step()
+        plain_graph_ms = timed(pg.replay, args.steps, args.warmup)
         eager_ms = timed(rn.forward_adjoint, args.steps, args.warmup)
         rn.capture()
         graph_ms = timed(rn.replay, args.steps, args.warmup)
@@ -562,7 +573,8 @@ def run_ragged(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
         "config": {"workload": "ragged batch: 64 problems, image 128/192/256/320 squared, grid 2x, 20k-400k points "
                                "(uniform random or variable-density spiral), 1-16 coil images, J=6, L=1024",
-                   "work_per_step": work, "plain_ms_per_step": plain_ms, "eager_ms_per_step": eager_ms,
+                   "work_per_step": work, "plain_ms_per_step": plain_ms,
+                   "plain_loop_graph_ms_per_step": plain_graph_ms, "eager_ms_per_step": eager_ms,
                    "graph_ms_per_step": graph_ms, "speedup_graph_vs_plain": plain_ms / graph_ms,
                    "tiles": {f"{k[0]}x{k[1]}": v for k, v in rn.tiles.items()},
                    "parity_gate_rel_l2_vs_per_problem": gate},
@@ -688,9 +700,10 @@ def run_config(args):
         desc = ("2D SENSE NUFFT fwd+adj in complex128, image 320x320, grid 640x640, J=6, L=1024, 16 coils, "
                 "batch 4, golden-angle 404x640 (258560 points)")
     elif w == "kooshball":
-        n, om, Bc, Cc = 128, kooshball_traj(20000, 256), 1, 8
+        sp = args.kooshball_spokes
+        n, om, Bc, Cc = 128, kooshball_traj(sp, 256), 1, 8
         smaps = torch.tensor(smooth_maps_3d(8, 128, 3), device=dev)
-        desc = "3D kooshball, image 128^3, grid 256^3, 8 coils, 20000x256 (5.12M points), batch 1"
+        desc = f"3D kooshball, image 128^3, grid 256^3, 8 coils, {sp}x256 ({sp * 256} points), batch 1"
     else:
         n, om, Bc, Cc = 256, spiral_traj(32, 2048), 8, 16
         smaps = torch.tensor(ring_smaps(16, 256, 1, 4)[:1], device=dev)
@@ -862,6 +875,8 @@ def main():
                         "own PyTorch path on the GPU (a second comparator)")
     p.add_argument("--device", default=None, help="device of the reference-gpu arm (default cuda)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--kooshball-spokes", type=int, default=20000,
+                   help="spokes of the kooshball workload (20000 is the configuration; fewer for a small profiling case)")
     p.add_argument("--workload", default="sense", choices=["sense", "ragged", "single", "kooshball", "spiral-grad", "sense-c128"],
                    help="sense: the metric's workload (default); the others are reported beside it")
     args = p.parse_args()
