@@ -87,22 +87,24 @@ extern "C" {
 #define TKBN_TABLES_LINEAR_PHASE 8   /* every table is |table[k]| exp(i c (k - J*L/2) / L) to
                                         within float rounding, with c = 2 arg(table[J*L/2 + L/2])
                                         (true for KB tables: the fftshift phase is linear in the
-                                        distance); the complex64 2D register adjoint then works
-                                        with real kernel values and applies the phases per point
-                                        and per tile cell. Set only after checking the tables. */
+                                        distance); the complex64 2D gather and register adjoint
+                                        then work with real kernel values and apply the phases
+                                        per point and per tile cell or patch cell. Set only
+                                        after checking the tables. */
 #define TKBN_LAYOUT_FORWARD_ONLY 4   /* layout without the adjoint's per-tile point lists
                                         (smaller workspace, for forward-only callers); an
                                         adjoint on it scans candidates instead (slower). Must
                                         be the same in tkbn_points_build and every call that
                                         uses the layout. */
-#define TKBN_ADJ_REUSE_FACTORS 16    /* tkbn_interp_adj / tkbn_nufft_adj only: the workspace
-                                        still holds the per-point table factors that an earlier
-                                        adjoint call on it computed, with the same tables (same
-                                        contents at the same addresses) and the same other
-                                        flags, so this call does not recompute them. They
-                                        depend on the trajectory and the tables only, not on
-                                        the k-space data. No other call writes them; a new
-                                        tkbn_points_build invalidates them. A call captured
+#define TKBN_ADJ_REUSE_FACTORS 16    /* tkbn_interp_fwd / tkbn_interp_adj / tkbn_nufft_fwd /
+                                        tkbn_nufft_adj: the workspace still holds the per-point
+                                        table factors that an earlier forward or adjoint call on
+                                        it computed, with the same tables (same contents at the
+                                        same addresses) and the same other flags, so this call
+                                        does not recompute them. They depend on the trajectory
+                                        and the tables only, not on the grid or k-space data.
+                                        No other call writes them; a new tkbn_points_build
+                                        invalidates them. A call captured
                                         into a CUDA graph that sets it makes the graph depend
                                         on the factors staying in place; leave it unset there
                                         and the graph recomputes them on every replay. */
@@ -142,14 +144,19 @@ int tkbn_points_build(const tkbn_geometry* g, const tkbn_points_desc* p, const v
                       void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---- interpolation ------------------------------------------------------ */
-/* kdata = interp(grid): gather of J^d neighbours per point, times the fftshift phase. */
+/* kdata = interp(grid): gather of J^d neighbours per point, times the fftshift phase.
+ * With 2D complex64 J = 6 layouts of 16 x 14 tiles the call fills the workspace's
+ * per-point factor scratch as tkbn_interp_adj does (unless TKBN_ADJ_REUSE_FACTORS),
+ * and with TKBN_TABLES_LINEAR_PHASE the coil-pair gather reads it, so forward and
+ * adjoint calls that share one workspace must be ordered (one stream). */
 int tkbn_interp_fwd(const tkbn_geometry* g, const tkbn_points_desc* p, const void* workspace,
                     const void* const* tables, const void* grid, int64_t nbatch, int64_t ncoil,
                     void* kdata, void* stream);
 /* grid = interp^H(kdata). grid is fully overwritten (zeroed first). With 2D
  * complex64 J = 6 layouts of 16 x 14 tiles the call also fills a per-point
- * scratch region inside the workspace (the table factors), so adjoint calls
- * that share one workspace must be ordered (one stream). */
+ * scratch region inside the workspace (the table factors; unless
+ * TKBN_ADJ_REUSE_FACTORS), so forward and adjoint calls that share one
+ * workspace must be ordered (one stream). */
 int tkbn_interp_adj(const tkbn_geometry* g, const tkbn_points_desc* p, const void* workspace,
                     const void* const* tables, const void* kdata, int64_t nbatch, int64_t ncoil,
                     void* grid, void* stream);

@@ -133,9 +133,9 @@ def test_linear_phase_table_check():
     assert not R._linear_phase(t.to(torch.complex128))  # the linear-phase kernels are complex64
 
 
-def test_adjoint_factor_reuse_key():
-    """An adjoint reuses the layout's per-point factors only for the very table
-    tensors (unmodified) and table flags they were computed with."""
+def test_factor_reuse_key():
+    """A call reuses the layout's per-point factors only for tables with the
+    contents (unmodified since) and table flags they were computed with."""
     import torch
 
     from torchkbnufft_gb300 import _runtime as R
@@ -145,7 +145,11 @@ def test_adjoint_factor_reuse_key():
     assert R.factors_reusable(stored, [a, b], 9)
     assert not R.factors_reusable(None, [a, b], 9)
     assert not R.factors_reusable(stored, [a, b], 1)  # other table flags
-    assert not R.factors_reusable(stored, [a, a.clone()], 9)  # same contents, another tensor
+    assert R.factors_reusable(stored, [a, b.clone()], 9)  # same contents, another tensor
+    other = b.clone()
+    other[0] = 2
+    assert not R.factors_reusable(stored, [a, other], 9)  # other contents
+    assert not R.factors_reusable(stored, [a, torch.ones(6, dtype=torch.complex64)], 9)
     assert not R.factors_reusable(stored, [a], 9)
     a.mul_(2)
     assert not R.factors_reusable(stored, [a, b], 9)  # changed in place
@@ -172,7 +176,7 @@ def test_missing_library_raises_instead_of_falling_back():
     assert "raised: CUDA library not built" in out.stdout and "raised: OSError" in out.stdout, out.stdout
 
 
-def test_adjoint_factor_reuse_is_off_under_graph_capture(monkeypatch):
+def test_factor_reuse_is_off_under_graph_capture(monkeypatch):
     """A call captured into a CUDA graph always carries the pre-pass and leaves
     no record (nothing ran at capture time); eager calls reuse as before."""
     import torch
@@ -186,13 +190,13 @@ def test_adjoint_factor_reuse_is_off_under_graph_capture(monkeypatch):
     seen = []
     capturing = [False]
     monkeypatch.setattr(R, "stream_capturing", lambda device: capturing[0])
-    lay.adjoint_call(tabs, 9, seen.append)  # eager: computes, records
-    lay.adjoint_call(tabs, 9, seen.append)  # eager: reuses
+    lay.factor_call(tabs, 9, seen.append)  # eager: computes, records
+    lay.factor_call(tabs, 9, seen.append)  # eager: reuses
     capturing[0] = True
-    lay.adjoint_call(tabs, 9, seen.append)  # captured: recomputes, no record
+    lay.factor_call(tabs, 9, seen.append)  # captured: recomputes, no record
     capturing[0] = False
-    lay.adjoint_call(tabs, 9, seen.append)  # eager after capture: recomputes
-    lay.adjoint_call(tabs, 9, seen.append)  # and reuses again
+    lay.factor_call(tabs, 9, seen.append)  # eager after capture: recomputes
+    lay.factor_call(tabs, 9, seen.append)  # and reuses again
     reuse = [bool(f & L.TKBN_ADJ_REUSE_FACTORS) for f in seen]
     assert reuse == [False, True, False, False, True]
     assert all(f & ~L.TKBN_ADJ_REUSE_FACTORS == 9 for f in seen)

@@ -340,8 +340,9 @@ def test_specialised_kernels_are_selected(case, tmp_path):
     want = "k_interp_adj_reg3" if case == "3d8" else "k_interp_adj_reg<"
     assert any(want in n for n in names), names
     if case != "3d8":
+        # the linear-phase form of the coil-pair gather
         names = _kernels_launched(lambda: R.interp_fwd(geom, lay, tables, grid), tmp_path)
-        assert any("k_interp_fwd_pairs" in n for n in names), names
+        assert any("k_interp_fwd_pairs<" in n and "true>" in n for n in names), names
 
 
 def _bins_mismatched(om, op, K):
@@ -424,3 +425,69 @@ def test_adjoint_factor_reuse_follows_the_tables(tmp_path):
         a1.table_0.mul_(2)
     assert prepass_launched(a1)
     assert rel_l2(run(a1), ref1b) < TOL64
+
+
+@pytest.mark.parametrize("C", [16, 4])
+@pytest.mark.parametrize("subset", ["centre_heavy", "left_out_only"])
+def test_linear_phase_gather_exact_pass(C, subset, tmp_path):
+    """The linear-phase coil-pair gather works with real kernel values on a
+    patch multiplied by the E tables; points whose table bins do not step by
+    exactly L get their exact values from a second pass (k_fwd_lp_fix). Cases:
+    3/4 of the points near the k-space centre, and only the left-out points."""
+    gen = torch.Generator().manual_seed(43)
+    K, M = (160, 144), 30000
+    grid = _rand(gen, (2, C) + K, torch.complex64)
+    om = _traj(gen, (2, M)).float()
+    om[..., : 3 * M // 4] *= 0.01
+    op = O.Operator(K, K, cdtype=np.complex64)
+    if subset == "left_out_only":
+        per_dim = _bins_mismatched(om.numpy(), op, K)
+        assert all(m.any() for m in per_dim), [int(m.sum()) for m in per_dim]
+        om = om[:, torch.tensor(np.any(per_dim, axis=0))].contiguous()
+    fwd = tkbn().KbInterp(im_size=K, grid_size=K, dtype=torch.complex64, device=DEV)
+    gd, omd = grid.to(DEV), om.to(DEV)
+    names = _kernels_launched(lambda: fwd(gd, omd), tmp_path)
+    assert any("k_fwd_lp_fix" in n for n in names), names
+    assert any("k_interp_fwd_pairs<" in n and "true>" in n for n in names), names
+    assert rel_l2(_np(fwd(gd, omd)), op.interp(grid.numpy(), om.numpy())) < TOL64
+
+
+def test_factor_reuse_between_forward_and_adjoint(tmp_path):
+    """Forward and adjoint calls on one layout share its per-point factor
+    scratch: whichever runs first fills it, the other reuses it for the same
+    tables, and another table set (or a table changed in place) recomputes it.
+    Every result matches the oracle for its own tables."""
+    from torchkbnufft_gb300 import _runtime as R
+
+    gen = torch.Generator().manual_seed(53)
+    K, C, M = (96, 84), 4, 6000
+    grid = _rand(gen, (1, C) + K, torch.complex64)
+    y = _rand(gen, (1, C, M), torch.complex64)
+    om = _traj(gen, (2, M)).float()
+    f1 = tkbn().KbInterp(im_size=K, grid_size=K, device=DEV)
+    a1 = tkbn().KbInterpAdjoint(im_size=K, grid_size=K, device=DEV)
+    f2 = tkbn().KbInterp(im_size=K, grid_size=K, kbwidth=2.0, device=DEV)
+    o1 = O.Operator(K, K, cdtype=np.complex64)
+    o2 = O.Operator(K, K, kbwidth=2.0, cdtype=np.complex64)
+    gd, yd, omd = grid.to(DEV), y.to(DEV), om.to(DEV)
+    R._layout_cache.clear()
+
+    def prepass(fn):
+        names = _kernels_launched(fn, tmp_path)
+        return any("k_point_factors2" in n for n in names)
+
+    assert prepass(lambda: f1(gd, omd))  # a new layout: the forward fills the scratch
+    assert rel_l2(_np(f1(gd, omd)), o1.interp(grid.numpy(), om.numpy())) < TOL64
+    assert not prepass(lambda: a1(yd, omd))  # the adjoint reuses the forward's factors
+    assert rel_l2(_np(a1(yd, omd)), o1.interp_adj(y.numpy(), om.numpy())) < TOL64
+    assert prepass(lambda: f2(gd, omd))  # other tables on the same layout
+    assert rel_l2(_np(f2(gd, omd)), o2.interp(grid.numpy(), om.numpy())) < TOL64
+    assert prepass(lambda: a1(yd, omd))
+    assert not prepass(lambda: f1(gd, omd))
+    assert rel_l2(_np(f1(gd, omd)), o1.interp(grid.numpy(), om.numpy())) < TOL64
+    with torch.no_grad():
+        f1.table_0.mul_(2)
+    assert prepass(lambda: f1(gd, omd))
+    want = O.interp_forward(grid.numpy(), om.numpy(), [o1.tables[0] * 2, o1.tables[1]], o1.n_shift, o1.numpoints,
+                            o1.table_oversamp)
+    assert rel_l2(_np(f1(gd, omd)), want) < TOL64

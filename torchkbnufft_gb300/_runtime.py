@@ -193,7 +193,7 @@ class PointsLayout:
         self.workspace = torch.empty(self.nbytes, dtype=torch.uint8, device=self.device)
         om = omega.detach().to(real_of(torch.complex64 if geom.dtype == L.TKBN_C64 else torch.complex128)).contiguous()
         self._omega_keepalive = om
-        # (tables, their versions, table flags) whose per-point adjoint factors
+        # (tables, their versions, table flags) whose per-point table factors
         # the workspace holds, or None; the tables are kept alive, so identity
         # and version pin their contents
         self._factors = None
@@ -203,27 +203,29 @@ class PointsLayout:
         )
         # cross-stream ordering: the build's stream, an event after the build,
         # the streams already ordered after it, and the stream of the last
-        # adjoint (adjoints write the per-point factor scratch in the workspace)
+        # interpolation call (forward and adjoint calls may write the per-point
+        # factor scratch in the workspace)
         build_stream = torch.cuda.current_stream(self.device)
         self._built = None
         self._ready_streams = {build_stream.cuda_stream}
-        self._adj_stream = build_stream
+        self._factor_stream = build_stream
         if not stream_capturing(self.device):
             self._built = torch.cuda.Event()
             self._built.record(build_stream)
 
-    def stream_for_call(self, adjoint: bool) -> int:
+    def stream_for_call(self, writes_factors: bool) -> int:
         """Orders a call on torch's current stream after the work it depends on
         and returns that stream's handle.
 
         Every call waits (once per stream) for the layout build when it runs
         on another stream than the build, and the workspace is marked as used
         by that stream, so the caching allocator keeps it until the stream's
-        work is done even after the layout is evicted. Adjoint calls also wait
-        for the last adjoint on this layout when that ran on another stream:
-        they write and read the per-point factor scratch. Forward calls only
-        read what the build wrote. Under CUDA graph capture nothing is added
-        (a captured sequence is ordered by its own stream)."""
+        work is done even after the layout is evicted. Forward and adjoint
+        interpolation calls (``writes_factors``) also wait for the last such
+        call on this layout when that ran on another stream: they write and
+        read the per-point factor scratch. Trajectory-gradient calls only read
+        what the build wrote. Under CUDA graph capture nothing is added (a
+        captured sequence is ordered by its own stream)."""
         s = torch.cuda.current_stream(self.device)
         h = s.cuda_stream
         if stream_capturing(self.device):
@@ -234,19 +236,20 @@ class PointsLayout:
                     s.wait_event(self._built)
                 self.workspace.record_stream(s)
                 self._ready_streams.add(h)
-            if adjoint:
-                prev = self._adj_stream
+            if writes_factors:
+                prev = self._factor_stream
                 if prev is not None and prev.cuda_stream != h:
                     ev = torch.cuda.Event()
                     ev.record(prev)
                     s.wait_event(ev)
-                self._adj_stream = s
+                self._factor_stream = s
         return h
 
-    def adjoint_call(self, tables: Sequence[torch.Tensor], table_flags: int, call) -> None:
-        """Runs ``call(flags)``, an adjoint entry point on this layout's workspace,
-        with the layout's flags and TKBN_ADJ_REUSE_FACTORS when the workspace
-        holds the factors of these same, unmodified table tensors. The record
+    def factor_call(self, tables: Sequence[torch.Tensor], table_flags: int, call) -> None:
+        """Runs ``call(flags)``, a forward or adjoint entry point on this layout's
+        workspace (either may fill the per-point factor scratch), with the
+        layout's flags and TKBN_ADJ_REUSE_FACTORS when the workspace holds the
+        factors of these same, unmodified table tensors. The record
         and the enqueue happen under one lock, so threads sharing a cached
         layout keep the record in the order their calls reach the stream.
 
@@ -277,13 +280,27 @@ def stream_capturing(device: torch.device) -> bool:
 
 
 def factors_reusable(stored, tables: Sequence[torch.Tensor], table_flags: int) -> bool:
-    """True when ``stored`` (tables, versions, flags) names exactly these table
-    tensors, none modified since, with the same table flags."""
+    """True when ``stored`` (tables, versions, flags) names tables with these
+    contents, none modified since, with the same table flags. A table tensor
+    other than the stored one counts when its contents are equal (a forward and
+    an adjoint module hold separate copies of the same tables); that comparison
+    is cached per pair of tensors and versions."""
     if stored is None:
         return False
     tabs, versions, flags = stored
-    return (flags == table_flags and len(tabs) == len(tables) and
-            all(a is b and b._version == v for a, b, v in zip(tabs, tables, versions)))
+    if flags != table_flags or len(tabs) != len(tables):
+        return False
+    for a, b, v in zip(tabs, tables, versions):
+        if a._version != v:
+            return False
+        if a is b:
+            continue
+        same = _cached_prop(("eq", id(b), b._version, b.data_ptr(), a.data_ptr(), a._version), b,
+                            lambda: (a.shape == b.shape and a.dtype == b.dtype and a.device == b.device
+                                     and bool(torch.equal(a, b))))
+        if not same:
+            return False
+    return True
 
 
 _layout_cache: "collections.OrderedDict" = collections.OrderedDict()
@@ -527,9 +544,9 @@ def interp_fwd(geom: GeomKey, lay: PointsLayout, tables, grid: torch.Tensor) -> 
     B, C = grid.shape[:2]
     kdata = torch.empty((B, C, lay.npts), dtype=grid.dtype, device=dev)
     tp, keep, fl = table_ptrs(tables, grid.dtype)
-    L.check(L.lib().tkbn_interp_fwd(ctypes.byref(geom_struct(geom, fl | lay.flags)), ctypes.byref(lay.desc),
-                                    lay.workspace.data_ptr(), tp, grid.data_ptr(), B, C, kdata.data_ptr(),
-                                    lay.stream_for_call(False)))
+    lay.factor_call(keep, fl, lambda flags: L.check(L.lib().tkbn_interp_fwd(
+        ctypes.byref(geom_struct(geom, flags)), ctypes.byref(lay.desc), lay.workspace.data_ptr(), tp,
+        grid.data_ptr(), B, C, kdata.data_ptr(), lay.stream_for_call(True))))
     return kdata
 
 
@@ -540,7 +557,7 @@ def interp_adj(geom: GeomKey, lay: PointsLayout, tables, kdata: torch.Tensor) ->
     B, C = kdata.shape[:2]
     grid = torch.empty((B, C) + geom.grid_size, dtype=kdata.dtype, device=dev)
     tp, keep, fl = table_ptrs(tables, kdata.dtype)
-    lay.adjoint_call(keep, fl, lambda flags: L.check(L.lib().tkbn_interp_adj(
+    lay.factor_call(keep, fl, lambda flags: L.check(L.lib().tkbn_interp_adj(
         ctypes.byref(geom_struct(geom, flags)), ctypes.byref(lay.desc), lay.workspace.data_ptr(), tp,
         kdata.data_ptr(), B, C, grid.data_ptr(), lay.stream_for_call(True))))
     return grid
@@ -622,10 +639,10 @@ def nufft_fwd(geom: GeomKey, lay: PointsLayout, tables, scaling, image, smaps, n
     grid = torch.empty((B, C) + geom.grid_size, dtype=image.dtype, device=dev)
     kdata = torch.empty((B, C, lay.npts), dtype=image.dtype, device=dev)
     tp, keep, fl = table_ptrs(tables, image.dtype)
-    L.check(L.lib().tkbn_nufft_fwd(ctypes.byref(geom_struct(geom, fl | lay.flags)), ctypes.byref(lay.desc),
-                                   lay.workspace.data_ptr(),
-                                   plan.handle, tp, _c(scaling), image.data_ptr(), _c(smaps), sb, B, C,
-                                   norm_code(norm), grid.data_ptr(), kdata.data_ptr(), lay.stream_for_call(False)))
+    lay.factor_call(keep, fl, lambda flags: L.check(L.lib().tkbn_nufft_fwd(
+        ctypes.byref(geom_struct(geom, flags)), ctypes.byref(lay.desc), lay.workspace.data_ptr(), plan.handle, tp,
+        _c(scaling), image.data_ptr(), _c(smaps), sb, B, C, norm_code(norm), grid.data_ptr(), kdata.data_ptr(),
+        lay.stream_for_call(True))))
     return kdata
 
 
@@ -645,7 +662,7 @@ def nufft_adj(geom: GeomKey, lay: PointsLayout, tables, scaling, kdata, smaps, n
     co = 1 if smaps is not None else C
     image = torch.empty((B, co) + geom.im_size, dtype=kdata.dtype, device=dev)
     tp, keep, fl = table_ptrs(tables, kdata.dtype)
-    lay.adjoint_call(keep, fl, lambda flags: L.check(L.lib().tkbn_nufft_adj(
+    lay.factor_call(keep, fl, lambda flags: L.check(L.lib().tkbn_nufft_adj(
         ctypes.byref(geom_struct(geom, flags)), ctypes.byref(lay.desc), lay.workspace.data_ptr(), plan.handle, tp,
         _c(scaling), kdata.data_ptr(), _c(smaps), sb, B, C, norm_code(norm), grid.data_ptr(), image.data_ptr(),
         lay.stream_for_call(True))))

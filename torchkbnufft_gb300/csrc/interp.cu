@@ -481,6 +481,25 @@ __device__ __forceinline__ void fwd_job(const Geo<R>& geo, const Launch& a, cons
   }
 }
 
+// 2D register-adjoint tile (rows x columns) and coils per job; the
+// linear-phase gather and adjoint below share its E tables.
+constexpr int kRegTileY = 16, kRegTileX = 14, kRegCoils = 16;
+
+// Linear-phase tables (TKBN_TABLES_LINEAR_PHASE): table[k] = m(k) e^{i c u_k},
+// u_k = (k - center) / L, m >= 0. A point's factors sit at u_0 - j (u_0 in
+// (J/2 - 1, J/2]), so with E[n] = e^{-i c n} and h^ = h / |h|,
+//   e^{-i c u_0} = conj(h^[2]) E[2]       (h[2]: |u| <= 1, a well-defined phase)
+// and, with tile-local cell (y, x) and footprint start (ry, rx), jy = y - ry:
+//   conj(hy[jy] hx[jx] phase) = my[jy] mx[jx] * Q * R(y, x),
+//   Q = conj(phase hy^[2] hx^[2]) Ey[2 + ry] Ex[2 + rx],  R(y, x) = conj(Ey[y] Ex[x]).
+// The adjoint multiplies the k-space values by Q (per list entry),
+// accumulates with the real my, mx and multiplies the tile by R. The slope c
+// is fitted by least squares to the table's phases over u in (0, 1] (error
+// ~1e-8), and the E tables are evaluated in double.
+constexpr int kLpE0 = 3;              // E tables start at n = -kLpE0
+constexpr int kLpEy = kRegTileY + 5;  // n = -3 .. 17 (entries 2 + ry and cells y)
+constexpr int kLpEx = kRegTileX + 5;  // n = -3 .. 15
+
 // ---------------------------------------------------------------- K3, coil pairs
 // Gather for 2D complex64, J = 6, CC coils per job (2, 4, 8 or 16): the tile
 // patch is stored coil-fastest ([cell][CC + 2]), so a lane reads two coils of a
@@ -519,11 +538,22 @@ __device__ __forceinline__ void load_patch_pairs(const Geo<float>& geo, const fl
   cp_async_wait_all();
 }
 
-template <int CC>
+// LP (linear-phase tables, see kLpE0): real kernel values from the per-point
+// pre-pass records {mx[6], my[6], P} (P = conj(phase hy^[2] hx^[2])). Patch
+// cell (Y, X) is multiplied once per job by Ey[Y - 3] Ex[X - 3], so that with
+// the footprint start (ly, lx) in the patch and Y = ly + jy, E[jy - 2] =
+// E[Y - 3] conj(E[ly - 1]) gives
+//   y = conj(P Ey[ly - 1] Ex[lx - 1]) sum_jy my[jy] sum_jx mx[jx] X'(ly + jy, lx + jx):
+// two real multiply-adds per tap and coil instead of four. Points whose bins
+// do not step by exactly L have P = 0 here and are rewritten by k_fwd_lp_fix.
+// pfr: the records (16 floats per sorted point); etab: {Ey[kLpEy], Ex[kLpEx]}
+// in shared memory; the patch must be at most kLpEy x kLpEx cells.
+template <int CC, bool LP = false>
 __device__ __forceinline__ void fwd_job_pairs(const Geo<float>& geo, const Launch& a, const float* __restrict__ tm,
                                               const float2* __restrict__ ph, const float2* __restrict__ grid,
                                               float2* __restrict__ kdata, int64_t job, int64_t nitems,
-                                              float2* patch) {
+                                              float2* patch, const float* __restrict__ pfr = nullptr,
+                                              const float2* etab = nullptr) {
   constexpr int D = 2, NJ = 6, LPP = CC / 2, PPW = 32 / LPP;  // lanes per point, points per warp
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int PX = geo.P[1];
@@ -539,12 +569,34 @@ __device__ __forceinline__ void fwd_job_pairs(const Geo<float>& geo, const Launc
   __syncthreads();
   load_patch_pairs<CC>(geo, grid, jc.b * a.C + jc.c0, a.gtot, jc.ncl, jc.origin, patch);
   __syncthreads();
+  if constexpr (LP) {
+    // the patch times Ey[Y - 3] Ex[X - 3] (thread per cell, 16 bytes at a time)
+    for (int cell = threadIdx.x; cell < cells; cell += kThreads) {
+      const int Y = cell / PX, X = cell - Y * PX;
+      const float2 E = cmul<float>(etab[Y], etab[kLpEy + X]);
+      float4* pc = reinterpret_cast<float4*>(patch + cell * CS);
+#pragma unroll
+      for (int q = 0; q < CC / 2; ++q) {
+        const float4 v = pc[q];
+        const float2 v0 = cmul<float>(make_float2(v.x, v.y), E), v1 = cmul<float>(make_float2(v.z, v.w), E);
+        pc[q] = make_float4(v0.x, v0.y, v1.x, v1.y);
+      }
+    }
+    __syncthreads();
+  }
   constexpr int PPB = PPW * kWarps;
   const int nrounds = (it.len + PPB - 1) / PPB;
   int64_t i_next = it.start + min(warp * PPW + pslot, it.len - 1);
   float tm_next[D];
   int32_t val_next = a.vals[i_next];
-  float2 ph_next = ph[i_next];
+  float2 ph_next = make_float2(0.f, 0.f);
+  float4 rec_next[4];
+  if constexpr (LP) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) rec_next[q] = reinterpret_cast<const float4*>(pfr + i_next * 16)[q];
+  } else {
+    ph_next = ph[i_next];
+  }
 #pragma unroll
   for (int d = 0; d < D; ++d) tm_next[d] = tm[d * a.n + i_next];
   for (int r = 0; r < nrounds; ++r) {
@@ -555,52 +607,92 @@ __device__ __forceinline__ void fwd_job_pairs(const Geo<float>& geo, const Launc
     for (int d = 0; d < D; ++d) tmv[d] = tm_next[d];
     const int32_t val = val_next;
     const float2 phv = ph_next;
+    float4 rec[4];
+    if constexpr (LP) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) rec[q] = rec_next[q];
+    }
     if (r + 1 < nrounds) {
       i_next = it.start + min(s + PPB, it.len - 1);
       val_next = a.vals[i_next];
-      ph_next = ph[i_next];
+      if constexpr (LP) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) rec_next[q] = reinterpret_cast<const float4*>(pfr + i_next * 16)[q];
+      } else {
+        ph_next = ph[i_next];
+      }
 #pragma unroll
       for (int d = 0; d < D; ++d) tm_next[d] = tm[d * a.n + i_next];
     }
     int base[D], local[D];
     const bool ok = point_base_at<float, D>(geo, tmv, jc.origin, base, local);
-    // the point's D*NJ table factors, split over its LPP lanes, exchanged in scratch
-#pragma unroll
-    for (int f = k; f < D * NJ; f += LPP) {
-      const int d = f / NJ, j = f % NJ;
-      const int kb = table_bin<float>(d == 0 ? tmv[0] : tmv[1], (d == 0 ? base[0] : base[1]) + j,
-                                      sel<float, D>(geo.Lr, d), sel<int, D>(geo.center, d), sel<int, D>(geo.tmax, d));
-      pscr[f] = table_entry<float>(sel<const float2*, D>(geo.tab, d), kb, sel<int, D>(geo.center, d),
-                                   sel<bool, D>(geo.half, d));
-    }
-    __syncwarp();
     float2 hy[NJ], hx[NJ];
+    if constexpr (!LP) {
+      // the point's D*NJ table factors, split over its LPP lanes, exchanged in scratch
 #pragma unroll
-    for (int j = 0; j < NJ; ++j) {
-      hy[j] = pscr[j];
-      hx[j] = pscr[NJ + j];
+      for (int f = k; f < D * NJ; f += LPP) {
+        const int d = f / NJ, j = f % NJ;
+        const int kb = table_bin<float>(d == 0 ? tmv[0] : tmv[1], (d == 0 ? base[0] : base[1]) + j,
+                                        sel<float, D>(geo.Lr, d), sel<int, D>(geo.center, d),
+                                        sel<int, D>(geo.tmax, d));
+        pscr[f] = table_entry<float>(sel<const float2*, D>(geo.tab, d), kb, sel<int, D>(geo.center, d),
+                                     sel<bool, D>(geo.half, d));
+      }
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        hy[j] = pscr[j];
+        hx[j] = pscr[NJ + j];
+      }
+      __syncwarp();
     }
-    __syncwarp();
     if (active && 2 * k < jc.ncl) {
       const int64_t m = val - jc.t * a.M;
       float2 y0, y1;
       if (ok) {
         float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
         const float4* prow = reinterpret_cast<const float4*>(patch + (local[0] * PX + local[1]) * CS) + k;
+        if constexpr (LP) {
+          const float mx[NJ] = {rec[0].x, rec[0].y, rec[0].z, rec[0].w, rec[1].x, rec[1].y};
+          const float my[NJ] = {rec[1].z, rec[1].w, rec[2].x, rec[2].y, rec[2].z, rec[2].w};
 #pragma unroll
-        for (int jy = 0; jy < NJ; ++jy) {
-          float2 r0 = make_float2(0.f, 0.f), r1 = make_float2(0.f, 0.f);
+          for (int jy = 0; jy < NJ; ++jy) {
+            float2 r0 = make_float2(0.f, 0.f), r1 = make_float2(0.f, 0.f);
 #pragma unroll
-          for (int jx = 0; jx < NJ; ++jx) {
-            const float4 q = prow[(jy * PX + jx) * (CS / 2)];
-            r0 = cfma<float>(hx[jx], make_float2(q.x, q.y), r0);
-            r1 = cfma<float>(hx[jx], make_float2(q.z, q.w), r1);
+            for (int jx = 0; jx < NJ; ++jx) {
+              const float4 q = prow[(jy * PX + jx) * (CS / 2)];
+              r0.x = fmaf(mx[jx], q.x, r0.x);
+              r0.y = fmaf(mx[jx], q.y, r0.y);
+              r1.x = fmaf(mx[jx], q.z, r1.x);
+              r1.y = fmaf(mx[jx], q.w, r1.y);
+            }
+            acc0.x = fmaf(my[jy], r0.x, acc0.x);
+            acc0.y = fmaf(my[jy], r0.y, acc0.y);
+            acc1.x = fmaf(my[jy], r1.x, acc1.x);
+            acc1.y = fmaf(my[jy], r1.y, acc1.y);
           }
-          acc0 = cfma<float>(hy[jy], r0, acc0);
-          acc1 = cfma<float>(hy[jy], r1, acc1);
+          // conj(P Ey[ly - 1] Ex[lx - 1])
+          const float2 Pc = cconj<float>(cmul<float>(
+              make_float2(rec[3].x, rec[3].y),
+              cmul<float>(etab[kLpE0 + local[0] - 1], etab[kLpEy + kLpE0 + local[1] - 1])));
+          y0 = cmul<float>(acc0, Pc);
+          y1 = cmul<float>(acc1, Pc);
+        } else {
+#pragma unroll
+          for (int jy = 0; jy < NJ; ++jy) {
+            float2 r0 = make_float2(0.f, 0.f), r1 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int jx = 0; jx < NJ; ++jx) {
+              const float4 q = prow[(jy * PX + jx) * (CS / 2)];
+              r0 = cfma<float>(hx[jx], make_float2(q.x, q.y), r0);
+              r1 = cfma<float>(hx[jx], make_float2(q.z, q.w), r1);
+            }
+            acc0 = cfma<float>(hy[jy], r0, acc0);
+            acc1 = cfma<float>(hy[jy], r1, acc1);
+          }
+          y0 = cmul<float>(acc0, phv);
+          y1 = cmul<float>(acc1, phv);
         }
-        y0 = cmul<float>(acc0, phv);
-        y1 = cmul<float>(acc1, phv);
       } else {
         y0 = y1 = make_float2(NAN, NAN);
       }
@@ -612,17 +704,81 @@ __device__ __forceinline__ void fwd_job_pairs(const Geo<float>& geo, const Launc
   }
 }
 
-template <int CC>
+// LP: pfr = the pre-pass records, followed (at float2 offset 12 n) by the
+// {Ey, Ex} tables, which each CTA copies behind its patch and factor scratch.
+template <int CC, bool LP>
 __global__ void __launch_bounds__(kThreads) k_interp_fwd_pairs(Geo<float> geo, Launch a, const float* __restrict__ tm,
                                                                const float2* __restrict__ ph,
                                                                const float2* __restrict__ grid,
-                                                               float2* __restrict__ kdata) {
+                                                               float2* __restrict__ kdata,
+                                                               const float* __restrict__ pfr) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* patch = reinterpret_cast<float2*>(smem_raw);
+  float2* etab = nullptr;
+  if constexpr (LP) {
+    constexpr int PPW = 64 / CC;
+    etab = patch + a.cells * pair_cell_stride<CC>() + kWarps * PPW * 2 * 6;
+    if (threadIdx.x < kLpEy + kLpEx) etab[threadIdx.x] = reinterpret_cast<const float2*>(pfr)[a.n * 12 + threadIdx.x];
+    __syncthreads();
+  }
   const int64_t nitems = a.hdr[0];
   const int64_t njobs = nitems * a.nbpt * a.ncc;
   for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
-    fwd_job_pairs<CC>(geo, a, tm, ph, grid, kdata, job, nitems, patch);
+    fwd_job_pairs<CC, LP>(geo, a, tm, ph, grid, kdata, job, nitems, patch, pfr, etab);
+}
+
+// Exact values of the points the linear-phase gather left out (P = 0 in their
+// records): one thread per (listed point, batch item, coil) gathers its 36
+// taps from the grid with the table factors, after the main pass.
+__global__ void __launch_bounds__(kThreads) k_fwd_lp_fix(Geo<float> geo, Launch a, const float* __restrict__ tm,
+                                                         const float2* __restrict__ ph,
+                                                         const float2* __restrict__ grid,
+                                                         const int32_t* __restrict__ fix,
+                                                         const int32_t* __restrict__ nfix, float2* __restrict__ kdata) {
+  constexpr int D = 2, NJ = 6;
+  const int64_t nb = a.ntraj == 1 ? a.B : 1;
+  const int64_t total = (int64_t)(*nfix) * nb * a.C;
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = w % a.C, r = w / a.C;
+    const int64_t i = fix[r / nb];
+    const int32_t val = a.vals[i];
+    const int64_t t = val / a.M, m = val - t * a.M;
+    const int64_t b = a.ntraj == 1 ? r % nb : t;
+    float2 hy[NJ], hx[NJ];
+    int gy[NJ], gx[NJ];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const float tv = tm[d * a.n + i];
+      const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
+      const float Lr = sel<float, D>(geo.Lr, d);
+      const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d);
+      const float2* tab = sel<const float2*, D>(geo.tab, d);
+      const bool half = sel<bool, D>(geo.half, d);
+      const int K = sel<int, D>(geo.K, d);
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        const float2 te = table_entry<float>(tab, table_bin<float>(tv, base + j, Lr, center, tmax), center, half);
+        if (d == 0) {
+          hy[j] = te;
+          gy[j] = wrap_cell(base + j, K);
+        } else {
+          hx[j] = te;
+          gx[j] = wrap_cell(base + j, K);
+        }
+      }
+    }
+    const float2* plane = grid + (b * a.C + c) * a.gtot;
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int jy = 0; jy < NJ; ++jy) {
+      const float2* row = plane + (int64_t)gy[jy] * geo.K[1];
+      float2 rs = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int jx = 0; jx < NJ; ++jx) rs = cfma<float>(hx[jx], row[gx[jx]], rs);
+      acc = cfma<float>(hy[jy], rs, acc);
+    }
+    kdata[(b * a.C + c) * a.M + m] = cmul<float>(acc, ph[i]);
+  }
 }
 
 template <typename R, int D, int JC>
@@ -1090,7 +1246,6 @@ __global__ void __launch_bounds__(kThreads) k_interp_adj_own(Geo<R> geo, OwnLaun
 constexpr int kNBR = 256;  // staged points per batch (== kThreads)
 static_assert(kNBR == kListChunk, "a 2D register-adjoint batch is one sorted list chunk");
 constexpr int kSVS = kNBR + 1;  // coil stride of the staged k-space values (bank spread)
-constexpr int kRegTileY = 16, kRegTileX = 14, kRegCoils = 16;
 
 // racc[LX + jx] += vy * fx[jx] for the columns inside the row (TXR cells).
 template <int TXR, int LX>
@@ -1119,21 +1274,6 @@ __device__ __forceinline__ void reg_point_factors(const Geo<float>& geo, const f
     out[j] = cconj<float>(d == 0 ? cmul<float>(te, phv) : te);
   }
 }
-
-// Linear-phase tables (TKBN_TABLES_LINEAR_PHASE): table[k] = m(k) e^{i c u_k},
-// u_k = (k - center) / L, m >= 0. A point's factors sit at u_0 - j (u_0 in
-// (J/2 - 1, J/2]), so with E[n] = e^{-i c n} and h^ = h / |h|,
-//   e^{-i c u_0} = conj(h^[2]) E[2]       (h[2]: |u| <= 1, a well-defined phase)
-// and, with tile-local cell (y, x) and footprint start (ry, rx), jy = y - ry:
-//   conj(hy[jy] hx[jx] phase) = my[jy] mx[jx] * Q * R(y, x),
-//   Q = conj(phase hy^[2] hx^[2]) Ey[2 + ry] Ex[2 + rx],  R(y, x) = conj(Ey[y] Ex[x]).
-// The adjoint multiplies the k-space values by Q (per list entry),
-// accumulates with the real my, mx and multiplies the tile by R. The slope c
-// is fitted by least squares to the table's phases over u in (0, 1] (error
-// ~1e-8), and the E tables are evaluated in double.
-constexpr int kLpE0 = 3;              // E tables start at n = -kLpE0
-constexpr int kLpEy = kRegTileY + 5;  // n = -3 .. 17 (entries 2 + ry and cells y)
-constexpr int kLpEx = kRegTileX + 5;  // n = -3 .. 15
 
 // Least-squares slopes of the D dims' table phases over u = k / L in (0, 1]
 // (the whole block of kThreads threads; every thread gets c[0 .. D)).
@@ -2242,7 +2382,7 @@ __global__ void __launch_bounds__(kThreads) k_ragged_fwd_pairs(const RaggedProb<
       __syncthreads();
       cur = pj.x;
     }
-    fwd_job_pairs<CC>(sp.geo, sp.a, sp.tm, sp.ph, sp.grid, sp.kdata, pj.y, sp.nitems, patch);
+    fwd_job_pairs<CC, false>(sp.geo, sp.a, sp.tm, sp.ph, sp.grid, sp.kdata, pj.y, sp.nitems, patch);
   }
 }
 
@@ -2388,6 +2528,56 @@ static int with_cc(int CC, Fn&& fn) {
   }
 }
 
+// The 2D per-point factor scratch of a layout (16 x 14 tiles, complex64,
+// J = 6): per sorted point a record (16 floats in the linear-phase form, 12
+// complex factors otherwise), then {Ey, Ex} and the left-out count past the
+// records, the left-out list in the records' spare room.
+struct PointFactors {
+  float2* pf;
+  float2* et;
+  int32_t* fix;
+  int32_t* nfix;
+};
+
+static PointFactors point_factors_of(const InterpPlan& ip, const char* ws) {
+  PointFactors f;
+  f.pf = (float2*)const_cast<char*>(ws + ip.L.off_pfac);
+  f.et = f.pf + ip.a.n * 12;
+  f.nfix = reinterpret_cast<int32_t*>(f.et + kLpEy + kLpEx + 8);
+  f.fix = reinterpret_cast<int32_t*>(f.pf + ip.a.n * 8);
+  return f;
+}
+
+// Whether the calls on this layout use the linear-phase factor records: the
+// tables are linear-phase and the layout is not deterministic (the adjoint
+// adds the left-out points with atomics).
+static bool lp_factors(const InterpPlan& ip) {
+  return ip.L.pfac && (ip.flags & TKBN_TABLES_LINEAR_PHASE) && !(ip.flags & TKBN_ADJ_DETERMINISTIC);
+}
+
+// Fills the factor scratch (lp: linear-phase records, else complex factors)
+// unless the caller passed TKBN_ADJ_REUSE_FACTORS, vouching that an earlier
+// call on this workspace left the factors of these tables and flags in place.
+static int point_factors_prepass(const Geo<float>& geo, const InterpPlan& ip, const char* ws, bool lp,
+                                 cudaStream_t s) {
+  if (!ip.L.pfac || ip.a.n == 0 || (ip.flags & TKBN_ADJ_REUSE_FACTORS)) return TKBN_OK;
+  const PointFactors f = point_factors_of(ip, ws);
+  const int64_t nb = (2 * ip.a.n + kThreads - 1) / kThreads;
+  const int grid_b = (int)(nb < 152 * 16 ? nb : 152 * 16);
+  if (lp) {
+    int rc = check_cuda(cudaMemsetAsync(f.nfix, 0, sizeof(int32_t), s), "reset left-out count");
+    if (rc) return rc;
+    k_point_factors2<true><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
+                                                        (const float2*)(ws + ip.L.off_phase), ip.a.n, f.pf, f.et,
+                                                        f.fix, f.nfix);
+  } else {
+    k_point_factors2<false><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
+                                                         (const float2*)(ws + ip.L.off_phase), ip.a.n, f.pf, f.et,
+                                                         f.fix, f.nfix);
+  }
+  return check_cuda(cudaGetLastError(), "point factor launch");
+}
+
 template <typename R, int D, int JC>
 static int launch_fwd_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws, const void* grid, void* kdata,
                         cudaStream_t s) {
@@ -2396,15 +2586,32 @@ static int launch_fwd_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws,
       return with_cc(ip.a.Cc, [&](auto ccv) {
         constexpr int CC = decltype(ccv)::value;
         constexpr int PPW = 64 / CC;
+        // linear-phase form: patches of at most kLpEy x kLpEx cells (the E tables' range)
+        const bool lp = lp_factors(ip) && geo.P[0] <= kLpEy && geo.P[1] <= kLpEx;
         const size_t smem = (size_t)ip.a.cells * pair_cell_stride<CC>() * sizeof(float2) +
-                            (size_t)kWarps * PPW * 2 * 6 * sizeof(float2);
+                            (size_t)kWarps * PPW * 2 * 6 * sizeof(float2) +
+                            (lp ? (size_t)(kLpEy + kLpEx) * sizeof(float2) : 0);
+        const float* tmp = (const float*)(ws + ip.L.off_coords);
+        const float2* php = (const float2*)(ws + ip.L.off_phase);
+        if (!lp) {
+          int blocks;
+          int rc = resident_blocks(k_interp_fwd_pairs<CC, false>, smem, ip.max_jobs, &blocks);
+          if (rc) return rc;
+          k_interp_fwd_pairs<CC, false><<<blocks, kThreads, smem, s>>>(geo, ip.a, tmp, php, (const float2*)grid,
+                                                                       (float2*)kdata, nullptr);
+          return check_cuda(cudaGetLastError(), "interp_fwd launch");
+        }
+        const PointFactors f = point_factors_of(ip, ws);
         int blocks;
-        int rc = resident_blocks(k_interp_fwd_pairs<CC>, smem, ip.max_jobs, &blocks);
+        int rc = resident_blocks(k_interp_fwd_pairs<CC, true>, smem, ip.max_jobs, &blocks);
         if (rc) return rc;
-        k_interp_fwd_pairs<CC><<<blocks, kThreads, smem, s>>>(geo, ip.a, (const float*)(ws + ip.L.off_coords),
-                                                              (const float2*)(ws + ip.L.off_phase),
-                                                              (const float2*)grid, (float2*)kdata);
-        return check_cuda(cudaGetLastError(), "interp_fwd launch");
+        k_interp_fwd_pairs<CC, true><<<blocks, kThreads, smem, s>>>(geo, ip.a, tmp, php, (const float2*)grid,
+                                                                    (float2*)kdata, (const float*)f.pf);
+        rc = check_cuda(cudaGetLastError(), "interp_fwd launch");
+        if (rc) return rc;
+        k_fwd_lp_fix<<<152, kThreads, 0, s>>>(geo, ip.a, tmp, php, (const float2*)grid, f.fix, f.nfix,
+                                              (float2*)kdata);
+        return check_cuda(cudaGetLastError(), "interp_fwd fix launch");
       });
     }
   }
@@ -2457,6 +2664,11 @@ static int interp_fwd_r(const tkbn_geometry* g, const tkbn_points_desc* p, const
   if (p->npts == 0) return TKBN_OK;
   Geo<R> geo = make_geo<R>(g, &ip.L, tables, nullptr);
   const char* w = (const char*)ws;
+  if constexpr (std::is_same<R, float>::value) {
+    // every forward or adjoint call on a layout with a factor scratch leaves
+    // the factors of its tables and flags there, whichever kernel it runs
+    if (ip.L.pfac && (rc = point_factors_prepass(geo, ip, w, lp_factors(ip), s))) return rc;
+  }
   const bool j6 = all_j(g, 6);
   switch (g->ndim) {
     case 1:
@@ -2591,33 +2803,13 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
       // linear-phase tables: real factors (needs the per-point pre-pass)
       // (a deterministic layout keeps the table path: the linear-phase form
       // adds its left-out points with atomics)
-      const bool lp = (ip.flags & TKBN_TABLES_LINEAR_PHASE) && !(ip.flags & TKBN_ADJ_DETERMINISTIC) && ip.L.pfac;
-      // the layout's factor scratch (see tkbn_interp_adj: calls sharing a workspace are ordered):
-      // per-point records, then {Ey, Ex} and the left-out count past them, the
-      // left-out list in the records' spare room
-      float2* pf = (float2*)const_cast<char*>(ws + ip.L.off_pfac);
-      float2* et = pf + ip.a.n * 12;
-      int32_t* nfix = reinterpret_cast<int32_t*>(et + kLpEy + kLpEx + 8);
-      int32_t* fix = reinterpret_cast<int32_t*>(pf + ip.a.n * 8);
-      if (ip.L.pfac && ip.a.n > 0) {
-        const int64_t nb = (2 * ip.a.n + kThreads - 1) / kThreads;
-        const int grid_b = (int)(nb < 152 * 16 ? nb : 152 * 16);
-        if (ip.flags & TKBN_ADJ_REUSE_FACTORS) {
-          // the caller vouches that an earlier call on this workspace left the
-          // factors (and the left-out list) of these tables and flags in place
-        } else if (lp) {
-          int rc0 = check_cuda(cudaMemsetAsync(nfix, 0, sizeof(int32_t), s), "reset left-out count");
-          if (rc0) return rc0;
-          k_point_factors2<true><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
-                                                              (const float2*)(ws + ip.L.off_phase), ip.a.n, pf, et,
-                                                              fix, nfix);
-        } else {
-          k_point_factors2<false><<<grid_b, kThreads, 0, s>>>(geo, (const float*)(ws + ip.L.off_coords),
-                                                               (const float2*)(ws + ip.L.off_phase), ip.a.n, pf, et,
-                                                               fix, nfix);
-        }
-        orr.pfac = pf;
-      }
+      // the factor scratch was filled (or vouched for) by interp_adj_r
+      const bool lp = lp_factors(ip);
+      const PointFactors f = point_factors_of(ip, ws);
+      float2* pf = f.pf;
+      int32_t* nfix = f.nfix;
+      int32_t* fix = f.fix;
+      if (ip.L.pfac && ip.a.n > 0) orr.pfac = pf;
       return with_cc(reg_cc(o.Cc), [&](auto ccv) {
         constexpr int CC = decltype(ccv)::value;
         const size_t rsmem = reg_smem(CC);
@@ -2703,6 +2895,11 @@ static int interp_adj_r(const tkbn_geometry* g, const tkbn_points_desc* p, const
     return check_cuda(cudaMemsetAsync(grid, 0, (size_t)(B * C * ip.a.gtot) * sizeof(cplx<R>), s), "zero grid");
   Geo<R> geo = make_geo<R>(g, &ip.L, tables, nullptr);
   const char* w = (const char*)ws;
+  if constexpr (std::is_same<R, float>::value) {
+    // every forward or adjoint call on a layout with a factor scratch leaves
+    // the factors of its tables and flags there, whichever kernel it runs
+    if (ip.L.pfac && (rc = point_factors_prepass(geo, ip, w, lp_factors(ip), s))) return rc;
+  }
   const bool j6 = all_j(g, 6);
   switch (g->ndim) {
     case 1:
