@@ -1473,6 +1473,8 @@ __device__ __forceinline__ void reg_columns(const int32_t* ko, int r_lo, int r_h
   int p = ko[kb + r_lo];
   const int e = ko[kb + r_hi + 5];
   if (NG > 1) p += (grp - p % NG + NG) % NG;
+  // two entries per iteration: their shared-memory loads are in flight together
+#pragma unroll 2
   for (; p < e; p += NG) {
     const int2 lp = sloc[p];
     const int jy = myrow - lp.x;
@@ -1520,6 +1522,8 @@ __device__ __forceinline__ void reg_columns_lp(const int32_t* ko, int r_lo, int 
   int p = ko[kb + r_lo];
   const int e = ko[kb + r_hi + 5];
   if (NG > 1) p += (grp - p % NG + NG) % NG;
+  // two entries per iteration: their shared-memory loads are in flight together
+#pragma unroll 2
   for (; p < e; p += NG) {
     const int2 lp = sloc[p];
     const int jy = myrow - lp.x;
@@ -1769,6 +1773,8 @@ __device__ __forceinline__ void reg3_columns(const int32_t* ko, int ylo, int yhi
   int p = ko[kb + ylo];
   const int e = ko[kb + yhi + 5];
   if (NG > 1) p += (grp - p % NG + NG) % NG;
+  // two entries per iteration: their shared-memory loads are in flight together
+#pragma unroll 2
   for (; p < e; p += NG) {
     const int4 loc = sloc[p];
     const int jz = mz - loc.x, jy = my - loc.y;
@@ -1803,6 +1809,8 @@ __device__ __forceinline__ void reg3_columns_lp(const int32_t* ko, int ylo, int 
   int p = ko[kb + ylo];
   const int e = ko[kb + yhi + 5];
   if (NG > 1) p += (grp - p % NG + NG) % NG;
+  // two entries per iteration: their shared-memory loads are in flight together
+#pragma unroll 2
   for (; p < e; p += NG) {
     const int4 loc = sloc[p];
     const int jz = mz - loc.x, jy = my - loc.y;
