@@ -493,7 +493,8 @@ __global__ void __launch_bounds__(ct_threads<NC>(), FW == kFftF ? ct_min_blocks<
     const int64_t plane = u / ngrp;
     const int col = (int)(u - plane * ngrp) * F + f;
     const bool cok = col < K1;
-    cplx<R>* g = grid + plane * gtot + (cok ? col : 0);
+    const int64_t gplane = s.pk == s.pt ? plane : (plane / s.pk) * s.pt + plane % s.pk;
+    cplx<R>* g = grid + gplane * gtot + (cok ? col : 0);
     auto ld = [&](int row) { return (cok && row < nload) ? g[(int64_t)row * K1] : mk<R>(0, 0); };
     const R osc = MODE == kColToep ? R(1) : scale;
     auto st = [&](int row, cplx<R> v) {
@@ -690,12 +691,13 @@ __global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC, R>())
     const int64_t b = u / N0;
     const int n0 = (int)(u - b * N0);
     const cplx<R>* sc = scaling ? scaling + (int64_t)n0 * N1 : nullptr;
+    const int64_t grow = (int64_t)(n0 / s.ny) * s.ky + n0 % s.ny;  // the row's grid row
     for (int64_t c0 = 0; c0 < C; c0 += F) {
       const int64_t c = c0 + f;
       const bool cok = c < C;
       const cplx<R>* im = image + (b * ci + (ci == 1 ? 0 : (cok ? c : 0))) * ntot + (int64_t)n0 * N1;
       const cplx<R>* sm = smaps ? smaps + ((sb == 1 ? 0 : b) * C + (cok ? c : 0)) * ntot + (int64_t)n0 * N1 : nullptr;
-      cplx<R>* g = grid + (b * C + (cok ? c : 0)) * gtot + (int64_t)n0 * NC;
+      cplx<R>* g = grid + (b * C + (cok ? c : 0)) * gtot + grow * NC;
       auto ld = [&](int m) {
         cplx<R> v = mk<R>(0, 0);
         if (cok && m < N1) {
@@ -742,10 +744,11 @@ __global__ void __launch_bounds__(ct_threads<NC>(), ct_min_blocks<NC, R>())
     const int64_t b = u / N0;
     const int n0 = (int)(u - b * N0);
     const cplx<R>* sc = scaling ? scaling + (int64_t)n0 * N1 : nullptr;
+    const int64_t grow = (int64_t)(n0 / s.ny) * s.ky + n0 % s.ny;  // the row's grid row
     for (int64_t c0 = 0; c0 < C; c0 += F) {
       const int64_t c = c0 + f;
       const bool cok = c < C;
-      const cplx<R>* g = grid + (b * C + (cok ? c : 0)) * gtot + (int64_t)n0 * NC;
+      const cplx<R>* g = grid + (b * C + (cok ? c : 0)) * gtot + grow * NC;
       auto ld = [&](int m) { return cok ? g[m] : mk<R>(0, 0); };
       if (smaps) {
         const cplx<R>* sm = smaps + ((sb == 1 ? 0 : b) * C + (cok ? c : 0)) * ntot + (int64_t)n0 * N1;
@@ -1164,6 +1167,105 @@ int fft2d_inverse(const Fft2d& p, int dtype, int64_t B, int64_t C, void* grid, c
                   const void* scaling, double scale, void* out, cudaStream_t st) {
   return dtype == TKBN_C64 ? inverse_r<float>(p, B, C, grid, smaps, sb, scaling, scale, out, st)
                            : inverse_r<double>(p, B, C, grid, smaps, sb, scaling, scale, out, st);
+}
+
+static bool ct_size(int n) {
+  return n == 256 || n == 320 || n == 384 || n == 512 || n == 640 || n == 768 || n == 1024;
+}
+
+bool fft3d_supported(const int K[3]) { return ct_size(K[0]) && ct_size(K[1]) && ct_size(K[2]); }
+
+// Shapes of the three passes of a 3D transform: the x rows of the nonzero
+// (z, y) image rows, the y columns of the nonzero z slices, and the z columns
+// of each volume seen as Kz rows of Ky*Kx columns.
+static Fft2dShape rows3(const Fft3d& p) {
+  Fft2dShape s = fft2d_shape(p.N[0] * p.N[1], p.N[2], p.K[0] * p.K[1], p.K[2]);
+  s.ny = p.N[1];
+  s.ky = p.K[1];
+  return s;
+}
+static Fft2dShape cols_y3(const Fft3d& p) {
+  Fft2dShape s = fft2d_shape(p.N[1], p.N[2], p.K[1], p.K[2]);
+  s.pk = p.N[0];
+  s.pt = p.K[0];
+  return s;
+}
+static Fft2dShape cols_z3(const Fft3d& p) { return fft2d_shape(p.N[0], p.N[1] * p.N[2], p.K[0], p.K[1] * p.K[2]); }
+
+static const FftPlan1 kNoPlan = {0, 0, {0, 0, 0, 0}, 0};
+
+template <typename R>
+static int forward3_r(const Fft3d& p, int64_t B, int64_t C, int64_t ci, const void* image, const void* smaps,
+                      int64_t sb, const void* scaling, double scale, void* grid, cudaStream_t st) {
+  int rc = with_size<R>(p.K[2], [&](auto nc) {
+    if constexpr (decltype(nc)::value == 0) {
+      return set_error(TKBN_ERR_UNSUPPORTED, "3D fused FFT needs compile-time plan sizes");
+    } else {
+      return rows_pad_r<R, decltype(nc)::value>(rows3(p), kNoPlan, p.tw[2], B, C, ci, image, smaps, sb, scaling,
+                                                scale, grid, st);
+    }
+  });
+  if (rc) return rc;
+  rc = with_size<R>(p.K[1], [&](auto nc) {
+    if constexpr (decltype(nc)::value == 0) {
+      return set_error(TKBN_ERR_UNSUPPORTED, "3D fused FFT needs compile-time plan sizes");
+    } else {
+      return cols_r<R, decltype(nc)::value>(cols_y3(p), kNoPlan, p.tw[1], kColFwd, B * C * p.N[0], C, nullptr, 1, 0,
+                                            1.0, grid, st);
+    }
+  });
+  if (rc) return rc;
+  return with_size<R>(p.K[0], [&](auto nc) {
+    if constexpr (decltype(nc)::value == 0) {
+      return set_error(TKBN_ERR_UNSUPPORTED, "3D fused FFT needs compile-time plan sizes");
+    } else {
+      return cols_r<R, decltype(nc)::value>(cols_z3(p), kNoPlan, p.tw[0], kColFwd, B * C, C, nullptr, 1, 0, 1.0,
+                                            grid, st);
+    }
+  });
+}
+
+template <typename R>
+static int inverse3_r(const Fft3d& p, int64_t B, int64_t C, void* grid, const void* smaps, int64_t sb,
+                      const void* scaling, double scale, void* out, cudaStream_t st) {
+  int rc = with_size<R>(p.K[0], [&](auto nc) {
+    if constexpr (decltype(nc)::value == 0) {
+      return set_error(TKBN_ERR_UNSUPPORTED, "3D fused FFT needs compile-time plan sizes");
+    } else {
+      return cols_r<R, decltype(nc)::value>(cols_z3(p), kNoPlan, p.tw[0], kColInv, B * C, C, nullptr, 1, 0, 1.0,
+                                            grid, st);
+    }
+  });
+  if (rc) return rc;
+  rc = with_size<R>(p.K[1], [&](auto nc) {
+    if constexpr (decltype(nc)::value == 0) {
+      return set_error(TKBN_ERR_UNSUPPORTED, "3D fused FFT needs compile-time plan sizes");
+    } else {
+      return cols_r<R, decltype(nc)::value>(cols_y3(p), kNoPlan, p.tw[1], kColInv, B * C * p.N[0], C, nullptr, 1, 0,
+                                            1.0, grid, st);
+    }
+  });
+  if (rc) return rc;
+  return with_size<R>(p.K[2], [&](auto nc) {
+    if constexpr (decltype(nc)::value == 0) {
+      return set_error(TKBN_ERR_UNSUPPORTED, "3D fused FFT needs compile-time plan sizes");
+    } else {
+      return rows_crop_r<R, decltype(nc)::value>(rows3(p), kNoPlan, p.tw[2], B, C, grid, smaps, sb, scaling, scale,
+                                                 out, st);
+    }
+  });
+}
+
+int fft3d_forward(const Fft3d& p, int dtype, int64_t B, int64_t C, int64_t ci, const void* image, const void* smaps,
+                  int64_t sb, const void* scaling, double scale, void* grid, cudaStream_t st) {
+  return dtype == TKBN_C64 ? forward3_r<float>(p, B, C, ci, image, smaps, sb, scaling, scale, grid, st)
+                           : forward3_r<double>(p, B, C, ci, image, smaps, sb, scaling, scale, grid, st);
+}
+
+int fft3d_inverse(const Fft3d& p, int dtype, int64_t B, int64_t C, void* grid, const void* smaps, int64_t sb,
+                  const void* scaling, double scale, void* out, cudaStream_t st) {
+  return dtype == TKBN_C64 ? inverse3_r<float>(p, B, C, grid, smaps, sb, scaling, scale, out, st)
+                           : inverse3_r<double>(p, B, C, grid, smaps, sb, scaling, scale, out, st);
 }
 
 int fft2d_toeplitz(const Fft2d& p, int dtype, int64_t B, int64_t C, int64_t ci, const void* image,

@@ -21,7 +21,26 @@ struct FftPlan1 {
 struct Fft2dShape {
   int N0, N1;  // image size
   int K0, K1;  // grid size
+  // Row passes: image row n0 sits in grid row (n0 / ny) * ky + n0 % ny (a 3D
+  // volume's (z, y) rows: ny = Ny, ky = Ky; 2D: ny = N0). Column passes: unit
+  // plane p is grid plane (p / pk) * pt + p % pk (the nonzero z slices of a
+  // 3D volume: pk = Nz, pt = Kz; 2D: pk = pt = 1).
+  int ny, ky;
+  int pk, pt;
 };
+
+// The fused-pass shape of a 2D grid (every mapping the identity).
+inline Fft2dShape fft2d_shape(int N0, int N1, int K0, int K1) {
+  Fft2dShape s;
+  s.N0 = N0;
+  s.N1 = N1;
+  s.K0 = K0;
+  s.K1 = K1;
+  s.ny = N0 > 0 ? N0 : 1;
+  s.ky = K0;
+  s.pk = s.pt = 1;
+  return s;
+}
 
 }  // namespace tkbn
 
@@ -48,6 +67,20 @@ int fft2d_forward(const Fft2d& p, int dtype, int64_t B, int64_t C, int64_t ci, c
                   int64_t sb, const void* scaling, double scale, void* grid, cudaStream_t st);
 // out = [sum_c conj(smaps) *] conj(scaling) * scale * crop(IFFT2(grid)); grid is overwritten
 int fft2d_inverse(const Fft2d& p, int dtype, int64_t B, int64_t C, void* grid, const void* smaps, int64_t sb,
+                  const void* scaling, double scale, void* out, cudaStream_t st);
+// 3D grids whose three sizes have compile-time plans: the same passes per
+// dimension, skipping the zero padding (rows past Nx in x, rows past Ny and
+// slices past Nz never read), with twiddles per dim.
+struct Fft3d {
+  int N[3], K[3];
+  void* tw[3];
+};
+bool fft3d_supported(const int K[3]);
+// grid[b, c] = FFT3(pad(image [* smaps] * scaling) * scale)
+int fft3d_forward(const Fft3d& p, int dtype, int64_t B, int64_t C, int64_t ci, const void* image, const void* smaps,
+                  int64_t sb, const void* scaling, double scale, void* grid, cudaStream_t st);
+// out = [sum_c conj(smaps) *] conj(scaling) * scale * crop(IFFT3(grid)); grid is overwritten
+int fft3d_inverse(const Fft3d& p, int dtype, int64_t B, int64_t C, void* grid, const void* smaps, int64_t sb,
                   const void* scaling, double scale, void* out, cudaStream_t st);
 // out = [sum_c conj(smaps) *] crop(IFFT2(kernel * scale * FFT2(pad([smaps *] image) * scale)))
 int fft2d_toeplitz(const Fft2d& p, int dtype, int64_t B, int64_t C, int64_t ci, const void* image,

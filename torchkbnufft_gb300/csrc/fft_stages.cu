@@ -15,6 +15,8 @@
 
 #include <cufft.h>
 
+#include <algorithm>
+
 #include <cmath>
 #include <new>
 
@@ -22,7 +24,9 @@
 #include "tkbn_common.cuh"
 
 // A plan is either the fused 2D passes of fft2d.cu (2D grids whose sizes
-// factor into radices 2..15 and fit shared memory) or a cuFFT plan.
+// factor into radices 2..15 and fit shared memory) or a cuFFT plan. 3D grids
+// whose three sizes have compile-time plans also get the fused passes (fused3)
+// for the forward and inverse stages; their Toeplitz filter keeps cuFFT.
 struct tkbn_fft_plan_s {
   cufftHandle handle;
   int ndim;
@@ -31,6 +35,8 @@ struct tkbn_fft_plan_s {
   int64_t batch;
   bool fused;
   tkbn_host::Fft2d f2;
+  bool fused3;
+  tkbn_host::Fft3d f3;
 };
 
 namespace tkbn {
@@ -225,6 +231,32 @@ int fft_plan_create(const tkbn_geometry* g, int64_t B, int64_t C, tkbn_fft_plan*
     p->n[d] = g->grid_size[d];
   }
   p->fused = false;
+  p->fused3 = false;
+  if (g->ndim == 3) {
+    int K[3] = {(int)g->grid_size[0], (int)g->grid_size[1], (int)g->grid_size[2]};
+    const bool dbl = g->dtype == TKBN_C128;
+    // the largest pass: a column pass of 8 columns or a row pass of 4 rows (plus the coil sum row)
+    size_t smem = 0;
+    for (int d = 0; d < 3; ++d) {
+      const size_t e = dbl ? 16 : 8;
+      const size_t c = 2 * (size_t)K[d] * 8 * e, r = (2 * (size_t)K[d] * tkbn::kFftF + (size_t)K[d]) * e;
+      smem = std::max(smem, std::max(c, r));
+    }
+    if (fft3d_supported(K) && smem <= 200 * 1024) {
+      int rc = TKBN_OK;
+      for (int d = 0; d < 3; ++d) p->f3.tw[d] = nullptr;
+      for (int d = 0; d < 3 && !rc; ++d) {
+        p->f3.K[d] = K[d];
+        rc = fft1_twiddles(K[d], dbl, &p->f3.tw[d]);
+      }
+      if (rc) {
+        for (int d = 0; d < 3; ++d) cudaFree(p->f3.tw[d]);
+        delete p;
+        return rc;
+      }
+      p->fused3 = true;  // the cuFFT plan below serves the Toeplitz filter
+    }
+  }
   if (g->ndim == 2 && g->grid_size[0] <= tkbn::kFftMaxN && g->grid_size[1] <= tkbn::kFftMaxN &&
       fft1_plan((int)g->grid_size[0], &p->f2.p0) && fft1_plan((int)g->grid_size[1], &p->f2.p1)) {
     p->f2.s.K0 = (int)g->grid_size[0];
@@ -249,6 +281,8 @@ int fft_plan_create(const tkbn_geometry* g, int64_t B, int64_t C, tkbn_fft_plan*
   }
   int rc = check_cufft(cufftCreate(&p->handle), "cufftCreate");
   if (rc) {
+    if (p->fused3)
+      for (int d = 0; d < 3; ++d) cudaFree(p->f3.tw[d]);
     delete p;
     return rc;
   }
@@ -258,6 +292,8 @@ int fft_plan_create(const tkbn_geometry* g, int64_t B, int64_t C, tkbn_fft_plan*
                    "cufftMakePlanMany64");
   if (rc) {
     cufftDestroy(p->handle);
+    if (p->fused3)
+      for (int d = 0; d < 3; ++d) cudaFree(p->f3.tw[d]);
     delete p;
     return rc;
   }
@@ -274,6 +310,12 @@ int fft_plan_destroy(tkbn_fft_plan p) {
     if (!rc) rc = rc1;
   } else {
     rc = check_cufft(cufftDestroy(p->handle), "cufftDestroy");
+    if (p->fused3) {
+      for (int d = 0; d < 3; ++d) {
+        const int rc1 = check_cuda(cudaFree(p->f3.tw[d]), "free twiddles");
+        if (!rc) rc = rc1;
+      }
+    }
   }
   delete p;
   return rc;
@@ -282,8 +324,13 @@ int fft_plan_destroy(tkbn_fft_plan p) {
 // The fused passes of a plan with this call's image size.
 static Fft2d fused_for(const tkbn_fft_plan p, const Shape& s) {
   Fft2d f = p->f2;
-  f.s.N0 = s.N[0];
-  f.s.N1 = s.N[1];
+  f.s = tkbn::fft2d_shape(s.N[0], s.N[1], f.s.K0, f.s.K1);
+  return f;
+}
+
+static Fft3d fused3_for(const tkbn_fft_plan p, const Shape& s) {
+  Fft3d f = p->f3;
+  for (int d = 0; d < 3; ++d) f.N[d] = s.N[d];
   return f;
 }
 
@@ -358,6 +405,8 @@ int fft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image,
   const double sc = ortho_scale(s, norm);
   if (plan->fused)
     return fft2d_forward(fused_for(plan, s), g->dtype, B, C, ci, image, smaps, smaps_batch, scaling, sc, grid, st);
+  if (plan->fused3)
+    return fft3d_forward(fused3_for(plan, s), g->dtype, B, C, ci, image, smaps, smaps_batch, scaling, sc, grid, st);
   rc = g->dtype == TKBN_C64 ? pad_scale_r<float>(s, B, C, ci, image, smaps, smaps_batch, scaling, sc, grid, st)
                             : pad_scale_r<double>(s, B, C, ci, image, smaps, smaps_batch, scaling, sc, grid, st);
   if (rc) return rc;
@@ -375,6 +424,8 @@ int ifft_and_scale(const tkbn_geometry* g, tkbn_fft_plan plan, void* grid, const
   const double sc = ortho_scale(s, norm);
   if (plan->fused)
     return fft2d_inverse(fused_for(plan, s), g->dtype, B, C, grid, smaps, smaps_batch, scaling, sc, image, st);
+  if (plan->fused3)
+    return fft3d_inverse(fused3_for(plan, s), g->dtype, B, C, grid, smaps, smaps_batch, scaling, sc, image, st);
   rc = fft_exec(plan, grid, CUFFT_INVERSE, st);
   if (rc) return rc;
   return g->dtype == TKBN_C64 ? crop_scale_r<float>(s, B, C, grid, smaps, smaps_batch, scaling, sc, image, st)
