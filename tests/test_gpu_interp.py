@@ -491,3 +491,22 @@ def test_factor_reuse_between_forward_and_adjoint(tmp_path):
     want = O.interp_forward(grid.numpy(), om.numpy(), [o1.tables[0] * 2, o1.tables[1]], o1.n_shift, o1.numpoints,
                             o1.table_oversamp)
     assert rel_l2(_np(f1(gd, omd)), want) < TOL64
+
+
+def test_linear_phase_factors_beyond_one_pass_of_the_prepass_grid():
+    """The per-point factor pre-pass runs a grid-stride loop; with more points
+    than its grid has threads (152 * 16 blocks of 256), threads take several
+    points, some of them left out (near the k-space centre). Forward and
+    adjoint against the oracle at 700k points."""
+    gen = torch.Generator().manual_seed(59)
+    K, C, M = (160, 144), 2, 700_000
+    grid = _rand(gen, (1, C) + K, torch.complex64)
+    y = _rand(gen, (1, C, M), torch.complex64)
+    om = _traj(gen, (2, M)).float()
+    om[..., ::4] *= 0.01  # every fourth point near the centre, spread over the sorted order
+    op = O.Operator(K, K, cdtype=np.complex64)
+    fwd = tkbn().KbInterp(im_size=K, grid_size=K, dtype=torch.complex64, device=DEV)
+    adj = tkbn().KbInterpAdjoint(im_size=K, grid_size=K, dtype=torch.complex64, device=DEV)
+    omd = om.to(DEV)
+    assert rel_l2(_np(fwd(grid.to(DEV), omd)), op.interp(grid.numpy(), om.numpy())) < TOL64
+    assert rel_l2(_np(adj(y.to(DEV), omd)), op.interp_adj(y.numpy(), om.numpy())) < TOL64

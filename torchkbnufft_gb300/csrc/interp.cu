@@ -1370,30 +1370,21 @@ __global__ void __launch_bounds__(kThreads) k_point_factors2(Geo<float> geo, con
         etab[t] = make_float2((float)cs, (float)-sn);
       }
     }
-    // thread pair (2i, 2i + 1) takes point i's two dims; the pair meets to form P
-    for (int64_t e0 = blockIdx.x * (int64_t)blockDim.x; e0 < 2 * n; e0 += (int64_t)gridDim.x * blockDim.x) {
-      const int64_t e = e0 + threadIdx.x, i = e >> 1;
-      const int d = (int)(e & 1);
-      const bool on = e < 2 * n;
+    // one thread per point, both dims (no exchange between lanes)
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
       float* rec = reinterpret_cast<float*>(pfac) + i * 16;
-      float2 hat = make_float2(1.f, 0.f);
-      bool mis = false;
-      if (on) hat = reg_point_factors_lp(geo, tm, n, i, d, rec, &mis);
-      const float2 other = make_float2(__shfl_xor_sync(0xffffffffu, hat.x, 1), __shfl_xor_sync(0xffffffffu, hat.y, 1));
-      // every lane takes part in the shuffle (not behind a short-circuit ||)
-      const int other_mis = __shfl_xor_sync(0xffffffffu, (int)mis, 1);
-      mis = mis || other_mis != 0;
-      if (on && d == 0) {
-        float2 P = cmul<float>(cmul<float>(ph[i], hat), other);
-        if (mis) {
-          P = make_float2(0.f, 0.f);
-          fix[atomicAdd(nfix, 1)] = (int32_t)i;
-        }
-        rec[12] = P.x;
-        rec[13] = -P.y;
-        rec[14] = 0.f;
-        rec[15] = 0.f;
+      bool mis_y = false, mis_x = false;
+      const float2 hy = reg_point_factors_lp(geo, tm, n, i, 0, rec, &mis_y);
+      const float2 hx = reg_point_factors_lp(geo, tm, n, i, 1, rec, &mis_x);
+      float2 P = cmul<float>(cmul<float>(ph[i], hy), hx);
+      if (mis_y || mis_x) {
+        P = make_float2(0.f, 0.f);
+        fix[atomicAdd(nfix, 1)] = (int32_t)i;
       }
+      rec[12] = P.x;
+      rec[13] = -P.y;
+      rec[14] = 0.f;
+      rec[15] = 0.f;
     }
   } else {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 2 * n;
