@@ -153,7 +153,8 @@ int tkbn_interp_fwd(const tkbn_geometry* g, const tkbn_points_desc* p, const voi
                     const void* const* tables, const void* grid, int64_t nbatch, int64_t ncoil,
                     void* kdata, void* stream);
 /* grid = interp^H(kdata). grid is fully overwritten (zeroed first). With 2D
- * complex64 J = 6 layouts of 16 x 14 tiles the call also fills a per-point
+ * complex64 J = 6 layouts of 16 x 14 tiles, and 3D ones of 4 x 8 x 8 tiles with
+ * TKBN_TABLES_LINEAR_PHASE, the call (forward or adjoint) also fills a per-point
  * scratch region inside the workspace (the table factors; unless
  * TKBN_ADJ_REUSE_FACTORS), so forward and adjoint calls that share one
  * workspace must be ordered (one stream). */

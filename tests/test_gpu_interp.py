@@ -387,23 +387,24 @@ def test_linear_phase_adjoint_exact_pass(ndim, subset, tmp_path):
     assert rel_l2(_np(adj(y.to(DEV), om.to(DEV))), op.interp_adj(y.numpy(), om.numpy())) < TOL64
 
 
-def test_adjoint_factor_reuse_follows_the_tables(tmp_path):
-    """The 2D register adjoint keeps its per-point table factors in the layout's
+@pytest.mark.parametrize("ndim", [2, 3])
+def test_adjoint_factor_reuse_follows_the_tables(ndim, tmp_path):
+    """The register adjoints keep their per-point table factors in the layout's
     workspace between calls (they depend on the trajectory and the tables
     only). The same tables again skip the pre-pass; another table set on the
     same layout (same geometry, other kbwidth) or a table changed in place
     recomputes it. Every result matches the oracle for its own tables."""
     gen = torch.Generator().manual_seed(47)
-    K, C, M = (96, 84), 4, 6000
+    K, C, M = ((96, 84), 4, 6000) if ndim == 2 else ((40, 32, 48), 4, 6000)
     y = _rand(gen, (1, C, M), torch.complex64)
-    om = _traj(gen, (2, M)).float()
+    om = _traj(gen, (ndim, M)).float()
     a1 = tkbn().KbInterpAdjoint(im_size=K, grid_size=K, device=DEV)
     a2 = tkbn().KbInterpAdjoint(im_size=K, grid_size=K, kbwidth=2.0, device=DEV)
     o1 = O.Operator(K, K, cdtype=np.complex64)
     ref1 = o1.interp_adj(y.numpy(), om.numpy())
     ref2 = O.Operator(K, K, kbwidth=2.0, cdtype=np.complex64).interp_adj(y.numpy(), om.numpy())
-    ref1b = O.interp_adjoint(y.numpy(), om.numpy(), [o1.tables[0] * 2, o1.tables[1]], o1.n_shift, o1.numpoints,
-                             o1.table_oversamp, K)
+    ref1b = O.interp_adjoint(y.numpy(), om.numpy(), [o1.tables[0] * 2] + list(o1.tables[1:]), o1.n_shift,
+                             o1.numpoints, o1.table_oversamp, K)
     yd, omd = y.to(DEV), om.to(DEV)
 
     def run(mod):
@@ -411,8 +412,8 @@ def test_adjoint_factor_reuse_follows_the_tables(tmp_path):
 
     def prepass_launched(mod):
         names = _kernels_launched(lambda: mod(yd, omd), tmp_path)
-        assert any("k_interp_adj_reg<" in n for n in names), names
-        return any("k_point_factors2" in n for n in names)
+        assert any(("k_interp_adj_reg<" if ndim == 2 else "k_interp_adj_reg3<") in n for n in names), names
+        return any(("k_point_factors2" if ndim == 2 else "k_point_factors3") in n for n in names)
 
     assert rel_l2(run(a1), ref1) < TOL64
     assert not prepass_launched(a1)

@@ -1819,6 +1819,56 @@ __device__ __forceinline__ void reg3_columns_lp(const int32_t* ko, int ylo, int 
     reg3_columns_lp<CC, NG, LXI + 1>(ko, ylo, yhi, grp, sfr, sv, sloc, mz, my, rowok, c, racc);
 }
 
+// Pre-pass of the 3D linear-phase register adjoint: per sorted point its 18
+// real magnitudes where the adjoint stages them (x at 0, y at 8, z at 14)
+// and at 20 the phase word conj(phase hz^[2] hy^[2] hx^[2]) (kLp3PRec floats
+// per point), so the adjoint's staging is plain 16-byte copies. A point whose
+// bins do not step by exactly L gets a zero phase word and is listed in lfix
+// (count at 0, indices from 16; the count reset by the host) for
+// k_adj_lp_fix3. One thread per point.
+__global__ void __launch_bounds__(kThreads) k_point_factors3(Geo<float> geo, const float* __restrict__ tm,
+                                                             const float2* __restrict__ ph, int64_t n,
+                                                             float* __restrict__ rec3, int32_t* __restrict__ lfix) {
+  constexpr int D = 3, NJ = 6;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float* rec = rec3 + i * kLp3PRec;
+    float2 P = ph[i];
+    bool mis = false;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const float tv = tm[d * n + i];
+      const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
+      const float Lr = sel<float, D>(geo.Lr, d);
+      const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d), L = sel<int, D>(geo.L, d);
+      const float2* tab = sel<const float2*, D>(geo.tab, d);
+      const bool half = sel<bool, D>(geo.half, d);
+      const int k0 = table_bin<float>(tv, base, Lr, center, tmax);
+      float* out = rec + (d == 2 ? 0 : (d == 1 ? 8 : 14));
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        const int kb = table_bin<float>(tv, base + j, Lr, center, tmax);
+        // for |tm| >= 8, tm and every g are within a factor 2 of each other:
+        // fl(tm - g) is exact and the bins step by exactly L
+        mis = mis || (fabsf(tv) < 8.f && kb != k0 - j * L);
+        const float2 te = table_entry<float>(tab, kb, center, half);
+        out[j] = sqrtf(te.x * te.x + te.y * te.y);
+      }
+      const float2 te = table_entry<float>(tab, k0 - 2 * L, center, half);
+      const float mg = sqrtf(te.x * te.x + te.y * te.y);
+      P = cmul<float>(P, make_float2(te.x / mg, te.y / mg));
+    }
+    float2 Pc = cconj<float>(P);
+    if (mis) {
+      Pc = make_float2(0.f, 0.f);
+      lfix[16 + atomicAdd(lfix, 1)] = (int32_t)i;
+    }
+    rec[6] = rec[7] = 0.f;
+    rec[20] = Pc.x;
+    rec[21] = Pc.y;
+    rec[22] = rec[23] = 0.f;
+  }
+}
+
 // End of the 3D register adjoint's staging buffers (the E tables follow).
 __host__ __device__ constexpr size_t reg3_etab_offset(int CC) {
   return (((size_t)kNBR * 3 * 6 * sizeof(float2) + (size_t)CC * kSVS * sizeof(float2) + (size_t)kNBR * sizeof(int4) +
@@ -1835,7 +1885,7 @@ template <int CC, bool LP = false>
 __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch& a, const float* __restrict__ tm,
                                          const float2* __restrict__ ph, const float2* __restrict__ kdata,
                                          float2* __restrict__ grid, int vec_ok, int64_t job, unsigned char* smem_raw,
-                                         const float2* etab = nullptr, int32_t* lfix = nullptr) {
+                                         const float2* etab = nullptr, const float* __restrict__ rec3 = nullptr) {
   constexpr int D = 3, NJ = 6;
   // lane (coil, z, y): a warp covers all kReg3Z planes of YB rows y0 .. y0 + YB - 1
   constexpr int RPW = 32 / CC, YB = RPW / kReg3Z, WPT = kReg3Y / YB, NG = kWarps / WPT;
@@ -1893,7 +1943,17 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
             sv[cl * kSVS + s] = make_float2(0.f, 0.f);
         }
       }
-      for (int e = threadIdx.x; e < nv * D; e += kThreads) {
+      if constexpr (LP) {
+        // the sorted point's 18 magnitudes: five 16-byte copies of its pre-pass record
+        for (int e = threadIdx.x; e < nv * 5; e += kThreads) {
+          const int pt = e / 5, q = e - pt * 5;
+          const int4 ent = sents[pt];
+          if (q == 0) sloc[pt] = make_int4(ent.z, (int)(short)(ent.w & 0xffff), ent.y, 0);
+          cp_async_16(sfac + pt * (kLp3Rec / 2) + 2 * q,
+                      reinterpret_cast<const float2*>(rec3) + (int64_t)ent.x * (kLp3PRec / 2) + 2 * q);
+        }
+      }
+      for (int e = threadIdx.x; e < (LP ? 0 : nv * D); e += kThreads) {
         const int pt = e / D, d = e - (e / D) * D;
         const int4 ent = sents[pt];
         if (d == 0) sloc[pt] = make_int4(ent.z, (int)(short)(ent.w & 0xffff), ent.y, 0);
@@ -1923,41 +1983,14 @@ __device__ __forceinline__ void reg3_job(const Geo<float>& geo, const OwnLaunch&
       }
       cp_async_wait_all();
       if (LP && (int)threadIdx.x < nv) {
-        // this thread's own copies have landed: entry s's values times Q
+        // this thread's own copies have landed: entry s's values times
+        // Q = (phase word of its point) * prod_d E_d[2 + r_d] (zero for a left-out point)
         const int s = threadIdx.x;
         const int4 ent = ents[s];
         const int r[3] = {ent.z, (int)(short)(ent.w & 0xffff), ent.w >> 16};
-        float2 P = ph[ent.x];
-        float2 E = make_float2(1.f, 0.f);
-        bool mis = false;
+        float2 Q = reinterpret_cast<const float2*>(rec3)[(int64_t)ent.x * (kLp3PRec / 2) + 10];
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-          const float tv = tm[d * a.n + ent.x];
-          const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
-          const float Lr = sel<float, D>(geo.Lr, d);
-          const int center = sel<int, D>(geo.center, d), tmax = sel<int, D>(geo.tmax, d), L = sel<int, D>(geo.L, d);
-          const int k0 = table_bin<float>(tv, base, Lr, center, tmax);
-          // for |tm| >= 8, tm and every g are within a factor 2 of each other:
-          // fl(tm - g) is exact and the bins step by exactly L
-          if (fabsf(tv) < 8.f) {
-#pragma unroll
-            for (int j = 1; j < NJ; ++j)
-              mis = mis || (table_bin<float>(tv, base + j, Lr, center, tmax) != k0 - j * L);
-          }
-          const float2 te = table_entry<float>(sel<const float2*, D>(geo.tab, d), k0 - 2 * L, center,
-                                               sel<bool, D>(geo.half, d));
-          const float mg = sqrtf(te.x * te.x + te.y * te.y);
-          P = cmul<float>(P, make_float2(te.x / mg, te.y / mg));
-          E = cmul<float>(E, etab[d * kLp3En + kLp3E0 + 2 + r[d]]);
-        }
-        float2 Q = cmul<float>(cconj<float>(P), E);
-        if (mis) {
-          Q = make_float2(0.f, 0.f);
-          // listed once: from its home tile's entry, in the job of batch item 0 and coil chunk 0
-          if (bb == 0 && cc == 0 && r[0] >= 0 && r[0] < kReg3Z && r[1] >= 0 && r[1] < kReg3Y && r[2] >= 0 &&
-              r[2] < kReg3X)
-            lfix[16 + atomicAdd(lfix, 1)] = ent.x;
-        }
+        for (int d = 0; d < D; ++d) Q = cmul<float>(Q, etab[d * kLp3En + kLp3E0 + 2 + r[d]]);
 #pragma unroll
         for (int cl = 0; cl < CC; ++cl) sv[cl * kSVS + s] = cmul<float>(sv[cl * kSVS + s], Q);
       }
@@ -2040,7 +2073,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg3(Geo<float> geo,
                                                                  const float2* __restrict__ ph,
                                                                  const float2* __restrict__ kdata,
                                                                  float2* __restrict__ grid, int vec_ok,
-                                                                 int32_t* __restrict__ lfix) {
+                                                                 const float* __restrict__ rec3) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* etab = reinterpret_cast<float2*>(smem_raw + reg3_etab_offset(CC));  // [3][kLp3En], past the staging
   if constexpr (LP) {
@@ -2057,7 +2090,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_interp_adj_reg3(Geo<float> geo,
   }
   const int64_t njobs = a.hdr[1] * a.nbpt * a.ncc;
   for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
-    reg3_job<CC, LP>(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw, etab, lfix);
+    reg3_job<CC, LP>(geo, a, tm, ph, kdata, grid, vec_ok, job, smem_raw, etab, rec3);
 }
 
 // Exact contributions of the points the 3D linear-phase adjoint left out
@@ -2554,6 +2587,26 @@ static bool lp_factors(const InterpPlan& ip) {
   return ip.L.pfac && (ip.flags & TKBN_TABLES_LINEAR_PHASE) && !(ip.flags & TKBN_ADJ_DETERMINISTIC);
 }
 
+// 3D: whether the calls on this layout use the linear-phase records (the
+// same conditions as in 2D).
+static bool lp3_factors(const InterpPlan& ip) {
+  return ip.L.pfac3 && (ip.flags & TKBN_TABLES_LINEAR_PHASE) && !(ip.flags & TKBN_ADJ_DETERMINISTIC);
+}
+
+// Fills the 3D records and the left-out list unless TKBN_ADJ_REUSE_FACTORS
+// (an earlier call on this workspace left those of these tables and flags).
+static int point_factors3_prepass(const Geo<float>& geo, const InterpPlan& ip, const char* ws, cudaStream_t s) {
+  if (!lp3_factors(ip) || ip.a.n == 0 || (ip.flags & TKBN_ADJ_REUSE_FACTORS)) return TKBN_OK;
+  int32_t* lfix = (int32_t*)const_cast<char*>(ws + ip.L.off_lfix);
+  int rc = check_cuda(cudaMemsetAsync(lfix, 0, sizeof(int32_t), s), "reset left-out count");
+  if (rc) return rc;
+  const int64_t nb = (ip.a.n + kThreads - 1) / kThreads;
+  k_point_factors3<<<(int)(nb < 152 * 16 ? nb : 152 * 16), kThreads, 0, s>>>(
+      geo, (const float*)(ws + ip.L.off_coords), (const float2*)(ws + ip.L.off_phase), ip.a.n,
+      (float*)const_cast<char*>(ws + ip.L.off_pfac3), lfix);
+  return check_cuda(cudaGetLastError(), "point factor launch");
+}
+
 // Fills the factor scratch (lp: linear-phase records, else complex factors)
 // unless the caller passed TKBN_ADJ_REUSE_FACTORS, vouching that an earlier
 // call on this workspace left the factors of these tables and flags in place.
@@ -2667,6 +2720,7 @@ static int interp_fwd_r(const tkbn_geometry* g, const tkbn_points_desc* p, const
     // every forward or adjoint call on a layout with a factor scratch leaves
     // the factors of its tables and flags there, whichever kernel it runs
     if (ip.L.pfac && (rc = point_factors_prepass(geo, ip, w, lp_factors(ip), s))) return rc;
+    if (ip.L.pfac3 && (rc = point_factors3_prepass(geo, ip, w, s))) return rc;
   }
   const bool j6 = all_j(g, 6);
   switch (g->ndim) {
@@ -2843,20 +2897,21 @@ static int launch_adj_own_t(const Geo<R>& geo, const InterpPlan& ip, const char*
         const int vec_ok = ((uintptr_t)grid % 16 == 0) && (geo.K[2] % 2 == 0);
         // linear-phase tables: real kernel values (not for deterministic layouts:
         // the left-out points are added with atomics)
-        const bool lp = (ip.flags & TKBN_TABLES_LINEAR_PHASE) && !(ip.flags & TKBN_ADJ_DETERMINISTIC) && ip.L.lfix;
+        // (the records and the left-out list come from the pre-pass, run by interp_adj_r)
+        const bool lp = lp3_factors(ip);
         int32_t* lfix = lp ? (int32_t*)const_cast<char*>(ws + ip.L.off_lfix) : nullptr;
+        const float* rec3 = lp ? (const float*)(ws + ip.L.off_pfac3) : nullptr;
         auto launch = [&](auto kernel) {
           int blocks;
           int rc = resident_blocks(kernel, rsmem, max_jobs, &blocks);
           if (rc) return rc;
           kernel<<<blocks, kThreads, rsmem, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
                                                  (const float2*)(ws + ip.L.off_phase), (const float2*)kdata,
-                                                 (float2*)grid, vec_ok, lfix);
+                                                 (float2*)grid, vec_ok, rec3);
           return check_cuda(cudaGetLastError(), "interp_adj launch");
         };
         if (!lp) return launch(k_interp_adj_reg3<CC, false>);
-        int rc = check_cuda(cudaMemsetAsync(lfix, 0, sizeof(int32_t), s), "reset left-out count");
-        if (!rc) rc = launch(k_interp_adj_reg3<CC, true>);
+        int rc = launch(k_interp_adj_reg3<CC, true>);
         if (rc) return rc;
         k_adj_lp_fix3<<<152, kThreads, 0, s>>>(geo, o, (const float*)(ws + ip.L.off_coords),
                                                 (const float2*)(ws + ip.L.off_phase), (const float2*)kdata, lfix,
@@ -2898,6 +2953,7 @@ static int interp_adj_r(const tkbn_geometry* g, const tkbn_points_desc* p, const
     // every forward or adjoint call on a layout with a factor scratch leaves
     // the factors of its tables and flags there, whichever kernel it runs
     if (ip.L.pfac && (rc = point_factors_prepass(geo, ip, w, lp_factors(ip), s))) return rc;
+    if (ip.L.pfac3 && (rc = point_factors3_prepass(geo, ip, w, s))) return rc;
   }
   const bool j6 = all_j(g, 6);
   switch (g->ndim) {

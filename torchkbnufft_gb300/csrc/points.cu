@@ -522,6 +522,7 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
              L->knk <= tkbn::kSortMaxKeys;
   L->pfac = L->csort && g->ndim == 2;
   L->lfix = L->csort && g->ndim == 3;
+  L->pfac3 = L->lfix;
   L->koff_rows = L->ksort ? L->nkeys : (L->csort ? L->max_valid / tkbn::kListChunk + L->nkeys + 1 : 0);
   L->max_subjobs = 2 * L->nkeys + (L->span.ncombo * L->npts_total + L->adj_chunk - 1) / L->adj_chunk;
   int sbits = 1;
@@ -597,6 +598,8 @@ int points_layout(const tkbn_geometry* g, const tkbn_points_desc* p, PointsLayou
   o = align_up(o + (L->pfac ? (size_t)L->npts_total * 12 * 8 + 512 : 0));  // + linear-phase tables
   L->off_lfix = o;
   o = align_up(o + (L->lfix ? (size_t)4 * L->npts_total + 64 : 0));
+  L->off_pfac3 = o;
+  o = align_up(o + (L->pfac3 ? (size_t)tkbn::kLp3PRec * sizeof(float) * L->npts_total : 0));
   L->off_coords = o;
   o = align_up(o + rsize * g->ndim * n);
   L->off_phase = o;

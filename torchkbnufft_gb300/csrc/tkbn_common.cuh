@@ -10,6 +10,8 @@ namespace tkbn {
 
 // Entries of a tile's point list staged per adjoint batch (2D register adjoint).
 constexpr int kListChunk = 256;
+// floats per sorted point of the 3D linear-phase factor records
+constexpr int kLp3PRec = 24;
 
 constexpr int kMaxDim = 3;
 constexpr int kMaxJ = 8;  // numpoints supported per dimension
@@ -268,8 +270,11 @@ struct PointsLayout {
   // filled by the register adjoint before it runs
   bool pfac;
   // 3D chunk-sorted layouts: list of points the linear-phase adjoint leaves
-  // out (count first, then indices)
+  // out (count first, then indices), and room for each sorted point's 18
+  // real table magnitudes and phase word (24 floats), filled by a pre-pass
   bool lfix;
+  bool pfac3;
+  size_t off_pfac3;
   size_t off_hdr, off_keys_in, off_vals_in, off_keys, off_vals, off_counts, off_tile_off, off_nit, off_item_off,
       off_items, off_items_raw, off_ikeys_in, off_ikeys, off_ivals_in, off_ivals, off_coords, off_phase,
       off_tile_work, off_tile_nsub, off_tile_suboff, off_sj_raw, off_adj_jobs, off_sj_keys_in, off_sj_keys,
