@@ -339,10 +339,12 @@ def test_specialised_kernels_are_selected(case, tmp_path):
     names = _kernels_launched(lambda: R.interp_adj(geom, lay, tables, kdata), tmp_path)
     want = "k_interp_adj_reg3" if case == "3d8" else "k_interp_adj_reg<"
     assert any(want in n for n in names), names
+    # the linear-phase gathers
+    names = _kernels_launched(lambda: R.interp_fwd(geom, lay, tables, grid), tmp_path)
     if case != "3d8":
-        # the linear-phase form of the coil-pair gather
-        names = _kernels_launched(lambda: R.interp_fwd(geom, lay, tables, grid), tmp_path)
         assert any("k_interp_fwd_pairs<" in n and "true>" in n for n in names), names
+    else:
+        assert any("k_interp_fwd_lp3<" in n for n in names), names
 
 
 def _bins_mismatched(om, op, K):
@@ -428,17 +430,24 @@ def test_adjoint_factor_reuse_follows_the_tables(ndim, tmp_path):
     assert rel_l2(run(a1), ref1b) < TOL64
 
 
-@pytest.mark.parametrize("C", [16, 4])
+@pytest.mark.parametrize("case", ["2d16", "2d4", "3d8", "3d3"])
 @pytest.mark.parametrize("subset", ["centre_heavy", "left_out_only"])
-def test_linear_phase_gather_exact_pass(C, subset, tmp_path):
-    """The linear-phase coil-pair gather works with real kernel values on a
-    patch multiplied by the E tables; points whose table bins do not step by
-    exactly L get their exact values from a second pass (k_fwd_lp_fix). Cases:
-    3/4 of the points near the k-space centre, and only the left-out points."""
+def test_linear_phase_gather_exact_pass(case, subset, tmp_path):
+    """The linear-phase gathers (2D coil pairs, 3D one lane per coil) work with
+    real kernel values on a patch multiplied by the E tables; points whose
+    table bins do not step by exactly L get their exact values from a second
+    pass (k_fwd_lp_fix, k_fwd_lp_fix3). Cases: 3/4 of the points near the
+    k-space centre, and only the left-out points (with a mismatch in every
+    dimension among them)."""
+    ndim, C = (2 if case.startswith("2d") else 3), int(case[2:])
     gen = torch.Generator().manual_seed(43)
-    K, M = (160, 144), 30000
-    grid = _rand(gen, (2, C) + K, torch.complex64)
-    om = _traj(gen, (2, M)).float()
+    K, M = ((160, 144), 30000) if ndim == 2 else ((40, 32, 48), 20000)
+    if ndim == 2:
+        grid = _rand(gen, (2, C) + K, torch.complex64)
+        om = _traj(gen, (ndim, M)).float()
+    else:  # the trajectory first, so that it does not depend on the coil count
+        om = _traj(gen, (ndim, M)).float()
+        grid = _rand(gen, (2, C) + K, torch.complex64)
     om[..., : 3 * M // 4] *= 0.01
     op = O.Operator(K, K, cdtype=np.complex64)
     if subset == "left_out_only":
@@ -448,8 +457,12 @@ def test_linear_phase_gather_exact_pass(C, subset, tmp_path):
     fwd = tkbn().KbInterp(im_size=K, grid_size=K, dtype=torch.complex64, device=DEV)
     gd, omd = grid.to(DEV), om.to(DEV)
     names = _kernels_launched(lambda: fwd(gd, omd), tmp_path)
-    assert any("k_fwd_lp_fix" in n for n in names), names
-    assert any("k_interp_fwd_pairs<" in n and "true>" in n for n in names), names
+    if ndim == 2:
+        assert any("k_fwd_lp_fix" in n for n in names), names
+        assert any("k_interp_fwd_pairs<" in n and "true>" in n for n in names), names
+    else:
+        assert any("k_fwd_lp_fix3" in n for n in names), names
+        assert any("k_interp_fwd_lp3<" in n for n in names), names
     assert rel_l2(_np(fwd(gd, omd)), op.interp(grid.numpy(), om.numpy())) < TOL64
 
 

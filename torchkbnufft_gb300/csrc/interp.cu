@@ -2141,6 +2141,184 @@ __global__ void __launch_bounds__(kThreads) k_adj_lp_fix3(Geo<float> geo, OwnLau
   }
 }
 
+// ---------------------------------------------------------------- K3, 3D linear-phase
+// Gather for 3D complex64, J = 6, 4 x 8 x 8 tiles (patch 9 x 13 x 13, fixed at
+// compile time), linear-phase tables, with the layout of the generic gather:
+// one shared-memory plane per coil, one lane per (point, coil). After staging,
+// patch cell (Z, Y, X) is multiplied by Ez[Z - 3] Ey[Y - 3] Ex[X - 3]; a lane
+// takes its point's 18 real magnitudes and phase word Pw from the point's
+// pre-pass record (k_point_factors3) and does two real multiply-adds per tap:
+//   y = conj(Pw prod_d E_d[l_d - 1]) sum prod_d m_d[j_d] X'(l + j),
+// (l the footprint start in the patch; Pw = conj(phase prod_d h^_d[2])). A
+// left-out point has Pw = 0 and is rewritten by k_fwd_lp_fix3. Every lane
+// runs the taps; a point outside its tile reads the patch at its first cell
+// and is written as NaN.
+constexpr int kP3Z = kReg3Z + 5, kP3Y = kReg3Y + 5, kP3X = kReg3X + 5, kP3Cells = kP3Z * kP3Y * kP3X;
+constexpr int kP3PS = kP3Cells | 1;  // plane stride (odd: a point's coil lanes hit distinct banks)
+
+template <int CC>
+__host__ __device__ constexpr size_t fwd_lp3_smem() {
+  return (size_t)CC * kP3PS * sizeof(float2) + (size_t)3 * kLp3En * sizeof(float2);
+}
+
+template <int CC>
+__device__ __forceinline__ void fwd_job_lp3(const Geo<float>& geo, const Launch& a, const float* __restrict__ tm,
+                                            const float2* __restrict__ grid, float2* __restrict__ kdata, int64_t job,
+                                            int64_t nitems, float2* patch, const float2* etab,
+                                            const float* __restrict__ rec3) {
+  constexpr int D = 3, NJ = 6, PPW = 32 / CC;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int c = lane % CC, pslot = lane / CC;
+  Item it;
+  JobCtx jc;
+  next_job<float>(geo, a, job, nitems, &it, &jc);
+  __syncthreads();
+  load_patch<float, D>(geo, grid, jc.b * a.C + jc.c0, a.gtot, jc.ncl, kP3Cells, kP3PS, jc.origin, patch);
+  __syncthreads();
+  // the patch times Ez[Z - 3] Ey[Y - 3] Ex[X - 3] (E_d[n] at etab[d kLp3En + kLp3E0 + n])
+  for (int e = threadIdx.x; e < CC * kP3Cells; e += kThreads) {
+    const int cl = e / kP3Cells, cell = e - cl * kP3Cells;
+    const int Z = cell / (kP3Y * kP3X), rem = cell - Z * (kP3Y * kP3X);
+    const int Y = rem / kP3X, X = rem - Y * kP3X;
+    const float2 E = cmul<float>(cmul<float>(etab[Z], etab[kLp3En + Y]), etab[2 * kLp3En + X]);
+    float2* pc = patch + cl * kP3PS + cell;
+    *pc = cmul<float>(*pc, E);
+  }
+  __syncthreads();
+  constexpr int PPB = PPW * kWarps;
+  const int nrounds = (it.len + PPB - 1) / PPB;
+  int64_t i_next = it.start + min(warp * PPW + pslot, it.len - 1);
+  float tm_next[D];
+  int32_t val_next = a.vals[i_next];
+#pragma unroll
+  for (int d = 0; d < D; ++d) tm_next[d] = tm[d * a.n + i_next];
+  for (int r = 0; r < nrounds; ++r) {
+    const int s = r * PPB + warp * PPW + pslot;
+    const bool active = s < it.len;
+    const int64_t i = it.start + min(s, it.len - 1);
+    float tmv[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) tmv[d] = tm_next[d];
+    const int32_t val = val_next;
+    if (r + 1 < nrounds) {
+      i_next = it.start + min(s + PPB, it.len - 1);
+      val_next = a.vals[i_next];
+#pragma unroll
+      for (int d = 0; d < D; ++d) tm_next[d] = tm[d * a.n + i_next];
+    }
+    int base[D], local[D];
+    const bool ok = point_base_at<float, D>(geo, tmv, jc.origin, base, local);
+    // the record: mx at 0, my at 8, mz at 14, Pw at 20
+    const float4* rq = reinterpret_cast<const float4*>(rec3 + i * kLp3PRec);
+    const float4 q0 = rq[0], q1 = rq[1], q2 = rq[2], q3 = rq[3], q4 = rq[4], q5 = rq[5];
+    const float mx[NJ] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+    const float my[NJ] = {q2.x, q2.y, q2.z, q2.w, q3.x, q3.y};
+    const float mz[NJ] = {q3.z, q3.w, q4.x, q4.y, q4.z, q4.w};
+    const int lz = ok ? local[0] : 0, ly = ok ? local[1] : 0, lx = ok ? local[2] : 0;
+    const float2* pp = patch + c * kP3PS + (lz * kP3Y + ly) * kP3X + lx;
+    float ar = 0.f, ai = 0.f;
+#pragma unroll
+    for (int jz = 0; jz < NJ; ++jz) {
+      float sr = 0.f, si = 0.f;
+#pragma unroll
+      for (int jy = 0; jy < NJ; ++jy) {
+        float rr = 0.f, ri = 0.f;
+#pragma unroll
+        for (int jx = 0; jx < NJ; ++jx) {
+          const float2 v = pp[(jz * kP3Y + jy) * kP3X + jx];
+          rr = fmaf(mx[jx], v.x, rr);
+          ri = fmaf(mx[jx], v.y, ri);
+        }
+        sr = fmaf(my[jy], rr, sr);
+        si = fmaf(my[jy], ri, si);
+      }
+      ar = fmaf(mz[jz], sr, ar);
+      ai = fmaf(mz[jz], si, ai);
+    }
+    const float2 El = cmul<float>(cmul<float>(etab[kLp3E0 + lz - 1], etab[kLp3En + kLp3E0 + ly - 1]),
+                                  etab[2 * kLp3En + kLp3E0 + lx - 1]);
+    float2 y = cmulc<float>(make_float2(ar, ai), cmul<float>(make_float2(q5.x, q5.y), El));
+    if (!ok) y = make_float2(NAN, NAN);
+    if (active && c < jc.ncl) kdata[(jc.b * a.C + jc.c0 + c) * a.M + (val - jc.t * a.M)] = y;
+    if (active && !ok && c == 0) atomicOr(&g_status, kStatusNonFinite | kStatusOutsidePatch);
+  }
+}
+
+template <int CC>
+__global__ void __launch_bounds__(kThreads) k_interp_fwd_lp3(Geo<float> geo, Launch a, const float* __restrict__ tm,
+                                                             const float2* __restrict__ grid,
+                                                             float2* __restrict__ kdata, const float* __restrict__ rec3) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* patch = reinterpret_cast<float2*>(smem_raw);
+  float2* etab = patch + CC * kP3PS;  // [3][kLp3En]
+  {
+    // per CTA: the three dims' phase slopes (least squares) and E_d[n] = e^{-i c_d n} in double
+    double c3[3];
+    lp_slopes_block<3>(geo, c3);
+    if (threadIdx.x < 3 * kLp3En) {
+      const int d = threadIdx.x / kLp3En, nidx = threadIdx.x % kLp3En;
+      double sn, cs;
+      sincos(c3[d] * (double)(nidx - kLp3E0), &sn, &cs);
+      etab[threadIdx.x] = make_float2((float)cs, (float)-sn);
+    }
+    __syncthreads();
+  }
+  const int64_t nitems = a.hdr[0];
+  const int64_t njobs = nitems * a.nbpt * a.ncc;
+  for (int64_t job = blockIdx.x; job < njobs; job += gridDim.x)
+    fwd_job_lp3<CC>(geo, a, tm, grid, kdata, job, nitems, patch, etab, rec3);
+}
+
+// Exact values of the points the 3D linear-phase gather left out: one thread
+// per (listed point, batch item, coil) gathers its 216 taps from the grid with
+// the table factors.
+__global__ void __launch_bounds__(kThreads) k_fwd_lp_fix3(Geo<float> geo, Launch a, const float* __restrict__ tm,
+                                                          const float2* __restrict__ ph,
+                                                          const float2* __restrict__ grid,
+                                                          const int32_t* __restrict__ lfix, float2* __restrict__ kdata) {
+  constexpr int D = 3, NJ = 6;
+  const int64_t nb = a.ntraj == 1 ? a.B : 1;
+  const int64_t total = (int64_t)lfix[0] * nb * a.C;
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = w % a.C, r = w / a.C;
+    const int64_t i = lfix[16 + r / nb];
+    const int32_t val = a.vals[i];
+    const int64_t t = val / a.M, m = val - t * a.M;
+    const int64_t b = a.ntraj == 1 ? r % nb : t;
+    float2 h[D][NJ];
+    int g[D][NJ];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const float tv = tm[d * a.n + i];
+      const int base = 1 + (int)floorf(sub_rn(tv, sel<float, D>(geo.halfJ, d)));
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        h[d][j] = table_entry<float>(sel<const float2*, D>(geo.tab, d),
+                                     table_bin<float>(tv, base + j, sel<float, D>(geo.Lr, d),
+                                                      sel<int, D>(geo.center, d), sel<int, D>(geo.tmax, d)),
+                                     sel<int, D>(geo.center, d), sel<bool, D>(geo.half, d));
+        g[d][j] = wrap_cell(base + j, sel<int, D>(geo.K, d));
+      }
+    }
+    const float2* plane = grid + (b * a.C + c) * a.gtot;
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int jz = 0; jz < NJ; ++jz) {
+      float2 az = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int jy = 0; jy < NJ; ++jy) {
+        const float2* row = plane + ((int64_t)g[0][jz] * geo.K[1] + g[1][jy]) * geo.K[2];
+        float2 ay = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int jx = 0; jx < NJ; ++jx) ay = cfma<float>(h[2][jx], row[g[2][jx]], ay);
+        az = cfma<float>(h[1][jy], ay, az);
+      }
+      acc = cfma<float>(h[0][jz], az, acc);
+    }
+    kdata[(b * a.C + c) * a.M + m] = cmul<float>(acc, ph[i]);
+  }
+}
+
 template <int CC, bool LP>
 __global__ void __launch_bounds__(kThreads, 3)
     k_interp_adj_reg(Geo<float> geo, OwnLaunch a, const float* __restrict__ tm, const float2* __restrict__ ph,
@@ -2665,6 +2843,37 @@ static int launch_fwd_t(const Geo<R>& geo, const InterpPlan& ip, const char* ws,
                                               (float2*)kdata);
         return check_cuda(cudaGetLastError(), "interp_fwd fix launch");
       });
+    }
+  }
+  if constexpr (std::is_same<R, float>::value && D == 3 && JC == 6) {
+    // linear-phase tables on a 4 x 8 x 8 layout: real magnitudes from the
+    // per-point records the pre-pass left (run by interp_fwd_r), up to 8 coils per job
+    if (lp3_factors(ip) && geo.P[0] == kP3Z && geo.P[1] == kP3Y && geo.P[2] == kP3X) {
+      Launch a3 = ip.a;
+      a3.Cc = ip.a.C >= 8 ? 8 : next_pow2((int)ip.a.C);
+      a3.ncc = (int)((ip.a.C + a3.Cc - 1) / a3.Cc);
+      const int64_t max_jobs = ip.L.max_items * a3.nbpt * a3.ncc;
+      const float* tmp = (const float*)(ws + ip.L.off_coords);
+      const float* rec3 = (const float*)(ws + ip.L.off_pfac3);
+      auto launch = [&](auto kernel, size_t smem) {
+        int blocks;
+        int rc2 = resident_blocks(kernel, smem, max_jobs, &blocks);
+        if (rc2) return rc2;
+        kernel<<<blocks, kThreads, smem, s>>>(geo, a3, tmp, (const float2*)grid, (float2*)kdata, rec3);
+        return check_cuda(cudaGetLastError(), "interp_fwd launch");
+      };
+      int rc;
+      switch (a3.Cc) {
+        case 1: rc = launch(k_interp_fwd_lp3<1>, fwd_lp3_smem<1>()); break;
+        case 2: rc = launch(k_interp_fwd_lp3<2>, fwd_lp3_smem<2>()); break;
+        case 4: rc = launch(k_interp_fwd_lp3<4>, fwd_lp3_smem<4>()); break;
+        default: rc = launch(k_interp_fwd_lp3<8>, fwd_lp3_smem<8>()); break;
+      }
+      if (rc) return rc;
+      k_fwd_lp_fix3<<<152, kThreads, 0, s>>>(geo, a3, tmp, (const float2*)(ws + ip.L.off_phase),
+                                             (const float2*)grid, (const int32_t*)(ws + ip.L.off_lfix),
+                                             (float2*)kdata);
+      return check_cuda(cudaGetLastError(), "interp_fwd fix launch");
     }
   }
   auto k = k_interp_fwd<R, D, JC>;
