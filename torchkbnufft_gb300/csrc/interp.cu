@@ -2175,14 +2175,17 @@ __device__ __forceinline__ void fwd_job_lp3(const Geo<float>& geo, const Launch&
   __syncthreads();
   load_patch<float, D>(geo, grid, jc.b * a.C + jc.c0, a.gtot, jc.ncl, kP3Cells, kP3PS, jc.origin, patch);
   __syncthreads();
-  // the patch times Ez[Z - 3] Ey[Y - 3] Ex[X - 3] (E_d[n] at etab[d kLp3En + kLp3E0 + n])
-  for (int e = threadIdx.x; e < CC * kP3Cells; e += kThreads) {
-    const int cl = e / kP3Cells, cell = e - cl * kP3Cells;
+  // the patch times Ez[Z - 3] Ey[Y - 3] Ex[X - 3] (E_d[n] at etab[d kLp3En + kLp3E0 + n]):
+  // thread per cell, every coil plane
+  for (int cell = threadIdx.x; cell < kP3Cells; cell += kThreads) {
     const int Z = cell / (kP3Y * kP3X), rem = cell - Z * (kP3Y * kP3X);
     const int Y = rem / kP3X, X = rem - Y * kP3X;
     const float2 E = cmul<float>(cmul<float>(etab[Z], etab[kLp3En + Y]), etab[2 * kLp3En + X]);
-    float2* pc = patch + cl * kP3PS + cell;
-    *pc = cmul<float>(*pc, E);
+#pragma unroll
+    for (int cl = 0; cl < CC; ++cl) {
+      float2* pc = patch + cl * kP3PS + cell;
+      *pc = cmul<float>(*pc, E);
+    }
   }
   __syncthreads();
   constexpr int PPB = PPW * kWarps;
