@@ -87,10 +87,10 @@ extern "C" {
 #define TKBN_TABLES_LINEAR_PHASE 8   /* every table is |table[k]| exp(i c (k - J*L/2) / L) to
                                         within float rounding, with c = 2 arg(table[J*L/2 + L/2])
                                         (true for KB tables: the fftshift phase is linear in the
-                                        distance); the complex64 2D gather and register adjoint
-                                        then work with real kernel values and apply the phases
-                                        per point and per tile cell or patch cell. Set only
-                                        after checking the tables. */
+                                        distance); the complex64 2D and 3D gathers and register
+                                        adjoints then work with real kernel values and apply the
+                                        phases per point and per tile cell or patch cell. Set
+                                        only after checking the tables. */
 #define TKBN_LAYOUT_FORWARD_ONLY 4   /* layout without the adjoint's per-tile point lists
                                         (smaller workspace, for forward-only callers); an
                                         adjoint on it scans candidates instead (slower). Must
@@ -145,10 +145,11 @@ int tkbn_points_build(const tkbn_geometry* g, const tkbn_points_desc* p, const v
 
 /* ---- interpolation ------------------------------------------------------ */
 /* kdata = interp(grid): gather of J^d neighbours per point, times the fftshift phase.
- * With 2D complex64 J = 6 layouts of 16 x 14 tiles the call fills the workspace's
- * per-point factor scratch as tkbn_interp_adj does (unless TKBN_ADJ_REUSE_FACTORS),
- * and with TKBN_TABLES_LINEAR_PHASE the coil-pair gather reads it, so forward and
- * adjoint calls that share one workspace must be ordered (one stream). */
+ * With 2D complex64 J = 6 layouts of 16 x 14 tiles, and 3D ones of 4 x 8 x 8 tiles with
+ * TKBN_TABLES_LINEAR_PHASE, the call fills the workspace's per-point factor scratch as
+ * tkbn_interp_adj does (unless TKBN_ADJ_REUSE_FACTORS), and with linear-phase tables
+ * the gathers read it, so forward and adjoint calls that share one workspace must be
+ * ordered (one stream). */
 int tkbn_interp_fwd(const tkbn_geometry* g, const tkbn_points_desc* p, const void* workspace,
                     const void* const* tables, const void* grid, int64_t nbatch, int64_t ncoil,
                     void* kdata, void* stream);
