@@ -99,8 +99,8 @@ extern "C" {
 #define TKBN_ADJ_REUSE_FACTORS 16    /* tkbn_interp_fwd / tkbn_interp_adj / tkbn_nufft_fwd /
                                         tkbn_nufft_adj: the workspace still holds the per-point
                                         table factors that an earlier forward or adjoint call on
-                                        it computed, with the same tables (same contents at the
-                                        same addresses) and the same other flags, so this call
+                                        it computed, with tables of the same contents (at any
+                                        addresses) and the same other flags, so this call
                                         does not recompute them. They depend on the trajectory
                                         and the tables only, not on the grid or k-space data.
                                         No other call writes them; a new tkbn_points_build
