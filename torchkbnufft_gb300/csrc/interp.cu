@@ -730,15 +730,15 @@ __global__ void __launch_bounds__(kThreads) k_interp_fwd_pairs(Geo<float> geo, L
 // Exact values of the points the linear-phase gather left out (P = 0 in their
 // records): one thread per (listed point, batch item, coil) gathers its 36
 // taps from the grid with the table factors, after the main pass.
-__global__ void __launch_bounds__(kThreads) k_fwd_lp_fix(Geo<float> geo, Launch a, const float* __restrict__ tm,
-                                                         const float2* __restrict__ ph,
-                                                         const float2* __restrict__ grid,
-                                                         const int32_t* __restrict__ fix,
-                                                         const int32_t* __restrict__ nfix, float2* __restrict__ kdata) {
+// (the body: blocks blk of nblk take (point, batch, coil) triples by a grid stride)
+__device__ __forceinline__ void fwd_lp_fix_body(const Geo<float>& geo, const Launch& a, const float* __restrict__ tm,
+                                                const float2* __restrict__ ph, const float2* __restrict__ grid,
+                                                const int32_t* __restrict__ fix, const int32_t* __restrict__ nfix,
+                                                float2* __restrict__ kdata, int64_t blk, int64_t nblk) {
   constexpr int D = 2, NJ = 6;
   const int64_t nb = a.ntraj == 1 ? a.B : 1;
   const int64_t total = (int64_t)(*nfix) * nb * a.C;
-  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t w = blk * blockDim.x + threadIdx.x; w < total; w += nblk * blockDim.x) {
     const int64_t c = w % a.C, r = w / a.C;
     const int64_t i = fix[r / nb];
     const int32_t val = a.vals[i];
@@ -779,6 +779,14 @@ __global__ void __launch_bounds__(kThreads) k_fwd_lp_fix(Geo<float> geo, Launch 
     }
     kdata[(b * a.C + c) * a.M + m] = cmul<float>(acc, ph[i]);
   }
+}
+
+__global__ void __launch_bounds__(kThreads) k_fwd_lp_fix(Geo<float> geo, Launch a, const float* __restrict__ tm,
+                                                         const float2* __restrict__ ph,
+                                                         const float2* __restrict__ grid,
+                                                         const int32_t* __restrict__ fix,
+                                                         const int32_t* __restrict__ nfix, float2* __restrict__ kdata) {
+  fwd_lp_fix_body(geo, a, tm, ph, grid, fix, nfix, kdata, blockIdx.x, gridDim.x);
 }
 
 template <typename R, int D, int JC>
@@ -1396,15 +1404,16 @@ __global__ void __launch_bounds__(kThreads) k_point_factors2(Geo<float> geo, con
 // Exact contributions of the points the linear-phase adjoint left out: one
 // thread per (listed point, batch item, coil) adds its 36 taps with vector
 // atomics, after the register adjoint has written its tiles.
-__global__ void __launch_bounds__(kThreads) k_adj_lp_fix(Geo<float> geo, OwnLaunch a, const float* __restrict__ tm,
-                                                         const float2* __restrict__ ph,
-                                                         const float2* __restrict__ kdata,
-                                                         const int32_t* __restrict__ fix,
-                                                         const int32_t* __restrict__ nfix, float2* __restrict__ grid) {
+// (the body: blocks blk of nblk take (point, batch, coil) triples by a grid stride)
+__device__ __forceinline__ void adj_lp_fix_body(const Geo<float>& geo, const OwnLaunch& a,
+                                                const float* __restrict__ tm, const float2* __restrict__ ph,
+                                                const float2* __restrict__ kdata, const int32_t* __restrict__ fix,
+                                                const int32_t* __restrict__ nfix, float2* __restrict__ grid,
+                                                int64_t blk, int64_t nblk) {
   constexpr int D = 2, NJ = 6;
   const int64_t nb = a.ntraj == 1 ? a.B : 1;
   const int64_t total = (int64_t)(*nfix) * nb * a.C;
-  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t w = blk * blockDim.x + threadIdx.x; w < total; w += nblk * blockDim.x) {
     const int64_t c = w % a.C, r = w / a.C;
     const int64_t i = fix[r / nb];
     const int32_t val = a.vals[i];
@@ -1444,6 +1453,14 @@ __global__ void __launch_bounds__(kThreads) k_adj_lp_fix(Geo<float> geo, OwnLaun
         atomic_add_global(plane + (int64_t)gy[jy] * geo.K[1] + gx[jx], cmul<float>(vy, hx[jx]));
     }
   }
+}
+
+__global__ void __launch_bounds__(kThreads) k_adj_lp_fix(Geo<float> geo, OwnLaunch a, const float* __restrict__ tm,
+                                                         const float2* __restrict__ ph,
+                                                         const float2* __restrict__ kdata,
+                                                         const int32_t* __restrict__ fix,
+                                                         const int32_t* __restrict__ nfix, float2* __restrict__ grid) {
+  adj_lp_fix_body(geo, a, tm, ph, kdata, fix, nfix, grid, blockIdx.x, gridDim.x);
 }
 
 // Footprint starts of a 16 x 14 tile with J = 6: row offsets -5 .. 15 (21),
@@ -2550,7 +2567,10 @@ struct RaggedProb {
   cplx<R>* kdata;
   int64_t nitems;
   int vec_ok;
-  int pad_;
+  int lp;                 // linear-phase problem: the register adjoint and coil-pair gather in the real form
+  const float2* etab;     // lp: {Ey, Ex} in the problem's workspace
+  const int32_t* fix;     // lp: the left-out points and their count
+  const int32_t* nfix;
 };
 
 template <typename T>
@@ -2624,6 +2644,64 @@ __global__ void __launch_bounds__(kThreads, 3) k_ragged_adj_reg(const RaggedProb
     }
     reg_job<CC>(sp.geo, sp.o, sp.tm, sp.ph, sp.kdata, sp.grid, sp.vec_ok, pj.y, smem_raw, nullptr);
   }
+}
+
+// Linear-phase problems (RaggedProb::lp): the same per-job code in the real
+// form; a CTA also copies the problem's E tables when the problem changes.
+template <int CC>
+__global__ void __launch_bounds__(kThreads, 3) k_ragged_fwd_pairs_lp(const RaggedProb<float>* __restrict__ probs,
+                                                                  const int2* __restrict__ jobs, int64_t njobs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) RaggedProb<float> sp;
+  __shared__ float2 setab[kLpEy + kLpEx];
+  float2* patch = reinterpret_cast<float2*>(smem_raw);
+  int cur = -1;
+  for (int64_t g = blockIdx.x; g < njobs; g += gridDim.x) {
+    const int2 pj = jobs[g];
+    if (pj.x != cur) {
+      __syncthreads();
+      load_desc(&sp, probs + pj.x);
+      if (threadIdx.x < kLpEy + kLpEx) setab[threadIdx.x] = probs[pj.x].etab[threadIdx.x];
+      __syncthreads();
+      cur = pj.x;
+    }
+    fwd_job_pairs<CC, true>(sp.geo, sp.a, sp.tm, sp.ph, sp.grid, sp.kdata, pj.y, sp.nitems, patch,
+                            reinterpret_cast<const float*>(sp.o.pfac), setab);
+  }
+}
+
+template <int CC>
+__global__ void __launch_bounds__(kThreads, 3) k_ragged_adj_reg_lp(const RaggedProb<float>* __restrict__ probs,
+                                                                   const int2* __restrict__ jobs, int64_t njobs) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(16) RaggedProb<float> sp;
+  __shared__ float2 setab[kLpEy + kLpEx];
+  int cur = -1;
+  for (int64_t g = blockIdx.x; g < njobs; g += gridDim.x) {
+    const int2 pj = jobs[g];
+    if (pj.x != cur) {
+      __syncthreads();
+      load_desc(&sp, probs + pj.x);
+      if (threadIdx.x < kLpEy + kLpEx) setab[threadIdx.x] = probs[pj.x].etab[threadIdx.x];
+      __syncthreads();
+      cur = pj.x;
+    }
+    reg_job<CC, true>(sp.geo, sp.o, sp.tm, sp.ph, sp.kdata, sp.grid, sp.vec_ok, pj.y, smem_raw, nullptr, setab);
+  }
+}
+
+// The exact passes of the linear-phase problems' left-out points, after the
+// merged launches: blockIdx.y picks the problem (its index in lp_probs).
+__global__ void __launch_bounds__(kThreads) k_ragged_fwd_fix(const RaggedProb<float>* __restrict__ probs,
+                                                             const int* __restrict__ lp_probs) {
+  const RaggedProb<float>& P = probs[lp_probs[blockIdx.y]];
+  fwd_lp_fix_body(P.geo, P.a, P.tm, P.ph, P.grid, P.fix, P.nfix, P.kdata, blockIdx.x, gridDim.x);
+}
+
+__global__ void __launch_bounds__(kThreads) k_ragged_adj_fix(const RaggedProb<float>* __restrict__ probs,
+                                                             const int* __restrict__ lp_probs) {
+  const RaggedProb<float>& P = probs[lp_probs[blockIdx.y]];
+  adj_lp_fix_body(P.geo, P.o, P.tm, P.ph, P.kdata, P.fix, P.nfix, P.grid, blockIdx.x, gridDim.x);
 }
 
 template <typename R, int D, int JC>
@@ -3257,9 +3335,13 @@ struct tkbn_ragged_plan_s {
   int64_t nprob;
   void* probs;  // RaggedProb<R>[nprob] on the device
   // fwd_pairs[k], reg_jobs[k]: jobs of problems with 2 << k coils per job
+  // (the _lp lists: linear-phase problems)
   int2 *fwd_jobs, *fwd_pairs[4], *reg_jobs[4], *own_jobs, *zero_jobs;
-  int64_t n_fwd, n_fwd_pairs[4], n_reg[4], n_own, n_zero;
+  int2 *fwd_pairs_lp[4], *reg_jobs_lp[4];
+  int64_t n_fwd, n_fwd_pairs[4], n_reg[4], n_own, n_zero, n_fwd_pairs_lp[4], n_reg_lp[4];
   size_t smem_fwd, smem_fwd_pairs[4], smem_own;
+  int* lp_probs;  // the linear-phase problems, for the exact passes
+  int64_t n_lp;
 };
 
 namespace tkbn_host {
@@ -3290,7 +3372,8 @@ int upload_jobs(const std::vector<JobRec>& v, int2** dev) {
 template <typename R, int D, int JC>
 int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P) {
   std::vector<RaggedProb<R>> desc((size_t)n);
-  std::vector<JobRec> fwd, fwdp[4], reg[4], own, zero;
+  std::vector<JobRec> fwd, fwdp[4], reg[4], own, zero, fwdp_lp[4], reg_lp[4];
+  std::vector<int> lp_list;
   P->smem_fwd = 0;
   P->smem_own = 0;
   for (int k = 0; k < 4; ++k) P->smem_fwd_pairs[k] = 0;
@@ -3315,6 +3398,11 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
     d.kdata = (cplx<R>*)r.kdata;
     d.nitems = hdr[0];
     d.vec_ok = ((uintptr_t)r.grid % 16 == 0) && (r.geom.grid_size[D - 1] % 2 == 0);
+    // linear-phase problems (16 x 14 register-adjoint layouts, linear-phase
+    // tables, not deterministic) run both directions in the real form
+    bool lpq = false;
+    if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6)
+      lpq = lp_factors(ip) && ip.a.n > 0 && reg_eligible<R, D, JC>(ip, make_own(ip, ws, D));
     // forward jobs: item i % nitems of coil chunk i / nitems; 2D complex64
     // J = 6 problems with 2 or more coils per job take the coil-pair gather
     const bool pairs = std::is_same<R, float>::value && D == 2 && JC == 6 && ip.a.Cc >= 2;
@@ -3332,7 +3420,7 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
                            "read work items")))
         return rc;
       for (int64_t j = 0; j < hdr[0] * ip.a.ncc; ++j)
-        (pairs ? fwdp[pk] : fwd).push_back({items[(size_t)(j % hdr[0])].len, (int)q, (int)j});
+        (pairs ? (lpq ? fwdp_lp[pk] : fwdp[pk]) : fwd).push_back({items[(size_t)(j % hdr[0])].len, (int)q, (int)j});
     }
     // adjoint jobs: sub-job j / ncc of coil chunk j % ncc
     if (!ip.L.owned_ok || ip.L.span.ncombo > max_combo<D>())
@@ -3346,13 +3434,24 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
     if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
       if (use_reg && ip.L.pfac && ip.a.n > 0) {
         // the plan's trajectories and tables are fixed: the register adjoint's
-        // per-point factors are computed once, into the problem's workspace
-        float2* pf = (float2*)const_cast<char*>(ws + ip.L.off_pfac);
+        // per-point factors (linear-phase records, with the E tables and the
+        // left-out list, for lp problems) are computed once, into the problem's workspace
+        const PointFactors f = point_factors_of(ip, ws);
         const int64_t nb = (2 * ip.a.n + kThreads - 1) / kThreads;
-        k_point_factors2<false><<<(int)(nb < 152 * 16 ? nb : 152 * 16), kThreads>>>(
-            d.geo, d.tm, d.ph, ip.a.n, pf, nullptr, nullptr, nullptr);
+        const int gb = (int)(nb < 152 * 16 ? nb : 152 * 16);
+        if (lpq) {
+          if ((rc = check_cuda(cudaMemset(f.nfix, 0, sizeof(int32_t)), "reset left-out count"))) return rc;
+          k_point_factors2<true><<<gb, kThreads>>>(d.geo, d.tm, d.ph, ip.a.n, f.pf, f.et, f.fix, f.nfix);
+          d.lp = 1;
+          d.etab = f.et;
+          d.fix = f.fix;
+          d.nfix = f.nfix;
+          lp_list.push_back((int)q);
+        } else {
+          k_point_factors2<false><<<gb, kThreads>>>(d.geo, d.tm, d.ph, ip.a.n, f.pf, nullptr, nullptr, nullptr);
+        }
         if ((rc = check_cuda(cudaGetLastError(), "ragged factor pre-pass"))) return rc;
-        d.o.pfac = pf;
+        d.o.pfac = f.pf;
       }
     }
     if (!use_reg) {
@@ -3363,7 +3462,7 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
     const int rk = reg_cc(d.o.Cc) == 2 ? 0 : (reg_cc(d.o.Cc) == 4 ? 1 : (reg_cc(d.o.Cc) == 8 ? 2 : 3));
     for (int64_t j = 0; j < hdr[1] * ip.a.ncc; ++j) {
       const Item& it = sj[(size_t)(j / ip.a.ncc)];
-      (use_reg ? reg[rk] : own).push_back({it.len, (int)q, (int)j});
+      (use_reg ? (lpq ? reg_lp[rk] : reg[rk]) : own).push_back({it.len, (int)q, (int)j});
     }
     for (int64_t j = 0; j < hdr[1]; ++j)
       if (sj[(size_t)j].pad && sj[(size_t)j].start == 0) zero.push_back({sj[(size_t)j].len, (int)q, (int)j});
@@ -3373,6 +3472,8 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
   lpt_sort(fwd);
   for (auto& v : fwdp) lpt_sort(v);
   for (auto& v : reg) lpt_sort(v);
+  for (auto& v : fwdp_lp) lpt_sort(v);
+  for (auto& v : reg_lp) lpt_sort(v);
   lpt_sort(own);
   int rc = check_cuda(cudaMalloc(&P->probs, desc.size() * sizeof(RaggedProb<R>)), "ragged descriptors");
   if (rc) return rc;
@@ -3385,8 +3486,20 @@ int ragged_build(const tkbn_ragged_problem* pr, int64_t n, tkbn_ragged_plan_s* P
   for (int k = 0; k < 4; ++k) {
     if ((rc = upload_jobs(reg[k], &P->reg_jobs[k]))) return rc;
     if ((rc = upload_jobs(fwdp[k], &P->fwd_pairs[k]))) return rc;
+    if ((rc = upload_jobs(reg_lp[k], &P->reg_jobs_lp[k]))) return rc;
+    if ((rc = upload_jobs(fwdp_lp[k], &P->fwd_pairs_lp[k]))) return rc;
     P->n_reg[k] = (int64_t)reg[k].size();
     P->n_fwd_pairs[k] = (int64_t)fwdp[k].size();
+    P->n_reg_lp[k] = (int64_t)reg_lp[k].size();
+    P->n_fwd_pairs_lp[k] = (int64_t)fwdp_lp[k].size();
+  }
+  P->n_lp = (int64_t)lp_list.size();
+  P->lp_probs = nullptr;
+  if (P->n_lp > 0) {
+    if ((rc = check_cuda(cudaMalloc((void**)&P->lp_probs, lp_list.size() * sizeof(int)), "ragged lp list"))) return rc;
+    if ((rc = check_cuda(cudaMemcpy(P->lp_probs, lp_list.data(), lp_list.size() * sizeof(int), cudaMemcpyHostToDevice),
+                         "ragged lp list upload")))
+      return rc;
   }
   P->n_fwd = (int64_t)fwd.size();
   P->n_own = (int64_t)own.size();
@@ -3411,13 +3524,36 @@ int ragged_fwd_t(const tkbn_ragged_plan_s* P, cudaStream_t s) {
       });
       if (rc) return rc;
     }
+    for (int k = 0; k < 4; ++k) {
+      if (P->n_fwd_pairs_lp[k] == 0) continue;
+      rc = with_cc(2 << k, [&](auto ccv) {
+        constexpr int CC = decltype(ccv)::value;
+        int blocks;
+        int r = resident_blocks(k_ragged_fwd_pairs_lp<CC>, P->smem_fwd_pairs[k], P->n_fwd_pairs_lp[k], &blocks);
+        if (r) return r;
+        k_ragged_fwd_pairs_lp<CC><<<blocks, kThreads, P->smem_fwd_pairs[k], s>>>(
+            (const RaggedProb<float>*)P->probs, P->fwd_pairs_lp[k], P->n_fwd_pairs_lp[k]);
+        return check_cuda(cudaGetLastError(), "ragged interp_fwd launch");
+      });
+      if (rc) return rc;
+    }
   }
-  if (P->n_fwd == 0) return TKBN_OK;
-  int blocks;
-  rc = resident_blocks(k_ragged_fwd<R, D, JC>, P->smem_fwd, P->n_fwd, &blocks);
-  if (rc) return rc;
-  k_ragged_fwd<R, D, JC><<<blocks, kThreads, P->smem_fwd, s>>>((const RaggedProb<R>*)P->probs, P->fwd_jobs, P->n_fwd);
-  return check_cuda(cudaGetLastError(), "ragged interp_fwd launch");
+  if (P->n_fwd > 0) {
+    int blocks;
+    rc = resident_blocks(k_ragged_fwd<R, D, JC>, P->smem_fwd, P->n_fwd, &blocks);
+    if (rc) return rc;
+    k_ragged_fwd<R, D, JC><<<blocks, kThreads, P->smem_fwd, s>>>((const RaggedProb<R>*)P->probs, P->fwd_jobs,
+                                                                 P->n_fwd);
+    if ((rc = check_cuda(cudaGetLastError(), "ragged interp_fwd launch"))) return rc;
+  }
+  if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
+    if (P->n_lp > 0) {
+      k_ragged_fwd_fix<<<dim3(16, (unsigned)P->n_lp), kThreads, 0, s>>>((const RaggedProb<float>*)P->probs,
+                                                                          P->lp_probs);
+      return check_cuda(cudaGetLastError(), "ragged interp_fwd fix launch");
+    }
+  }
+  return TKBN_OK;
 }
 
 template <typename R, int D, int JC>
@@ -3442,12 +3578,32 @@ int ragged_adj_t(const tkbn_ragged_plan_s* P, cudaStream_t s) {
       });
       if (rc) return rc;
     }
+    for (int k = 0; k < 4; ++k) {
+      if (P->n_reg_lp[k] == 0) continue;
+      rc = with_cc(2 << k, [&](auto ccv) {
+        constexpr int CC = decltype(ccv)::value;
+        int blocks;
+        int r = resident_blocks(k_ragged_adj_reg_lp<CC>, reg_smem(CC), P->n_reg_lp[k], &blocks);
+        if (r) return r;
+        k_ragged_adj_reg_lp<CC><<<blocks, kThreads, reg_smem(CC), s>>>(probs, P->reg_jobs_lp[k], P->n_reg_lp[k]);
+        return check_cuda(cudaGetLastError(), "ragged interp_adj launch");
+      });
+      if (rc) return rc;
+    }
   }
   if (P->n_own > 0) {
     int blocks;
     if ((rc = resident_blocks(k_ragged_adj_own<R, D, JC>, P->smem_own, P->n_own, &blocks))) return rc;
     k_ragged_adj_own<R, D, JC><<<blocks, kThreads, P->smem_own, s>>>(probs, P->own_jobs, P->n_own);
     if ((rc = check_cuda(cudaGetLastError(), "ragged interp_adj launch"))) return rc;
+  }
+  if constexpr (std::is_same<R, float>::value && D == 2 && JC == 6) {
+    // the left-out points' exact contributions, after every tile is written
+    if (P->n_lp > 0) {
+      k_ragged_adj_fix<<<dim3(16, (unsigned)P->n_lp), kThreads, 0, s>>>((const RaggedProb<float>*)P->probs,
+                                                                          P->lp_probs);
+      return check_cuda(cudaGetLastError(), "ragged interp_adj fix launch");
+    }
   }
   return TKBN_OK;
 }
@@ -3495,7 +3651,10 @@ int ragged_plan_destroy(tkbn_ragged_plan p) {
   for (int k = 0; k < 4; ++k) {
     cudaFree(p->reg_jobs[k]);
     cudaFree(p->fwd_pairs[k]);
+    cudaFree(p->reg_jobs_lp[k]);
+    cudaFree(p->fwd_pairs_lp[k]);
   }
+  cudaFree(p->lp_probs);
   cudaFree(p->own_jobs);
   cudaFree(p->zero_jobs);
   delete p;
