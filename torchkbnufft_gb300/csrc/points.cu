@@ -79,12 +79,15 @@ __global__ void k_fill_items(const int32_t* __restrict__ counts, const int32_t* 
 
 // Work items are ordered longest first, so that a grid-stride walk over them
 // (CTA k takes items k, k + grid, ...) schedules the heavy k-space-centre tiles
-// in the first wave (longest-processing-time-first).
+// in the first wave (longest-processing-time-first). Items of at most `light`
+// points share one key, so the stable sort keeps them in tile order after the
+// heavy ones: CTAs that run at the same time then stage neighbouring tiles,
+// whose halos overlap in L2 (3D layouts; light = 0 orders every item by length).
 __global__ void k_item_keys(const Item* __restrict__ items, const int64_t* __restrict__ hdr, int64_t max_items,
-                            int chunk, uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+                            int chunk, int light, uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
   const int64_t nitems = hdr[0];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < max_items; i += (int64_t)gridDim.x * blockDim.x) {
-    keys[i] = i < nitems ? (uint32_t)(chunk - items[i].len) : (uint32_t)(chunk + 1);
+    keys[i] = i < nitems ? (uint32_t)(chunk - max(items[i].len, light)) : (uint32_t)(chunk + 1);
     vals[i] = (int32_t)i;
   }
 }
@@ -661,7 +664,10 @@ static int build_impl(const tkbn_geometry* g, const tkbn_points_desc* p, const P
     return set_error(TKBN_ERR_CUDA, "scan failed");
   k_fill_items<<<blocks_for(L.nkeys), threads, 0, s>>>(counts, tile_off, nit, item_off, L.nkeys, L.chunk, items_raw,
                                                        hdr);
-  k_item_keys<<<blocks_for(L.max_items), threads, 0, s>>>(items_raw, hdr, L.max_items, L.chunk, ikeys_in, ivals_in);
+  // 3D: items of up to 256 points stay in tile order (their 9 x 13 x 13 patch halos are reread from L2)
+  const int light = g->ndim == 3 ? (L.chunk < 256 ? L.chunk : 256) : 0;
+  k_item_keys<<<blocks_for(L.max_items), threads, 0, s>>>(items_raw, hdr, L.max_items, L.chunk, light, ikeys_in,
+                                                          ivals_in);
   tb = L.cub_bytes;
   if (cub::DeviceRadixSort::SortPairs(cubtmp, tb, ikeys_in, ikeys, ivals_in, ivals, (int)L.max_items, 0,
                                       L.item_key_bits, s) != cudaSuccess)
