@@ -1268,6 +1268,68 @@ int fft3d_inverse(const Fft3d& p, int dtype, int64_t B, int64_t C, void* grid, c
                            : inverse3_r<double>(p, B, C, grid, smaps, sb, scaling, scale, out, st);
 }
 
+// Toeplitz filter on a 3D grid: x rows and y columns forward, the z columns
+// transformed, multiplied by the kernel and transformed back in one pass,
+// then y columns and x rows inverse (with the crop and coil sum).
+template <typename R>
+static int toeplitz3_r(const Fft3d& p, int64_t B, int64_t C, int64_t ci, const void* image, const void* kernel,
+                       int64_t kbatch, int by_channel, const void* smaps, int64_t sb, double scale, void* grid,
+                       void* out, cudaStream_t st) {
+  auto need_ct = [] { return set_error(TKBN_ERR_UNSUPPORTED, "3D fused FFT needs compile-time plan sizes"); };
+  int rc = with_size<R>(p.K[2], [&](auto nc) {
+    if constexpr (decltype(nc)::value == 0) {
+      return need_ct();
+    } else {
+      return rows_pad_r<R, decltype(nc)::value>(rows3(p), kNoPlan, p.tw[2], B, C, ci, image, smaps, sb, nullptr,
+                                                scale, grid, st);
+    }
+  });
+  if (rc) return rc;
+  rc = with_size<R>(p.K[1], [&](auto nc) {
+    if constexpr (decltype(nc)::value == 0) {
+      return need_ct();
+    } else {
+      return cols_r<R, decltype(nc)::value>(cols_y3(p), kNoPlan, p.tw[1], kColFwd, B * C * p.N[0], C, nullptr, 1, 0,
+                                            1.0, grid, st);
+    }
+  });
+  if (rc) return rc;
+  rc = with_size<R>(p.K[0], [&](auto nc) {
+    if constexpr (decltype(nc)::value == 0) {
+      return need_ct();
+    } else {
+      return cols_r<R, decltype(nc)::value>(cols_z3(p), kNoPlan, p.tw[0], kColToep, B * C, C, kernel, kbatch,
+                                            by_channel, scale, grid, st);
+    }
+  });
+  if (rc) return rc;
+  rc = with_size<R>(p.K[1], [&](auto nc) {
+    if constexpr (decltype(nc)::value == 0) {
+      return need_ct();
+    } else {
+      return cols_r<R, decltype(nc)::value>(cols_y3(p), kNoPlan, p.tw[1], kColInv, B * C * p.N[0], C, nullptr, 1, 0,
+                                            1.0, grid, st);
+    }
+  });
+  if (rc) return rc;
+  return with_size<R>(p.K[2], [&](auto nc) {
+    if constexpr (decltype(nc)::value == 0) {
+      return need_ct();
+    } else {
+      return rows_crop_r<R, decltype(nc)::value>(rows3(p), kNoPlan, p.tw[2], B, C, grid, smaps, sb, nullptr, 1.0,
+                                                 out, st);
+    }
+  });
+}
+
+int fft3d_toeplitz(const Fft3d& p, int dtype, int64_t B, int64_t C, int64_t ci, const void* image,
+                   const void* kernel, int64_t kbatch, int by_channel, const void* smaps, int64_t sb, double scale,
+                   void* grid, void* out, cudaStream_t st) {
+  return dtype == TKBN_C64
+             ? toeplitz3_r<float>(p, B, C, ci, image, kernel, kbatch, by_channel, smaps, sb, scale, grid, out, st)
+             : toeplitz3_r<double>(p, B, C, ci, image, kernel, kbatch, by_channel, smaps, sb, scale, grid, out, st);
+}
+
 int fft2d_toeplitz(const Fft2d& p, int dtype, int64_t B, int64_t C, int64_t ci, const void* image,
                    const void* kernel, int64_t kbatch, int by_channel, const void* smaps, int64_t sb, double scale,
                    void* grid, void* out, cudaStream_t st) {

@@ -82,6 +82,10 @@ int fft3d_forward(const Fft3d& p, int dtype, int64_t B, int64_t C, int64_t ci, c
 // out = [sum_c conj(smaps) *] conj(scaling) * scale * crop(IFFT3(grid)); grid is overwritten
 int fft3d_inverse(const Fft3d& p, int dtype, int64_t B, int64_t C, void* grid, const void* smaps, int64_t sb,
                   const void* scaling, double scale, void* out, cudaStream_t st);
+// out = [sum_c conj(smaps) *] crop(IFFT3(kernel * scale * FFT3(pad([smaps *] image) * scale)))
+int fft3d_toeplitz(const Fft3d& p, int dtype, int64_t B, int64_t C, int64_t ci, const void* image,
+                   const void* kernel, int64_t kbatch, int by_channel, const void* smaps, int64_t sb, double scale,
+                   void* grid, void* out, cudaStream_t st);
 // out = [sum_c conj(smaps) *] crop(IFFT2(kernel * scale * FFT2(pad([smaps *] image) * scale)))
 int fft2d_toeplitz(const Fft2d& p, int dtype, int64_t B, int64_t C, int64_t ci, const void* image,
                    const void* kernel, int64_t kbatch, int by_channel, const void* smaps, int64_t sb, double scale,

@@ -25,8 +25,8 @@
 
 // A plan is either the fused 2D passes of fft2d.cu (2D grids whose sizes
 // factor into radices 2..15 and fit shared memory) or a cuFFT plan. 3D grids
-// whose three sizes have compile-time plans also get the fused passes (fused3)
-// for the forward and inverse stages; their Toeplitz filter keeps cuFFT.
+// whose three sizes have compile-time plans get the same passes per
+// dimension (fused3) for every stage, and no cuFFT plan.
 struct tkbn_fft_plan_s {
   cufftHandle handle;
   int ndim;
@@ -254,7 +254,9 @@ int fft_plan_create(const tkbn_geometry* g, int64_t B, int64_t C, tkbn_fft_plan*
         delete p;
         return rc;
       }
-      p->fused3 = true;  // the cuFFT plan below serves the Toeplitz filter
+      p->fused3 = true;  // every 3D stage runs on the fused passes: no cuFFT plan
+      *out = p;
+      return TKBN_OK;
     }
   }
   if (g->ndim == 2 && g->grid_size[0] <= tkbn::kFftMaxN && g->grid_size[1] <= tkbn::kFftMaxN &&
@@ -281,8 +283,6 @@ int fft_plan_create(const tkbn_geometry* g, int64_t B, int64_t C, tkbn_fft_plan*
   }
   int rc = check_cufft(cufftCreate(&p->handle), "cufftCreate");
   if (rc) {
-    if (p->fused3)
-      for (int d = 0; d < 3; ++d) cudaFree(p->f3.tw[d]);
     delete p;
     return rc;
   }
@@ -292,8 +292,6 @@ int fft_plan_create(const tkbn_geometry* g, int64_t B, int64_t C, tkbn_fft_plan*
                    "cufftMakePlanMany64");
   if (rc) {
     cufftDestroy(p->handle);
-    if (p->fused3)
-      for (int d = 0; d < 3; ++d) cudaFree(p->f3.tw[d]);
     delete p;
     return rc;
   }
@@ -308,14 +306,14 @@ int fft_plan_destroy(tkbn_fft_plan p) {
     rc = check_cuda(cudaFree(p->f2.tw0), "free twiddles");
     const int rc1 = check_cuda(cudaFree(p->f2.tw1), "free twiddles");
     if (!rc) rc = rc1;
+  } else if (p->fused3) {
+    rc = TKBN_OK;
+    for (int d = 0; d < 3; ++d) {
+      const int rc1 = check_cuda(cudaFree(p->f3.tw[d]), "free twiddles");
+      if (!rc) rc = rc1;
+    }
   } else {
     rc = check_cufft(cufftDestroy(p->handle), "cufftDestroy");
-    if (p->fused3) {
-      for (int d = 0; d < 3; ++d) {
-        const int rc1 = check_cuda(cudaFree(p->f3.tw[d]), "free twiddles");
-        if (!rc) rc = rc1;
-      }
-    }
   }
   delete p;
   return rc;
@@ -447,6 +445,9 @@ int toep_apply(const tkbn_geometry* g, tkbn_fft_plan plan, const void* image, co
   if (norm != TKBN_NORM_NONE && norm != TKBN_NORM_ORTHO) return set_error(TKBN_ERR_INVALID, "Only option for norm is 'ortho'.");
   const double sc = ortho_scale(s, norm);
   const int64_t ci = smaps ? 1 : C;
+  if (plan->fused3)
+    return fft3d_toeplitz(fused3_for(plan, s), g->dtype, B, C, ci, image, kernel, kbatch, by_channel, smaps,
+                          smaps_batch, sc, grid, out, st);
   if (plan->fused)
     return fft2d_toeplitz(fused_for(plan, s), g->dtype, B, C, ci, image, kernel, kbatch, by_channel, smaps,
                           smaps_batch, sc, grid, out, st);
