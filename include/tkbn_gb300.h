@@ -230,7 +230,9 @@ int tkbn_ragged_interp_fwd(tkbn_ragged_plan plan, void* stream);
 int tkbn_ragged_interp_adj(tkbn_ragged_plan plan, void* stream);
 
 /* ---- FFT stages --------------------------------------------------------- */
-/* cuFFT plan for nbatch*ncoil transforms of size grid_size (in place). */
+/* Plan for nbatch*ncoil transforms of size grid_size: the fused passes' twiddle
+ * tables when every grid size has a compile-time plan (2D and 3D), else a cuFFT
+ * plan (in place on the grid). */
 int tkbn_fft_plan_create(const tkbn_geometry* g, int64_t nbatch, int64_t ncoil, tkbn_fft_plan* plan);
 int tkbn_fft_plan_destroy(tkbn_fft_plan plan);
 
