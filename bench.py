@@ -760,6 +760,12 @@ def run_config(args):
         with torch.no_grad():
             ms = timed(lambda: adj(fwd(x, omega, smaps=smaps), omega, smaps=smaps), args.steps, args.warmup)
             extra = {"stage_ms": stage_times(fwd, omega, x, smaps, args.steps, args.warmup)}
+            if w == "kooshball":
+                # the Toeplitz normal operator (ToepNufft) on the same image, maps and trajectory
+                kern = tkbn.calc_toeplitz_kernel(omega, im)
+                toep = tkbn.ToepNufft()
+                extra["toep_nufft_ms"] = round(timed(lambda: toep(x, kern, smaps=smaps), args.steps, args.warmup), 4)
+                del kern
     parity = config_parity(w, fwd, adj, x, omega, smaps, om, im)
     line = {
         "metric": f"NU points*coils/s ({w})", "value": work / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
