@@ -368,6 +368,7 @@ __host__ __device__ constexpr int ct_min_blocks() {
 //             inverse FFT, rows < N0 written.
 enum ColMode { kColFwd = 0, kColInv = 1, kColToep = 2 };
 constexpr int kColWidth = 8;  // columns per unit of the compile-time column passes
+constexpr int64_t kToepPlaneFastBytes = 32ll << 20;  // see k_fft_cols_io
 
 // Transforms that read their first stage straight from global memory and
 // write their last stage straight back (compile-time plans): four passes
@@ -489,9 +490,15 @@ __global__ void __launch_bounds__(ct_threads<NC>(), FW == kFftF ? ct_min_blocks<
   const int64_t units = planes * ngrp;
   const int nload = MODE == kColInv ? NC : s.N0;
   const int nstore = MODE == kColFwd ? NC : s.N0;
+  // A Toeplitz kernel plane larger than kToepPlaneFastBytes (a 3D kernel) is
+  // read by every plane that shares it: with the planes of one column group
+  // run back to back, its columns come from DRAM once and from L2 for the
+  // other planes. Smaller kernels stay in L2 in either order.
+  const bool plane_fast = MODE == kColToep && gtot * (int64_t)sizeof(cplx<R>) > kToepPlaneFastBytes;
   for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
-    const int64_t plane = u / ngrp;
-    const int col = (int)(u - plane * ngrp) * F + f;
+    const int64_t plane = plane_fast ? u % planes : u / ngrp;
+    const int64_t grp = plane_fast ? u / planes : u - plane * ngrp;
+    const int col = (int)grp * F + f;
     const bool cok = col < K1;
     const int64_t gplane = s.pk == s.pt ? plane : (plane / s.pk) * s.pt + plane % s.pk;
     cplx<R>* g = grid + gplane * gtot + (cok ? col : 0);
