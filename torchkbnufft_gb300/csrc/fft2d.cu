@@ -470,12 +470,26 @@ struct NoIo {
   }
 };
 
+// Resident CTAs asked of the register allocator by the column pass. With
+// kColWidth columns per unit, single precision: 2 (up to 128 registers) in
+// general; for 256-point columns (256 threads, 32 KB of shared memory) the
+// pass is bound by global-load latency at 2 CTAs per SM, so it asks for 4
+// (64 registers) in the forward and inverse modes and 3 (80 registers) in the
+// Toeplitz mode, the most that compile without spills.
+template <typename R, int MODE, int NC, int FW>
+__host__ __device__ constexpr int cols_io_min_blocks() {
+  if (FW == kFftF) return ct_min_blocks<NC, R>();
+  if (sizeof(R) != 4) return 1;
+  if (NC == 256) return MODE == kColToep ? 3 : 4;
+  return 2;
+}
+
 // Column pass with compile-time plan NC: FW adjacent columns of one plane
 // per unit (every global access is a run of FW complex values), transformed
 // between global memory and two shared buffers by P * kFftF / FW threads
 // per column.
 template <typename R, int MODE, int NC, int FW>
-__global__ void __launch_bounds__(ct_threads<NC>(), FW == kFftF ? ct_min_blocks<NC, R>() : (sizeof(R) == 4 ? 2 : 1))
+__global__ void __launch_bounds__(ct_threads<NC>(), cols_io_min_blocks<R, MODE, NC, FW>())
     k_fft_cols_io(Fft2dShape s, const cplx<R>* __restrict__ tw, int64_t planes, int64_t C,
                   const cplx<R>* __restrict__ kernel, int64_t kbatch, int by_channel, R scale,
                   cplx<R>* __restrict__ grid) {
