@@ -421,9 +421,9 @@ void default_tiles(const tkbn_geometry* g, int tile[3], int* chunk) {
   if (g->ndim == 1) {
     tile[0] = 128;
   } else if (g->ndim == 2) {
-    // 14 x 16 cells: a 19 x 21 forward patch of 16 complex64 coil planes is
-    // 51 KB, so four 256-thread CTAs fit an SM; 14 rows split evenly enough
-    // over the 8 warps of the adjoint's row ownership.
+    // 16 rows x 14 columns: a 21 x 19 forward patch of 16 complex64 coil
+    // planes is 51 KB, so four 256-thread CTAs fit an SM; the register
+    // adjoint's 16-coil jobs give each of the 8 warps two of the 16 rows.
     tile[0] = 16;
     tile[1] = 14;
   } else {
